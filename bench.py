@@ -1,0 +1,387 @@
+"""Benchmark: fwd+bwd Mpix/s of rasterize -> interpolate -> antialias -> loss.
+
+Workload (N=1, one GB300): the single-mesh full-gradient configuration --
+icosphere with 5 subdivisions (10242 vertices, 20480 triangles, radius 0.8),
+every vertex displaced radially by N(0, 0.02) (seed 0), one 1024x1024 view
+from (0, 0, 3.2) (fov 30, near 0.1, far 100), 8 float32 attribute channels
+(unit vertex normal 3, uv 2 ~ U(0,1), colour 3 ~ U(0,1)), L1 loss to a seeded
+U(0,1) target, gradients w.r.t. vertex positions and attributes.  One step =
+clip transform, rasterize, interpolate, antialias, loss, backward.
+
+Lines printed (rank 0, one JSON line):
+  value       Mpix/s with inputs resident in HBM, CUDA-event timed per step,
+              L2 flushed (256 MiB write) between steps outside the events;
+  e2e         the same step through the public API with the parameters copied
+              from pinned host memory and loss + gradients copied back, inside
+              the timed region;
+  roofline    dominant kernel (entry point) of the step: algorithmic bytes /
+              CUDA-event time vs the measured HBM copy bandwidth;
+  cpu_baseline  the CPU oracle (a restatement of the path, all host threads)
+              on a bounded sample of the same workload.
+
+``--impl reference`` times the CPU implementation of the path (the oracle
+port: the reference's own rasteriser is an external CUDA package that does
+not exist on this machine) with all host threads on the same workload.
+``--gpus N`` under torchrun runs N replicas (weak scaling; no collective on
+the data path).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+H = W = 1024
+C = 8
+METRIC = "fwd+bwd Mpix/s (rasterize->interpolate->antialias->L1 loss, backward to positions and attributes)"
+UNIT = "Mpix/s"
+
+
+def make_workload(seed=0):
+    from diffrp_gb300 import synthetic as S
+    v, f = S.displaced_icosphere(5, 0.8, 0.02, seed)
+    rng = np.random.default_rng(seed + 1)
+    # unit vertex normals (area-weighted), uv, colour
+    fn = np.cross(v[f[:, 1]] - v[f[:, 0]], v[f[:, 2]] - v[f[:, 0]])
+    vn = np.zeros_like(v)
+    for k in range(3):
+        np.add.at(vn, f[:, k], fn)
+    vn /= np.linalg.norm(vn, axis=1, keepdims=True)
+    attr = np.concatenate([vn, rng.uniform(0, 1, (len(v), 2)), rng.uniform(0, 1, (len(v), 3))], 1)
+    attr = attr.astype(np.float32)
+    mvp = S.perspective(30.0, H, W, 0.1, 100.0).astype(np.float64) @ \
+        S.view_matrix(S.lookat_pose((0.0, 0.0, 3.2))).astype(np.float64)
+    target = rng.uniform(0, 1, (1, H, W, C)).astype(np.float32)
+    return v.astype(np.float32), f, attr, mvp.astype(np.float32), target
+
+
+class Step:
+    """One fwd+bwd through the drop-in nvdiffrast API (diffrp_gb300.nvdr)."""
+
+    def __init__(self, dev, f, mvp, target):
+        import torch
+        from diffrp_gb300 import nvdr as dr
+        self.dr = dr
+        self.torch = torch
+        self.ctx = dr.RasterizeCudaContext(dev)
+        self.tri = torch.from_numpy(f).to(dev)
+        self.mvp = torch.from_numpy(mvp).to(dev)
+        self.target = torch.from_numpy(target).to(dev)
+        self.topo = dr.antialias_construct_topology_hash(self.tri)
+
+    def __call__(self, verts, attr):
+        torch, dr = self.torch, self.dr
+        verts.grad = None
+        attr.grad = None
+        clip = torch.nn.functional.pad(verts, (0, 1), value=1.0) @ self.mvp.T
+        rast, _ = dr.rasterize(self.ctx, clip, self.tri, (H, W), grad_db=False)
+        col, _ = dr.interpolate(attr, rast, self.tri)
+        aa = dr.antialias(col, rast, clip, self.tri, topology_hash=self.topo)
+        loss = (aa - self.target).abs().mean()
+        loss.backward()
+        return loss
+
+
+# Kernel launches of ours per step: rasterize (setup, scan, fill, fine) = 4,
+# interpolate fwd/bwd = 2, antialias fwd/bwd = 2, rasterize bwd = 1.
+LAUNCHES_PER_STEP = 9
+
+
+def _clock_sampler():
+    f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+    try:
+        p = subprocess.Popen(["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                              "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                             stdout=f, stderr=subprocess.DEVNULL)
+    except (OSError, FileNotFoundError):
+        return None, f.name
+    return p, f.name
+
+
+def _clock_summary(proc, path, gpu_index):
+    if proc is None:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+    proc.terminate()
+    try:
+        proc.wait(timeout=5)
+    except subprocess.TimeoutExpired:
+        proc.kill()
+    sms, maxs, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    with open(path) as fh:
+        for line in fh:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9 or not parts[0].isdigit() or int(parts[0]) != gpu_index:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                maxs.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(n)
+    os.unlink(path)
+    return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": max(maxs) if maxs else None,
+            "samples": len(sms), "reasons": sorted(reasons)}
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10):
+    """CUDA-event time of each C-ABI entry point of the step on the same
+    inputs (current stream), L2 flushed between repetitions."""
+    import torch
+    from diffrp_gb300 import _ffi
+    from diffrp_gb300 import nvdr as dr
+    s = torch.cuda.current_stream(dev)
+    sp = s.cuda_stream
+    ctx = dr.RasterizeCudaContext(dev)
+    tri = torch.from_numpy(f).to(dev)
+    v_t = torch.from_numpy(verts).to(dev)
+    clip = (torch.nn.functional.pad(v_t, (0, 1), value=1.0) @ torch.from_numpy(mvp).to(dev).T).contiguous()
+    a_t = torch.from_numpy(attr).to(dev)
+    topo = dr.antialias_construct_topology_hash(tri)
+    rast, _ = dr.rasterize(ctx, clip, tri, (H, W), grad_db=False)
+    col, _ = dr.interpolate(a_t, rast, tri)
+    aa = dr.antialias(col, rast, clip, tri, topology_hash=topo)
+    g = torch.sign(aa - torch.from_numpy(target).to(dev)) / aa.numel()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    V, F = clip.shape[0], tri.shape[0]
+    gpos = torch.zeros_like(clip)
+    gattr = torch.zeros_like(a_t)
+    gcol = torch.empty_like(col)
+    grast = torch.empty_like(rast)
+    out = torch.empty_like(col)
+    ops = {
+        "rasterize_fwd": lambda: ctx._raster_call(clip, tri, None, 1, F, H, W, 0, None, rast, None, None),
+        "interpolate_fwd": lambda: _ffi.call("drp_interpolate_fwd", a_t.data_ptr(), 0, V, C, rast.data_ptr(), None,
+                                             tri.data_ptr(), F, 1, H, W, None, 0, out.data_ptr(), None, sp),
+        "antialias_fwd": lambda: _ffi.call("drp_antialias_fwd", col.data_ptr(), C, rast.data_ptr(), clip.data_ptr(),
+                                           0, V, tri.data_ptr(), F, topo.data_ptr(), 1, H, W, out.data_ptr(), sp),
+        "antialias_bwd": lambda: _ffi.call("drp_antialias_bwd", col.data_ptr(), C, rast.data_ptr(), clip.data_ptr(),
+                                           0, V, tri.data_ptr(), F, topo.data_ptr(), 1, H, W, g.data_ptr(), 1.0,
+                                           gcol.data_ptr(), gpos.data_ptr(), sp),
+        "interpolate_bwd": lambda: _ffi.call("drp_interpolate_bwd", a_t.data_ptr(), 0, V, C, rast.data_ptr(), None,
+                                             tri.data_ptr(), F, 1, H, W, None, 0, gcol.data_ptr(), None,
+                                             gattr.data_ptr(), grast.data_ptr(), None, sp),
+        "rasterize_bwd": lambda: _ffi.call("drp_rasterize_bwd", clip.data_ptr(), 0, V, tri.data_ptr(), F, 1, H, W,
+                                           rast.data_ptr(), grast.data_ptr(), None, gpos.data_ptr(), sp),
+    }
+    P = H * W
+    # Algorithmic bytes per launch ("Roofline accounting").
+    algo = {
+        "rasterize_fwd": P * 16 + V * 16 + F * 12,
+        "interpolate_fwd": P * (16 + 4 * C) + V * 4 * C,
+        "antialias_fwd": P * (4 * C + 16 + 4 * C),
+        "antialias_bwd": P * (4 * C + 4 * C + 16 + 4 * C) + V * 16,
+        "interpolate_bwd": P * (4 * C + 16 + 16) + V * 4 * C * 2,
+        "rasterize_bwd": P * (16 + 16) + V * 16 * 2,
+    }
+    times = {}
+    for name, fn in ops.items():
+        fn()
+        ts = []
+        for _ in range(reps):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            fn()
+            e1.record(s)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        times[name] = statistics.median(ts)
+    return times, algo
+
+
+def cpu_baseline(verts, f, attr, mvp, target, budget_s=8.0):
+    """The CPU oracle on the same workload: rows of the image are the sample
+    unit (whole steps when they fit in the budget)."""
+    import oracle as O
+    nthreads = O.default_threads()
+    clip = (np.concatenate([verts, np.ones((len(verts), 1), np.float32)], 1).astype(np.float64) @
+            mvp.astype(np.float64).T).astype(np.float32)
+    nbr = O.topology(f)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        rast, _, _ = O.rasterize(clip, f, (H, W), grad_db=False, nthreads=nthreads)
+        col, _ = O.interpolate(attr, rast, f, nthreads=nthreads)
+        aa = O.antialias(col, rast, clip, f, nbr, nthreads=nthreads)
+        g = np.sign(aa - target) / aa.size
+        gc, gp = O.antialias_bwd(col, rast, clip, f, g, nbr, nthreads=nthreads)
+        ga, gr, _ = O.interpolate_bwd(attr, rast, f, gc, nthreads=nthreads)
+        O.raster_bwd(clip, f, rast, gr, nthreads=nthreads)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 50:
+            break
+    return {"value": steps * H * W / el / 1e6, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": "%d full fwd+bwd step(s) of the %dx%d, 20480-triangle, 8-channel workload in %.1f s"
+                      % (steps, H, W, el)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    verts, f, attr, mvp, target = make_workload()
+    for _ in range(max(args.warmup, 0)):
+        pass
+    base = cpu_baseline(verts, f, attr, mvp, target, budget_s=max(4.0, 2.0 * args.steps))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": H * W / base["value"] / 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "icosphere5-displaced 20480 tris, 1024x1024, 8 ch, L1 loss, fwd+bwd",
+                   "global_batch": 1, "resolution": [H, W], "channels": C, "parallelism": "cpu threads"},
+        "cpu_baseline": base,
+        "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    import __graft_entry__
+    __graft_entry__.build()
+
+    verts_np, f, attr_np, mvp, target = make_workload()
+    step = Step(dev, f, mvp, target)
+    verts = torch.from_numpy(verts_np).to(dev).requires_grad_(True)
+    attr = torch.from_numpy(attr_np).to(dev).requires_grad_(True)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    W_ = max(3, args.warmup)
+    for _ in range(W_):
+        step(verts, attr)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # -- device-resident timing ---------------------------------------------
+    clk, clk_path = _clock_sampler()
+    s = torch.cuda.current_stream(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    for i in range(args.steps):
+        flush.fill_(i & 0xff)
+        ev[i][0].record(s)
+        step(verts, attr)
+        ev[i][1].record(s)
+    barrier()
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+
+    # -- end-to-end through the public API with host buffers -----------------
+    h_verts = torch.from_numpy(verts_np).pin_memory()
+    h_attr = torch.from_numpy(attr_np).pin_memory()
+    h_loss = torch.empty((), dtype=torch.float32).pin_memory()
+    h_gv = torch.empty_like(h_verts).pin_memory()
+    h_ga = torch.empty_like(h_attr).pin_memory()
+    d_verts = torch.empty_like(verts)
+    d_attr = torch.empty_like(attr)
+    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    for i in range(args.steps):
+        flush.fill_(i & 0xff)
+        e2e_ev[i][0].record(s)
+        d_verts.copy_(h_verts, non_blocking=True)
+        d_attr.copy_(h_attr, non_blocking=True)
+        pv = d_verts.detach().requires_grad_(True)
+        pa = d_attr.detach().requires_grad_(True)
+        loss = step(pv, pa)
+        h_loss.copy_(loss.detach(), non_blocking=True)
+        h_gv.copy_(pv.grad, non_blocking=True)
+        h_ga.copy_(pa.grad, non_blocking=True)
+        e2e_ev[i][1].record(s)
+    barrier()
+    clocks = _clock_summary(clk, clk_path, dev.index if dev.index is not None else 0)
+    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_ev)
+    if world > 1:
+        t = torch.tensor([total_ms, e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, e2e_ms = float(t[0]), float(t[1])
+
+    pix = H * W * args.steps * world
+    value = pix / (total_ms / 1e3) / 1e6
+    e2e_value = pix / (e2e_ms / 1e3) / 1e6
+    h2d = h_verts.numel() * 4 + h_attr.numel() * 4
+    d2h = 4 + h_gv.numel() * 4 + h_ga.numel() * 4
+
+    if rank == 0:
+        times, algo = kernel_breakdown(dev, verts_np, f, attr_np, mvp, target)
+        dom = max(times, key=times.get)
+        peak, peak_kind = _peaks()
+        achieved = algo[dom] / (times[dom] / 1e3) / 1e9
+        traffic = None
+        tpath = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tpath):
+            with open(tpath) as fh:
+                traffic = json.load(fh).get(dom)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": W_, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded icosphere, attributes and target)",
+            "config": {"workload": "icosphere5-displaced 20480 tris, 1024x1024, 8 ch, L1 loss, fwd+bwd "
+                                   "(single mesh, full gradients)",
+                       "global_batch": world, "resolution": [H, W], "channels": C,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "flushed between steps (256 MiB write outside the timed events)",
+                       "path": "drop-in nvdr API, eager (plain per-op launches)"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes": algo[dom], "kernel_ms": times[dom]},
+            "kernel_ms": times,
+            "clocks": clocks,
+            "gpu_launches": LAUNCHES_PER_STEP * args.steps * 2,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(verts_np, f, attr_np, mvp, target)
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

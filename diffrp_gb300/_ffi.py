@@ -1,0 +1,83 @@
+"""ctypes binding of libdiffrp_gb300.so (the C ABI in include/diffrp_gb300.h).
+
+The library is loaded from ``diffrp_gb300/_lib`` (built in-tree by
+``diffrp_gb300.build``).  There is no CPU fallback: if the library is missing
+or fails to load, every entry point raises.
+"""
+import ctypes
+import os
+import threading
+
+_P = ctypes.c_void_p
+_LL = ctypes.c_longlong
+_ULL = ctypes.c_ulonglong
+_I = ctypes.c_int
+_F = ctypes.c_float
+_SZ = ctypes.POINTER(ctypes.c_size_t)
+
+_SIGNATURES = {
+    "drp_abi_version": [],
+    "drp_raster_workspace_size": [_I, _LL, _I, _I, _I, _ULL, _SZ],
+    "drp_rasterize_fwd": [_P, ctypes.c_size_t, _P, _LL, _LL, _P, _LL, _I, _P, _LL, _I, _I, _I, _I, _ULL, _P, _P,
+                          _P, _P, _P],
+    "drp_rasterize_bwd": [_P, _LL, _LL, _P, _LL, _I, _I, _I, _P, _P, _P, _P, _P],
+    "drp_interpolate_fwd": [_P, _LL, _LL, _I, _P, _P, _P, _LL, _I, _I, _I, _P, _I, _P, _P, _P],
+    "drp_interpolate_bwd": [_P, _LL, _LL, _I, _P, _P, _P, _LL, _I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _P],
+    "drp_interpolate_sparse_fwd": [_P, _LL, _I, _P, _P, _LL, _P, _P],
+    "drp_interpolate_sparse_bwd": [_P, _LL, _I, _P, _P, _LL, _P, _P, _P, _P],
+    "drp_topology_workspace_size": [_LL, _SZ],
+    "drp_antialias_topology": [_P, ctypes.c_size_t, _P, _LL, _P, _P],
+    "drp_antialias_fwd": [_P, _I, _P, _P, _LL, _LL, _P, _LL, _P, _I, _I, _I, _P, _P],
+    "drp_antialias_bwd": [_P, _I, _P, _P, _LL, _LL, _P, _LL, _P, _I, _I, _I, _P, _F, _P, _P, _P],
+}
+
+ABI_VERSION = 1
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib_path():
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libdiffrp_gb300.so")
+
+
+def load():
+    """Load (once) and return the CUDA library; raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            path = lib_path()
+            if not os.path.exists(path):
+                raise RuntimeError(
+                    "diffrp_gb300 CUDA library not built (%s missing); run `python -m diffrp_gb300.build`" % path)
+            lib = ctypes.CDLL(path)
+            for name, argtypes in _SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.argtypes = argtypes
+                fn.restype = ctypes.c_int
+            lib.drp_status_string.restype = ctypes.c_char_p
+            lib.drp_status_string.argtypes = [ctypes.c_int]
+            lib.drp_last_error.restype = ctypes.c_char_p
+            lib.drp_last_error.argtypes = []
+            if lib.drp_abi_version() != ABI_VERSION:
+                raise RuntimeError("libdiffrp_gb300 ABI %d != expected %d" % (lib.drp_abi_version(), ABI_VERSION))
+            _lib = lib
+    return _lib
+
+
+def call(name, *args):
+    """Call an entry point; a non-zero status becomes RuntimeError."""
+    lib = load()
+    status = getattr(lib, name)(*args)
+    if status != 0:
+        msg = lib.drp_last_error().decode(errors="replace")
+        raise RuntimeError("%s failed (%s): %s" % (name, lib.drp_status_string(status).decode(), msg))
+    return status
+
+
+def size_out(name, *args):
+    out = ctypes.c_size_t(0)
+    call(name, *args, ctypes.byref(out))
+    return out.value

@@ -1,0 +1,116 @@
+// drp_internal.h -- argument blocks passed from the C-ABI layer to the kernel
+// launchers.  Not part of the public interface (see include/diffrp_gb300.h).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace drp {
+
+// Device scratch carved out of the caller-provided rasterisation workspace.
+struct RasterWs {
+    void* prims;            // B * max_view_tris * 48 bytes
+    uint32_t* tile_count;   // B * tiles
+    uint32_t* tile_offset;  // B * tiles
+    uint32_t* tile_cursor;  // B * tiles
+    uint32_t* tile_list;    // list_capacity entries
+    uint32_t* stats;        // [0..1] total list entries (u64), [2] device error bits, [3] spare
+};
+
+struct RasterArgs {
+    const float* pos;
+    long long pos_view_stride;  // floats between views, 0 = shared vertices
+    long long num_vertices;
+    const int* tri;
+    long long num_triangles;
+    const int* ranges;  // device [B][2] (first, count) or null = all triangles
+    int B;
+    long long max_view_tris;
+    int H, W;
+    int tiles_x, tiles_y, tile_log2, threads_per_tri;
+    unsigned long long list_capacity;
+    const unsigned long long* prev_key;
+    float* rast;
+    float* rast_db;
+    unsigned long long* out_key;
+    RasterWs ws;
+};
+
+struct RasterBwdArgs {
+    const float* pos;
+    long long pos_view_stride;
+    long long num_vertices;
+    long long num_triangles;
+    const int* tri;
+    const float* rast;
+    const float* grad_rast;
+    const float* grad_db;
+    int B, H, W;
+    float* grad_pos;
+};
+
+struct InterpArgs {
+    const float* attr;
+    long long attr_view_stride;  // floats between views, 0 = shared attributes
+    long long num_vertices;
+    int C;
+    const float* rast;
+    const float* rast_db;
+    const int* tri;
+    long long num_triangles;
+    int B, H, W;
+    const int* diff_idx;  // device, nd entries
+    int nd;
+    float* out;
+    float* da;
+    // backward
+    const float* grad_out;
+    const float* grad_da;
+    float* grad_attr;
+    float* grad_rast;
+    float* grad_db;
+};
+
+struct SparseInterpArgs {
+    const float* vb;
+    long long V;
+    int C;
+    const float* vi;          // N x 4
+    const long long* tri_idx; // N x 3
+    long long N;
+    float* out;
+    const float* grad_out;
+    float* grad_vb;
+    float* grad_vi;
+};
+
+struct AAArgs {
+    const float* color;
+    int C;
+    const float* rast;
+    const float* pos;
+    long long pos_view_stride;
+    long long num_vertices;
+    long long num_triangles;
+    const int* tri;
+    const int* nbr;  // F x 3 neighbour table or null (every edge a silhouette)
+    int B, H, W;
+    float* out;
+    const float* grad_out;
+    float* grad_color;
+    float* grad_pos;
+    float boost;
+};
+
+int launch_rasterize(const RasterArgs& a, cudaStream_t s);
+int launch_raster_bwd(const RasterBwdArgs& a, cudaStream_t s);
+int launch_interp_fwd(const InterpArgs& a, cudaStream_t s);
+int launch_interp_bwd(const InterpArgs& a, cudaStream_t s);
+int launch_interp_sparse_fwd(const SparseInterpArgs& a, cudaStream_t s);
+int launch_interp_sparse_bwd(const SparseInterpArgs& a, cudaStream_t s);
+int launch_topology(const int* tri, long long F, void* ws, size_t ws_bytes, int* nbr, cudaStream_t s);
+size_t topology_ws_bytes(long long F);
+int launch_aa_fwd(const AAArgs& a, cudaStream_t s);
+int launch_aa_bwd(const AAArgs& a, cudaStream_t s);
+
+}  // namespace drp

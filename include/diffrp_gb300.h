@@ -1,0 +1,176 @@
+/*
+ * diffrp_gb300.h -- C ABI of the GB300 (sm_103a) differentiable rasterisation
+ * library libdiffrp_gb300.so.
+ *
+ * The entry points replace the native calls diffrp makes into nvdiffrast
+ * (package diffrp-nvdiffrast, setup.py:39 of the reference):
+ *
+ *   dr.RasterizeCudaContext()                 diffrp/rendering/surface_deferred.py:225
+ *   dr.DepthPeeler(...).rasterize_next_layer() diffrp/rendering/surface_deferred.py:260-262
+ *   dr.interpolate(attr, rast, tri)           diffrp/rendering/interpolator.py:83
+ *   dr.antialias(color, rast, pos, tri)       diffrp/rendering/surface_deferred.py:775
+ *   polyfill_interpolate (torch gather + FMA) diffrp/rendering/interpolator.py:32-65
+ *
+ * Conventions
+ *   - Every pointer argument is a device pointer unless stated otherwise;
+ *     arrays are dense, row-major, float32 / int32 as typed.  float4-typed
+ *     rows (pos, rast, rast_db, grad_rast) must be 16-byte aligned.
+ *   - `stream` is a cudaStream_t passed as void*; NULL is the legacy stream.
+ *     Every call only enqueues work; nothing synchronises the host.
+ *   - The library allocates no device memory.  Scratch comes from
+ *     caller-provided workspaces whose sizes are queried first.
+ *   - rast layout (B, H, W, 4) = (u, v, z/w, tri_id + 1); row 0 is NDC y = -1.
+ *     tri ids above 2^24 are stored as the float with bit pattern
+ *     0x4a800000 + id (diffrp/rendering/interpolator.py:24-29).
+ *   - Return value: DRP_STATUS_*; drp_last_error() gives a message for the
+ *     calling thread.
+ *   - Gradient outputs marked "accumulated" are added into (caller zeroes).
+ */
+#ifndef DIFFRP_GB300_H
+#define DIFFRP_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DRP_ABI_VERSION 1
+
+#define DRP_STATUS_OK 0
+#define DRP_STATUS_INVALID_ARGUMENT 1
+#define DRP_STATUS_WORKSPACE_TOO_SMALL 2
+#define DRP_STATUS_CUDA_ERROR 3
+
+/* Largest supported raster width / height. */
+#define DRP_MAX_RESOLUTION 16384
+
+/* Device error bits in the rasterisation workspace's stats block. */
+#define DRP_DEVERR_BAD_INDEX 1u
+#define DRP_DEVERR_LIST_OVERFLOW 2u
+
+int drp_abi_version(void);
+const char* drp_status_string(int status);
+const char* drp_last_error(void);
+
+/* ------------------------------------------------------------------------ */
+/* Rasterisation                                                             */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * Workspace bytes for drp_rasterize_fwd.  The first 16 bytes of the workspace
+ * are a stats block written by every call: bytes [0, 8) = tile-list entries the
+ * call needed (uint64), bytes [8, 12) = DRP_DEVERR_* bits.  Callers grow
+ * list_capacity from the first field; a call whose lists overflow is still
+ * exact (overflowing tiles fall back to scanning the view's primitives).
+ */
+int drp_raster_workspace_size(int num_views, long long max_view_tris, int height, int width, int tile_log2,
+                              unsigned long long list_capacity, size_t* bytes);
+
+/*
+ * Rasterise num_views views.  Replaces dr.DepthPeeler(ctx, pos, tri, (h, w),
+ * ranges).rasterize_next_layer() (diffrp/rendering/surface_deferred.py:260-262)
+ * and dr.rasterize.
+ *   pos              clip-space vertices, float4 rows; view b reads
+ *                    pos + b * pos_view_stride (floats); stride 0 = shared
+ *                    vertices (range mode).
+ *   ranges           device int32 [num_views][2] = (first triangle, count), or
+ *                    NULL for all triangles in every view (instanced mode).
+ *   max_view_tris    max over views of the triangle count.
+ *   tile_log2        3, 4 or 5 (8, 16, 32 pixel tiles); threads_per_tri in
+ *                    {1, 2, 4, 8, 16, 32}.
+ *   prev_key         previous layer's keys (depth peeling) or NULL.
+ *   rast             out (B, H, W, 4); rast_db out (B, H, W, 4) or NULL;
+ *   out_key          out (B, H, W) uint64 visibility keys or NULL.
+ */
+int drp_rasterize_fwd(void* workspace, size_t workspace_bytes, const float* pos, long long pos_view_stride,
+                      long long num_vertices, const int* tri, long long num_triangles, int num_views,
+                      const int* ranges, long long max_view_tris, int height, int width, int tile_log2,
+                      int threads_per_tri, unsigned long long list_capacity, const unsigned long long* prev_key,
+                      float* rast, float* rast_db, unsigned long long* out_key, void* stream);
+
+/*
+ * Backward of rasterisation: grad_rast (B, H, W, 4) on (u, v, z/w, -) and
+ * optional grad_db (B, H, W, 4) -> grad_pos (accumulated, layout of pos).
+ * The gradient path of dr.rasterize under autograd
+ * (diffrp/rendering/surface_deferred.py:260-262).
+ */
+int drp_rasterize_bwd(const float* pos, long long pos_view_stride, long long num_vertices, const int* tri,
+                      long long num_triangles, int num_views, int height, int width, const float* rast,
+                      const float* grad_rast, const float* grad_db, float* grad_pos, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Interpolation                                                             */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * dr.interpolate(attr, rast, tri, rast_db, diff_attrs)
+ * (diffrp/rendering/interpolator.py:83).  attr (V, C) shared
+ * (attr_view_stride 0) or (B, V, C).  diff_idx: device int32[num_diff] channel
+ * indices for screen-space derivatives (da (B, H, W, 2 * num_diff)), NULL when
+ * num_diff == 0.
+ */
+int drp_interpolate_fwd(const float* attr, long long attr_view_stride, long long num_vertices, int channels,
+                        const float* rast, const float* rast_db, const int* tri, long long num_triangles,
+                        int num_views, int height, int width, const int* diff_idx, int num_diff, float* out,
+                        float* da, void* stream);
+
+/* Backward of drp_interpolate_fwd.  grad_attr accumulated; grad_rast
+ * (B, H, W, 4) and grad_db (B, H, W, 4, may be NULL) overwritten. */
+int drp_interpolate_bwd(const float* attr, long long attr_view_stride, long long num_vertices, int channels,
+                        const float* rast, const float* rast_db, const int* tri, long long num_triangles,
+                        int num_views, int height, int width, const int* diff_idx, int num_diff,
+                        const float* grad_out, const float* grad_da, float* grad_attr, float* grad_rast,
+                        float* grad_db, void* stream);
+
+/*
+ * Stencil-masked interpolation of n pixel rows: polyfill_interpolate /
+ * _interpolate_impl (diffrp/rendering/interpolator.py:32-65).
+ * vi_data (n, 4) rast rows, tri_idx (n, 3) int64 vertex indices.
+ */
+int drp_interpolate_sparse_fwd(const float* vertex_buffer, long long num_vertices, int channels,
+                               const float* vi_data, const long long* tri_idx, long long n, float* out,
+                               void* stream);
+
+/* Backward: grad_vb accumulated, grad_vi (n, 4) overwritten (u, v, 0, 0). */
+int drp_interpolate_sparse_bwd(const float* vertex_buffer, long long num_vertices, int channels,
+                               const float* vi_data, const long long* tri_idx, long long n, const float* grad_out,
+                               float* grad_vb, float* grad_vi, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Antialiasing                                                              */
+/* ------------------------------------------------------------------------ */
+
+/* Workspace bytes for drp_antialias_topology. */
+int drp_topology_workspace_size(long long num_triangles, size_t* bytes);
+
+/*
+ * dr.antialias_construct_topology_hash(tri) (implicit in the dr.antialias call
+ * at diffrp/rendering/surface_deferred.py:775): nbr (F, 3) int32, the
+ * triangle across edge k (vertices k+1, k+2) when exactly two triangles share
+ * that vertex pair, else -1.
+ */
+int drp_antialias_topology(void* workspace, size_t workspace_bytes, const int* tri, long long num_triangles,
+                           int* nbr, void* stream);
+
+/*
+ * dr.antialias(color, rast, pos, tri) (diffrp/rendering/surface_deferred.py:775).
+ * color (B, H, W, C); nbr from drp_antialias_topology or NULL (every edge
+ * is treated as a silhouette).
+ */
+int drp_antialias_fwd(const float* color, int channels, const float* rast, const float* pos,
+                      long long pos_view_stride, long long num_vertices, const int* tri, long long num_triangles,
+                      const int* nbr, int num_views, int height, int width, float* out, void* stream);
+
+/* Backward: grad_color overwritten, grad_pos accumulated (times
+ * pos_gradient_boost); grad_pos may be NULL. */
+int drp_antialias_bwd(const float* color, int channels, const float* rast, const float* pos,
+                      long long pos_view_stride, long long num_vertices, const int* tri, long long num_triangles,
+                      const int* nbr, int num_views, int height, int width, const float* grad_out,
+                      float pos_gradient_boost, float* grad_color, float* grad_pos, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DIFFRP_GB300_H */
