@@ -91,9 +91,41 @@ class Step:
         return loss
 
 
+class GraphedStep:
+    """The same step captured once as a CUDA graph (static parameter tensors,
+    gradients allocated in the graph's pool) and replayed."""
+
+    def __init__(self, step, verts_np, attr_np, dev):
+        import torch
+        self.torch = torch
+        self.verts = torch.from_numpy(verts_np).to(dev).requires_grad_(True)
+        self.attr = torch.from_numpy(attr_np).to(dev).requires_grad_(True)
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            for _ in range(3):
+                step(self.verts, self.attr)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.loss = step(self.verts, self.attr)
+        torch.cuda.synchronize(dev)
+
+    def load(self, h_verts, h_attr):
+        with self.torch.no_grad():
+            self.verts.copy_(h_verts, non_blocking=True)
+            self.attr.copy_(h_attr, non_blocking=True)
+
+    def __call__(self):
+        self.graph.replay()
+        return self.loss
+
+
 # Kernel launches of ours per step: rasterize (setup, scan, fill, fine) = 4,
-# interpolate fwd/bwd = 2, antialias fwd/bwd = 2, rasterize bwd = 1.
-LAUNCHES_PER_STEP = 9
+# interpolate fwd/bwd = 2, antialias fwd/bwd = 2 + 2 triangle setups,
+# rasterize bwd = 1.
+LAUNCHES_PER_STEP = 11
 
 
 def _clock_sampler():
@@ -171,15 +203,18 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10):
     gcol = torch.empty_like(col)
     grast = torch.empty_like(rast)
     out = torch.empty_like(col)
+    aws = torch.empty(_ffi.size_out("drp_antialias_workspace_size", 1, F), dtype=torch.uint8, device=dev)
     ops = {
         "rasterize_fwd": lambda: ctx._raster_call(clip, tri, None, 1, F, H, W, 0, None, rast, None, None),
         "interpolate_fwd": lambda: _ffi.call("drp_interpolate_fwd", a_t.data_ptr(), 0, V, C, rast.data_ptr(), None,
                                              tri.data_ptr(), F, 1, H, W, None, 0, out.data_ptr(), None, sp),
-        "antialias_fwd": lambda: _ffi.call("drp_antialias_fwd", col.data_ptr(), C, rast.data_ptr(), clip.data_ptr(),
-                                           0, V, tri.data_ptr(), F, topo.data_ptr(), 1, H, W, out.data_ptr(), sp),
-        "antialias_bwd": lambda: _ffi.call("drp_antialias_bwd", col.data_ptr(), C, rast.data_ptr(), clip.data_ptr(),
-                                           0, V, tri.data_ptr(), F, topo.data_ptr(), 1, H, W, g.data_ptr(), 1.0,
-                                           gcol.data_ptr(), gpos.data_ptr(), sp),
+        "antialias_fwd": lambda: _ffi.call("drp_antialias_fwd", aws.data_ptr(), aws.numel(), col.data_ptr(), C,
+                                           rast.data_ptr(), clip.data_ptr(), 0, V, tri.data_ptr(), F,
+                                           topo.data_ptr(), 1, H, W, out.data_ptr(), sp),
+        "antialias_bwd": lambda: _ffi.call("drp_antialias_bwd", aws.data_ptr(), aws.numel(), col.data_ptr(), C,
+                                           rast.data_ptr(), clip.data_ptr(), 0, V, tri.data_ptr(), F,
+                                           topo.data_ptr(), 1, H, W, g.data_ptr(), 1.0, gcol.data_ptr(),
+                                           gpos.data_ptr(), sp),
         "interpolate_bwd": lambda: _ffi.call("drp_interpolate_bwd", a_t.data_ptr(), 0, V, C, rast.data_ptr(), None,
                                              tri.data_ptr(), F, 1, H, W, None, 0, gcol.data_ptr(), None,
                                              gattr.data_ptr(), grast.data_ptr(), None, sp),
@@ -267,6 +302,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="full", choices=["full", "steps"],
+                    help="steps: only the warm-up and timed device-resident steps (for profilers)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -292,24 +329,42 @@ def main():
     for _ in range(W_):
         step(verts, attr)
     torch.cuda.synchronize()
+    graphed = GraphedStep(step, verts_np, attr_np, dev)
+    for _ in range(W_):
+        graphed()
+    torch.cuda.synchronize()
 
     def barrier():
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
 
-    # -- device-resident timing ---------------------------------------------
-    clk, clk_path = _clock_sampler()
     s = torch.cuda.current_stream(dev)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    barrier()
-    for i in range(args.steps):
-        flush.fill_(i & 0xff)
-        ev[i][0].record(s)
-        step(verts, attr)
-        ev[i][1].record(s)
-    barrier()
-    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+
+    def timed(fn, n):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        barrier()
+        for i in range(n):
+            flush.fill_(i & 0xff)
+            evs[i][0].record(s)
+            fn()
+            evs[i][1].record(s)
+        barrier()
+        return sum(a.elapsed_time(b) for a, b in evs)
+
+    # -- device-resident timing: the graph-captured step is the headline; the
+    # eager (plain per-op launch) step is reported beside it ----------------
+    clk, clk_path = _clock_sampler()
+    total_ms = timed(graphed, args.steps)
+    if args.mode == "steps":
+        if clk is not None:
+            clk.terminate()
+        if rank == 0:
+            print(json.dumps({"mode": "steps", "ms_per_step": total_ms / args.steps}))
+        if world > 1:
+            dist.destroy_process_group()
+        return 0
+    eager_ms = timed(lambda: step(verts, attr), args.steps)
 
     # -- end-to-end through the public API with host buffers -----------------
     h_verts = torch.from_numpy(verts_np).pin_memory()
@@ -317,29 +372,20 @@ def main():
     h_loss = torch.empty((), dtype=torch.float32).pin_memory()
     h_gv = torch.empty_like(h_verts).pin_memory()
     h_ga = torch.empty_like(h_attr).pin_memory()
-    d_verts = torch.empty_like(verts)
-    d_attr = torch.empty_like(attr)
-    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    barrier()
-    for i in range(args.steps):
-        flush.fill_(i & 0xff)
-        e2e_ev[i][0].record(s)
-        d_verts.copy_(h_verts, non_blocking=True)
-        d_attr.copy_(h_attr, non_blocking=True)
-        pv = d_verts.detach().requires_grad_(True)
-        pa = d_attr.detach().requires_grad_(True)
-        loss = step(pv, pa)
+
+    def e2e_step():
+        graphed.load(h_verts, h_attr)
+        loss = graphed()
         h_loss.copy_(loss.detach(), non_blocking=True)
-        h_gv.copy_(pv.grad, non_blocking=True)
-        h_ga.copy_(pa.grad, non_blocking=True)
-        e2e_ev[i][1].record(s)
-    barrier()
+        h_gv.copy_(graphed.verts.grad, non_blocking=True)
+        h_ga.copy_(graphed.attr.grad, non_blocking=True)
+
+    e2e_ms = timed(e2e_step, args.steps)
     clocks = _clock_summary(clk, clk_path, dev.index if dev.index is not None else 0)
-    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_ev)
     if world > 1:
-        t = torch.tensor([total_ms, e2e_ms], device=dev)
+        t = torch.tensor([total_ms, e2e_ms, eager_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, e2e_ms = float(t[0]), float(t[1])
+        total_ms, e2e_ms, eager_ms = float(t[0]), float(t[1]), float(t[2])
 
     pix = H * W * args.steps * world
     value = pix / (total_ms / 1e3) / 1e6
@@ -366,14 +412,16 @@ def main():
                        "global_batch": world, "resolution": [H, W], "channels": C,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "flushed between steps (256 MiB write outside the timed events)",
-                       "path": "drop-in nvdr API, eager (plain per-op launches)"},
+                       "path": "drop-in nvdr API ops, whole fwd+bwd step captured as one CUDA graph"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                          "algorithmic_bytes": algo[dom], "kernel_ms": times[dom]},
             "kernel_ms": times,
+            "eager": {"value": pix / (eager_ms / 1e3) / 1e6, "unit": UNIT,
+                      "note": "same step, eager per-op launches (host-launch bound)"},
             "clocks": clocks,
-            "gpu_launches": LAUNCHES_PER_STEP * args.steps * 2,
+            "gpu_launches": LAUNCHES_PER_STEP * args.steps * 3,
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(verts_np, f, attr_np, mvp, target)

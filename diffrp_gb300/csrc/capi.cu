@@ -94,12 +94,14 @@ DRP_API int drp_rasterize_fwd(void* workspace, size_t workspace_bytes, const flo
     if (num_views <= 0) return fail(DRP_STATUS_INVALID_ARGUMENT, "num_views must be positive");
     if (!res_ok(height, width)) return fail(DRP_STATUS_INVALID_ARGUMENT, "resolution %dx%d out of range", height, width);
     if (tile_log2 < 3 || tile_log2 > 5) return fail(DRP_STATUS_INVALID_ARGUMENT, "tile_log2 must be 3, 4 or 5");
-    if (threads_per_tri < 1 || threads_per_tri > 32 || (threads_per_tri & (threads_per_tri - 1)))
-        return fail(DRP_STATUS_INVALID_ARGUMENT, "threads_per_tri must be a power of two in [1, 32]");
+    if (threads_per_tri < 0 || threads_per_tri > 32 || (threads_per_tri & (threads_per_tri - 1)))
+        return fail(DRP_STATUS_INVALID_ARGUMENT, "threads_per_tri must be 0 or a power of two in [1, 32]");
     if (num_vertices < 0 || num_triangles < 0 || max_view_tris < 0 || pos_view_stride < 0)
         return fail(DRP_STATUS_INVALID_ARGUMENT, "negative size");
-    if (num_triangles > 0x7ffffffell || num_vertices > 0x7fffffffll)
-        return fail(DRP_STATUS_INVALID_ARGUMENT, "more than 2^31 - 2 triangles or 2^31 - 1 vertices");
+    // The rast w channel encodes id + 1 as the float with bits 0x4a800000 + id + 1
+    // above 2^24; it stays a finite positive float below id + 1 = 0x35000000.
+    if (num_triangles >= 0x34ffffffll || num_vertices > 0x7fffffffll)
+        return fail(DRP_STATUS_INVALID_ARGUMENT, "more than %lld triangles or 2^31 - 1 vertices", 0x34fffffell);
     if (!ranges && max_view_tris != num_triangles)
         return fail(DRP_STATUS_INVALID_ARGUMENT, "without ranges max_view_tris must equal num_triangles");
     if (max_view_tris > 0 && (!pos || !tri)) return fail(DRP_STATUS_INVALID_ARGUMENT, "pos / tri is null");
@@ -330,11 +332,29 @@ static int aa_common(const float* color, int channels, const float* rast, const 
     return DRP_STATUS_OK;
 }
 
-DRP_API int drp_antialias_fwd(const float* color, int channels, const float* rast, const float* pos,
-                              long long pos_view_stride, long long num_vertices, const int* tri,
-                              long long num_triangles, const int* nbr, int num_views, int height, int width,
-                              float* out, void* stream) {
+DRP_API int drp_antialias_workspace_size(int num_views, long long num_triangles, size_t* bytes) {
+    if (!bytes || num_views < 0 || num_triangles < 0) return fail(DRP_STATUS_INVALID_ARGUMENT, "bad arguments");
+    *bytes = drp::aa_ws_bytes(num_views, num_triangles);
+    return DRP_STATUS_OK;
+}
+
+static int aa_ws_check(void* workspace, size_t workspace_bytes, int num_views, long long num_triangles) {
+    if (!workspace || !aligned(workspace, 16)) return fail(DRP_STATUS_INVALID_ARGUMENT, "workspace must be 16-byte aligned");
+    if (workspace_bytes < drp::aa_ws_bytes(num_views, num_triangles))
+        return fail(DRP_STATUS_WORKSPACE_TOO_SMALL, "antialias workspace needs %zu bytes",
+                    drp::aa_ws_bytes(num_views, num_triangles));
+    if ((long long)num_views * num_triangles * 2 > 0x7fffffffll * 16)
+        return fail(DRP_STATUS_INVALID_ARGUMENT, "too many triangles x views");
+    return DRP_STATUS_OK;
+}
+
+DRP_API int drp_antialias_fwd(void* workspace, size_t workspace_bytes, const float* color, int channels,
+                              const float* rast, const float* pos, long long pos_view_stride, long long num_vertices,
+                              const int* tri, long long num_triangles, const int* nbr, int num_views, int height,
+                              int width, float* out, void* stream) {
     int st = aa_common(color, channels, rast, pos, pos_view_stride, tri, num_views, height, width);
+    if (st) return st;
+    st = aa_ws_check(workspace, workspace_bytes, num_views, num_triangles);
     if (st) return st;
     if (!out) return fail(DRP_STATUS_INVALID_ARGUMENT, "null output");
     drp::AAArgs a{};
@@ -347,6 +367,7 @@ DRP_API int drp_antialias_fwd(const float* color, int channels, const float* ras
     a.num_triangles = num_triangles;
     a.tri = tri;
     a.nbr = nbr;
+    a.tri_rec = workspace;
     a.B = num_views;
     a.H = height;
     a.W = width;
@@ -355,12 +376,14 @@ DRP_API int drp_antialias_fwd(const float* color, int channels, const float* ras
     return check_launch("drp_antialias_fwd");
 }
 
-DRP_API int drp_antialias_bwd(const float* color, int channels, const float* rast, const float* pos,
-                              long long pos_view_stride, long long num_vertices, const int* tri,
-                              long long num_triangles, const int* nbr, int num_views, int height, int width,
-                              const float* grad_out, float pos_gradient_boost, float* grad_color, float* grad_pos,
-                              void* stream) {
+DRP_API int drp_antialias_bwd(void* workspace, size_t workspace_bytes, const float* color, int channels,
+                              const float* rast, const float* pos, long long pos_view_stride, long long num_vertices,
+                              const int* tri, long long num_triangles, const int* nbr, int num_views, int height,
+                              int width, const float* grad_out, float pos_gradient_boost, float* grad_color,
+                              float* grad_pos, void* stream) {
     int st = aa_common(color, channels, rast, pos, pos_view_stride, tri, num_views, height, width);
+    if (st) return st;
+    st = aa_ws_check(workspace, workspace_bytes, num_views, num_triangles);
     if (st) return st;
     if (!grad_out || !grad_color) return fail(DRP_STATUS_INVALID_ARGUMENT, "null gradient pointer");
     if (!aligned(grad_pos, 16)) return fail(DRP_STATUS_INVALID_ARGUMENT, "grad_pos must be 16-byte aligned");
@@ -374,6 +397,7 @@ DRP_API int drp_antialias_bwd(const float* color, int channels, const float* ras
     a.num_triangles = num_triangles;
     a.tri = tri;
     a.nbr = nbr;
+    a.tri_rec = workspace;
     a.B = num_views;
     a.H = height;
     a.W = width;

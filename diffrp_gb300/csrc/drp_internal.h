@@ -94,6 +94,7 @@ struct AAArgs {
     long long num_triangles;
     const int* tri;
     const int* nbr;  // F x 3 neighbour table or null (every edge a silhouette)
+    void* tri_rec;   // workspace: B x F x 32-byte per-triangle records
     int B, H, W;
     float* out;
     const float* grad_out;
@@ -110,6 +111,7 @@ int launch_interp_sparse_fwd(const SparseInterpArgs& a, cudaStream_t s);
 int launch_interp_sparse_bwd(const SparseInterpArgs& a, cudaStream_t s);
 int launch_topology(const int* tri, long long F, void* ws, size_t ws_bytes, int* nbr, cudaStream_t s);
 size_t topology_ws_bytes(long long F);
+size_t aa_ws_bytes(int B, long long F);
 int launch_aa_fwd(const AAArgs& a, cudaStream_t s);
 int launch_aa_bwd(const AAArgs& a, cudaStream_t s);
 

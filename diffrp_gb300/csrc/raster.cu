@@ -237,7 +237,9 @@ __global__ void __launch_bounds__(256) fill_tiles_kernel(RasterArgs a) {
     }
 }
 
-// Rasterise one fan sub-triangle into the tile's key buffer (group-strided).
+// Rasterise one fan sub-triangle into the tile's key buffer (group-strided,
+// shared-memory atomicMin).  Used for clipped polygons, whose fan
+// sub-triangles each carry their own depth plane.
 template <int TILE_LOG2>
 __device__ __forceinline__ void raster_subtri_tile(int64_t X0, int64_t Y0, int64_t X1, int64_t Y1, int64_t X2,
                                                    int64_t Y2, const Plane& pl, uint32_t tri, int tx0, int ty0,
@@ -252,10 +254,10 @@ __device__ __forceinline__ void raster_subtri_tile(int64_t X0, int64_t Y0, int64
     }
     int64_t mnx = min(min(X0, X1), X2), mxx = max(max(X0, X1), X2);
     int64_t mny = min(min(Y0, Y1), Y2), mxy = max(max(Y0, Y1), Y2);
-    int x0 = (int)max(ceil_shift(mnx - DRP_HALF_SUBPIX), (int64_t)tx0);
-    int x1 = (int)min(floor_shift(mxx - DRP_HALF_SUBPIX), (int64_t)min(tx0 + T - 1, W - 1));
-    int y0 = (int)max(ceil_shift(mny - DRP_HALF_SUBPIX), (int64_t)ty0);
-    int y1 = (int)min(floor_shift(mxy - DRP_HALF_SUBPIX), (int64_t)min(ty0 + T - 1, H - 1));
+    const int x0 = (int)max(ceil_shift(mnx - DRP_HALF_SUBPIX), (int64_t)tx0);
+    const int x1 = (int)min(floor_shift(mxx - DRP_HALF_SUBPIX), (int64_t)min(tx0 + T - 1, W - 1));
+    const int y0 = (int)max(ceil_shift(mny - DRP_HALF_SUBPIX), (int64_t)ty0);
+    const int y1 = (int)min(floor_shift(mxy - DRP_HALF_SUBPIX), (int64_t)min(ty0 + T - 1, H - 1));
     if (x0 > x1 || y0 > y1) return;
     const int w = x1 - x0 + 1;
     const int n = w * (y1 - y0 + 1);
@@ -293,86 +295,233 @@ __device__ __noinline__ void raster_complex_tile(const RasterArgs& a, int b, uin
     }
 }
 
-template <int TILE_LOG2>
-__device__ __forceinline__ void raster_prim(const RasterArgs& a, int b, long long pidx, int tx0, int ty0, int rank,
-                                            int group, unsigned long long* keys, const unsigned long long* prev) {
-    constexpr int T = 1 << TILE_LOG2;
-    const int4* rec = reinterpret_cast<const int4*>(a.ws.prims) + pidx * 3;
+// A primitive prepared for one tile.  Edge k passes at tile pixel (dx, dy)
+// when C[k] + A[k] dx + B[k] dy >= 0 (top-left bias folded into C).  Edges
+// that accept every pixel of the tile are reduced to A = B = C = 0.  BIG
+// primitives have an edge too long for 32-bit steps and are tested in 64-bit
+// from the (oriented) vertices.
+#define TP_ACTIVE 1
+#define TP_BIG 2
+#define TP_COMPLEX 4
+
+struct __align__(16) TilePrim {
+    int4 e0;    // A0, B0, C0, A1
+    int4 e1;    // B1, C1, A2, B2
+    int4 e2;    // C2, flags, X0, Y0
+    float4 z;   // Z0, Az, Bz, tri (bits)
+    int4 v01;   // oriented vertices for the BIG path: x0, y0, x1, y1
+    int4 v2b;   // x2, y2, local bbox x0 | x1 << 16, y0 | y1 << 16
+};
+
+template <int T>
+__device__ __forceinline__ void prepare_tile_prim(const int4* rec, int tx0, int ty0, int W, int H, TilePrim& tp) {
+    tp.e2.y = 0;
     const int4 r1 = rec[1], r2 = rec[2];
     const PrimBox bx = unpack_box(r1, r2);
     if (bx.px0 > bx.px1 || bx.px1 < tx0 || bx.px0 >= tx0 + T || bx.py1 < ty0 || bx.py0 >= ty0 + T) return;
+    tp.z.w = __int_as_float(r1.z);
+    const int lx0 = max(bx.px0, tx0) - tx0, lx1 = min(min(bx.px1, tx0 + T - 1), W - 1) - tx0;
+    const int ly0 = max(bx.py0, ty0) - ty0, ly1 = min(min(bx.py1, ty0 + T - 1), H - 1) - ty0;
+    tp.v2b.z = lx0 | (lx1 << 16);
+    tp.v2b.w = ly0 | (ly1 << 16);
     if (bx.complex_) {
-        raster_complex_tile<TILE_LOG2>(a, b, (uint32_t)r1.z, tx0, ty0, rank, group, keys, prev);
+        tp.e2.y = TP_COMPLEX;
         return;
     }
     const int4 r0 = rec[0];
-    Plane pl;
-    pl.Z0 = __int_as_float(r2.x);
-    pl.A = __int_as_float(r2.y);
-    pl.B = __int_as_float(r2.z);
-    raster_subtri_tile<TILE_LOG2>(r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, pl, (uint32_t)r1.z, tx0, ty0, a.W, a.H, rank,
-                                  group, keys, prev);
-}
-
-template <int TILE_LOG2, int TPT>
-__global__ void __launch_bounds__(256) fine_raster_kernel(RasterArgs a) {
-    constexpr int T = 1 << TILE_LOG2;
-    constexpr int NPIX = T * T;
-    constexpr int NTHREADS = 256;
-    constexpr int GROUPS = NTHREADS / TPT;
-    __shared__ unsigned long long keys[NPIX];
-    __shared__ unsigned long long prevk[NPIX];
-    __shared__ uint32_t chunk[GROUPS];
-
-    const int tiles_x = (a.W + T - 1) >> TILE_LOG2;
-    const int tiles_y = (a.H + T - 1) >> TILE_LOG2;
-    const long long ntiles = (long long)tiles_x * tiles_y;
-    const int b = (int)(blockIdx.x / ntiles);
-    const int tile = (int)(blockIdx.x % ntiles);
-    const int tx0 = (tile % tiles_x) << TILE_LOG2, ty0 = (tile / tiles_x) << TILE_LOG2;
-    const long long npix_view = (long long)a.H * a.W;
-    const int tid = threadIdx.x;
-
-    for (int i = tid; i < NPIX; i += NTHREADS) {
-        keys[i] = ~0ull;
-        if (a.prev_key) {
-            const int px = tx0 + (i & (T - 1)), py = ty0 + (i >> TILE_LOG2);
-            prevk[i] = (px < a.W && py < a.H) ? a.prev_key[b * npix_view + (long long)py * a.W + px] : ~0ull;
+    const int64_t X0 = r0.x, Y0 = r0.y, X1 = r0.z, Y1 = r0.w, X2 = r1.x, Y2 = r1.y;
+    const int64_t area2 = (X1 - X0) * (Y2 - Y0) - (Y1 - Y0) * (X2 - X0);
+    int64_t vx[3] = {X0, X1, X2}, vy[3] = {Y0, Y1, Y2};
+    if (area2 < 0) {
+        vx[1] = X2; vy[1] = Y2; vx[2] = X1; vy[2] = Y1;
+    }
+    const int64_t ox = (int64_t)tx0 * DRP_SUBPIX + DRP_HALF_SUBPIX;
+    const int64_t oy = (int64_t)ty0 * DRP_SUBPIX + DRP_HALF_SUBPIX;
+    bool big = false;
+    int A[3], B[3], C[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int p = (k + 1) % 3, q = (k + 2) % 3;  // edges b->c, c->a, a->b
+        const int64_t dx = vx[q] - vx[p], dy = vy[q] - vy[p];
+        const bool tl = (dy < 0) || (dy == 0 && dx < 0);
+        const int64_t Cb = dx * (oy - vy[p]) - dy * (ox - vx[p]) - (tl ? 0 : 1);
+        const int64_t SX = -dy * DRP_SUBPIX, SY = dx * DRP_SUBPIX;
+        const int64_t lo = (min(SX, (int64_t)0) + min(SY, (int64_t)0)) * (T - 1);
+        const int64_t hi = (max(SX, (int64_t)0) + max(SY, (int64_t)0)) * (T - 1);
+        A[k] = B[k] = C[k] = 0;
+        if (Cb + hi < 0) return;  // no pixel centre of the tile is inside this edge
+        if (Cb + lo >= 0) continue;  // every pixel centre of the tile is inside
+        if (hi - lo < ((int64_t)1 << 30)) {
+            A[k] = (int)SX;
+            B[k] = (int)SY;
+            C[k] = (int)Cb;
+        } else {
+            big = true;
         }
     }
-    __syncthreads();
-    const unsigned long long* prev = a.prev_key ? prevk : nullptr;
+    tp.e0 = make_int4(A[0], B[0], C[0], A[1]);
+    tp.e1 = make_int4(B[1], C[1], A[2], B[2]);
+    tp.e2 = make_int4(C[2], TP_ACTIVE | (big ? TP_BIG : 0), (int)X0, (int)Y0);
+    tp.z.x = __int_as_float(r2.x);
+    tp.z.y = __int_as_float(r2.y);
+    tp.z.z = __int_as_float(r2.z);
+    tp.v01 = make_int4((int)vx[0], (int)vy[0], (int)vx[1], (int)vy[1]);
+    tp.v2b.x = (int)vx[2];
+    tp.v2b.y = (int)vy[2];
+}
 
-    const int rank = tid % TPT, grp = tid / TPT;
-    const long long tidx = (long long)b * ntiles + tile;
+__device__ __forceinline__ bool tile_prim_covers(const TilePrim& tp, const int4& e0, const int4& e1, const int4& e2,
+                                                 int dx, int dy, int sx, int sy) {
+    if (!(e2.y & TP_BIG)) {
+        return (e0.z + e0.x * dx + e0.y * dy >= 0) && (e1.y + e0.w * dx + e1.x * dy >= 0) &&
+               (e2.x + e1.z * dx + e1.w * dy >= 0);
+    }
+    const int4 v01 = tp.v01, v2b = tp.v2b;
+    return edge_inside(v01.z, v01.w, v2b.x, v2b.y, sx, sy) && edge_inside(v2b.x, v2b.y, v01.x, v01.y, sx, sy) &&
+           edge_inside(v01.x, v01.y, v01.z, v01.w, sx, sy);
+}
+
+__device__ __forceinline__ unsigned long long tile_prim_key(const float4& z4, int X0, int Y0, int sx, int sy,
+                                                            bool& ok) {
+    const float z = (z4.x + z4.y * (float)(sx - X0)) + z4.z * (float)(sy - Y0);
+    ok = (z >= -1.0f && z <= 1.0f);
+    return ((unsigned long long)depth_order(z) << 32) | (unsigned long long)__float_as_uint(z4.w);
+}
+
+// Fine raster + shade, one CTA per (tile, view).
+//   TPT == 0: every thread owns T*T/NTHREADS pixels and tests them against
+//             each primitive of the tile (keys in registers, no atomics);
+//   TPT  > 0: groups of TPT threads walk one primitive's bbox within the tile
+//             and resolve keys with shared-memory atomicMin.
+template <int TILE_LOG2, int TPT>
+__global__ void __launch_bounds__((1 << (2 * TILE_LOG2)) < 256 ? (1 << (2 * TILE_LOG2)) : 256)
+fine_raster_kernel(RasterArgs a) {
+    constexpr int T = 1 << TILE_LOG2;
+    constexpr int NPIX = T * T;
+    constexpr int NTHREADS = NPIX < 256 ? NPIX : 256;
+    constexpr int PPT = NPIX / NTHREADS;
+    constexpr int CHUNK = NTHREADS;
+    constexpr int GROUPS = TPT > 0 ? NTHREADS / TPT : 1;
+    __shared__ unsigned long long keys[NPIX];
+    __shared__ TilePrim prims[CHUNK];
+    __shared__ int n_complex;
+
+    const int b = blockIdx.y;
+    const int tile = blockIdx.x;
+    const int tx0 = (tile % a.tiles_x) << TILE_LOG2, ty0 = (tile / a.tiles_x) << TILE_LOG2;
+    const int npix_view = a.H * a.W;
+    const int tid = threadIdx.x;
+    const unsigned long long* prev_g = a.prev_key ? a.prev_key + (long long)b * npix_view : nullptr;
+
+    unsigned long long best[PPT], prevk[PPT];
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+        const int i = tid + q * NTHREADS;
+        const int px = tx0 + (i & (T - 1)), py = ty0 + (i >> TILE_LOG2);
+        best[q] = ~0ull;
+        prevk[q] = 0;
+        if (prev_g) prevk[q] = (px < a.W && py < a.H) ? prev_g[py * a.W + px] : ~0ull;
+        if (TPT > 0) keys[i] = ~0ull;
+    }
+    if (tid == 0) n_complex = 0;
+
+    const long long tidx = (long long)b * a.tiles_x * a.tiles_y + tile;
     const uint32_t cnt = a.ws.tile_count[tidx];
     const uint32_t off = a.ws.tile_offset[tidx];
     const bool overflow = (unsigned long long)off + cnt > (unsigned long long)a.list_capacity;
-    if (!overflow) {
-        for (uint32_t base = 0; base < cnt; base += GROUPS) {
-            if (tid < GROUPS) chunk[tid] = (base + tid < cnt) ? a.ws.tile_list[off + base + tid] : 0xffffffffu;
-            __syncthreads();
-            const uint32_t p = chunk[grp];
-            if (p != 0xffffffffu) raster_prim<TILE_LOG2>(a, b, (long long)p, tx0, ty0, rank, TPT, keys, prev);
-            __syncthreads();
+    const long long pbase = (long long)b * a.max_view_tris;
+    const long long total = overflow ? a.max_view_tris : (long long)cnt;
+    const int4* recs = reinterpret_cast<const int4*>(a.ws.prims);
+    if (overflow && tid == 0) atomicOr(a.ws.stats + 2, DRP_DEVERR_LIST_OVERFLOW);
+    __syncthreads();
+
+    for (long long base = 0; base < total; base += CHUNK) {
+        const int n = (int)min((long long)CHUNK, total - base);
+        if (tid < n) {
+            const long long pidx = overflow ? pbase + base + tid : (long long)a.ws.tile_list[off + base + tid];
+            prepare_tile_prim<T>(recs + pidx * 3, tx0, ty0, a.W, a.H, prims[tid]);
+            if (prims[tid].e2.y & TP_COMPLEX) atomicAdd(&n_complex, 1);
         }
-    } else {
-        // Capacity overflow: scan every primitive of this view.
-        const long long pbase = (long long)b * a.max_view_tris;
-        for (long long base = 0; base < a.max_view_tris; base += GROUPS) {
-            const long long j = base + grp;
-            if (j < a.max_view_tris) raster_prim<TILE_LOG2>(a, b, pbase + j, tx0, ty0, rank, TPT, keys, prev);
+        __syncthreads();
+        if (TPT == 0) {
+            for (int j = 0; j < n; ++j) {
+                const TilePrim& tp = prims[j];
+                const int4 e2 = tp.e2;
+                if (!(e2.y & TP_ACTIVE)) continue;
+                const int4 e0 = tp.e0, e1 = tp.e1;
+#pragma unroll
+                for (int q = 0; q < PPT; ++q) {
+                    const int i = tid + q * NTHREADS;
+                    const int dx = i & (T - 1), dy = i >> TILE_LOG2;
+                    const int sx = (tx0 + dx) * DRP_SUBPIX + DRP_HALF_SUBPIX;
+                    const int sy = (ty0 + dy) * DRP_SUBPIX + DRP_HALF_SUBPIX;
+                    if (!tile_prim_covers(tp, e0, e1, e2, dx, dy, sx, sy)) continue;
+                    bool ok;
+                    const unsigned long long k = tile_prim_key(tp.z, e2.z, e2.w, sx, sy, ok);
+                    if (ok && k < best[q] && (!prev_g || k > prevk[q])) best[q] = k;
+                }
+            }
+        } else {
+            constexpr int G = TPT > 0 ? TPT : 1;
+            const int rank = tid % G;
+            for (int j = tid / G; j < n; j += GROUPS) {
+                const TilePrim& tp = prims[j];
+                const int4 e2 = tp.e2;
+                if (!(e2.y & TP_ACTIVE)) continue;
+                const int4 e0 = tp.e0, e1 = tp.e1, v2b = tp.v2b;
+                const int x0 = v2b.z & 0xffff, x1 = v2b.z >> 16, y0 = v2b.w & 0xffff, y1 = v2b.w >> 16;
+                for (int dy = y0; dy <= y1; ++dy) {
+                    for (int dx = x0 + rank; dx <= x1; dx += G) {
+                        const int sx = (tx0 + dx) * DRP_SUBPIX + DRP_HALF_SUBPIX;
+                        const int sy = (ty0 + dy) * DRP_SUBPIX + DRP_HALF_SUBPIX;
+                        if (!tile_prim_covers(tp, e0, e1, e2, dx, dy, sx, sy)) continue;
+                        bool ok;
+                        const unsigned long long k = tile_prim_key(tp.z, e2.z, e2.w, sx, sy, ok);
+                        if (!ok) continue;
+                        const int li = (dy << TILE_LOG2) + dx;
+                        if (prev_g && !(k > prev_g[(ty0 + dy) * a.W + tx0 + dx])) continue;
+                        if (k < keys[li]) atomicMin(keys + li, k);
+                    }
+                }
+            }
         }
-        if (tid == 0) atomicOr(a.ws.stats + 2, DRP_DEVERR_LIST_OVERFLOW);
+        __syncthreads();
+    }
+    if (TPT == 0) {
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) keys[tid + q * NTHREADS] = best[q];
     }
     __syncthreads();
+    if (n_complex > 0) {
+        // Clipped polygons (rare): second pass over the list, group-parallel.
+        __shared__ unsigned long long prev_s[NPIX];
+        if (prev_g) {
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) prev_s[tid + q * NTHREADS] = prevk[q];
+        }
+        __syncthreads();
+        constexpr int CG = 8;
+        for (long long j = tid / CG; j < total; j += NTHREADS / CG) {
+            const long long pidx = overflow ? pbase + j : (long long)a.ws.tile_list[off + j];
+            const int4 r1 = recs[pidx * 3 + 1], r2 = recs[pidx * 3 + 2];
+            const PrimBox bx = unpack_box(r1, r2);
+            if (!bx.complex_ || bx.px0 > bx.px1 || bx.px1 < tx0 || bx.px0 >= tx0 + T || bx.py1 < ty0 ||
+                bx.py0 >= ty0 + T)
+                continue;
+            raster_complex_tile<TILE_LOG2>(a, b, (uint32_t)r1.z, tx0, ty0, tid % CG, CG, keys,
+                                           prev_g ? prev_s : nullptr);
+        }
+        __syncthreads();
+    }
 
     // Shade.
     const float4* P = reinterpret_cast<const float4*>(a.pos + (long long)b * a.pos_view_stride);
-    for (int i = tid; i < NPIX; i += NTHREADS) {
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+        const int i = tid + q * NTHREADS;
         const int px = tx0 + (i & (T - 1)), py = ty0 + (i >> TILE_LOG2);
         if (px >= a.W || py >= a.H) continue;
-        const long long o = b * npix_view + (long long)py * a.W + px;
+        const long long o = (long long)b * npix_view + py * a.W + px;
         const unsigned long long k = keys[i];
         float4 r = make_float4(0.f, 0.f, 0.f, 0.f), d = make_float4(0.f, 0.f, 0.f, 0.f);
         if (k != ~0ull) {
@@ -446,14 +595,17 @@ __global__ void __launch_bounds__(256) raster_bwd_kernel(RasterBwdArgs a) {
 // Host-side launchers.
 // ---------------------------------------------------------------------------
 template <int TL>
-static void launch_fine(const RasterArgs& a, int tpt, long long nblocks, cudaStream_t s) {
+static void launch_fine(const RasterArgs& a, int tpt, cudaStream_t s) {
+    constexpr int NT = (1 << (2 * TL)) < 256 ? (1 << (2 * TL)) : 256;
+    dim3 grid((unsigned)(a.tiles_x * a.tiles_y), (unsigned)a.B);
     switch (tpt) {
-    case 1: fine_raster_kernel<TL, 1><<<(unsigned)nblocks, 256, 0, s>>>(a); break;
-    case 2: fine_raster_kernel<TL, 2><<<(unsigned)nblocks, 256, 0, s>>>(a); break;
-    case 4: fine_raster_kernel<TL, 4><<<(unsigned)nblocks, 256, 0, s>>>(a); break;
-    case 8: fine_raster_kernel<TL, 8><<<(unsigned)nblocks, 256, 0, s>>>(a); break;
-    case 16: fine_raster_kernel<TL, 16><<<(unsigned)nblocks, 256, 0, s>>>(a); break;
-    default: fine_raster_kernel<TL, 32><<<(unsigned)nblocks, 256, 0, s>>>(a); break;
+    case 0: fine_raster_kernel<TL, 0><<<grid, NT, 0, s>>>(a); break;
+    case 1: fine_raster_kernel<TL, 1><<<grid, NT, 0, s>>>(a); break;
+    case 2: fine_raster_kernel<TL, 2><<<grid, NT, 0, s>>>(a); break;
+    case 4: fine_raster_kernel<TL, 4><<<grid, NT, 0, s>>>(a); break;
+    case 8: fine_raster_kernel<TL, 8><<<grid, NT, 0, s>>>(a); break;
+    case 16: fine_raster_kernel<TL, 16><<<grid, NT, 0, s>>>(a); break;
+    default: fine_raster_kernel<TL, 32><<<grid, NT, 0, s>>>(a); break;
     }
 }
 
@@ -481,9 +633,9 @@ int launch_rasterize(const RasterArgs& a, cudaStream_t s) {
         cudaMemsetAsync(a.ws.tile_offset, 0, sizeof(uint32_t) * ntiles, s);
     }
     switch (a.tile_log2) {
-    case 3: launch_fine<3>(a, a.threads_per_tri, ntiles, s); break;
-    case 5: launch_fine<5>(a, a.threads_per_tri, ntiles, s); break;
-    default: launch_fine<4>(a, a.threads_per_tri, ntiles, s); break;
+    case 3: launch_fine<3>(a, a.threads_per_tri, s); break;
+    case 5: launch_fine<5>(a, a.threads_per_tri, s); break;
+    default: launch_fine<4>(a, a.threads_per_tri, s); break;
     }
     return 0;
 }

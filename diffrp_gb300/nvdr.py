@@ -17,6 +17,7 @@ CUDA (``libdiffrp_gb300.so`` through ``_ffi``).  There is no CPU path: every op
 requires CUDA tensors and the built library.
 """
 import numbers
+import threading
 
 import torch
 
@@ -83,12 +84,13 @@ class RasterizeCudaContext:
     back asynchronously; an undersized call is still exact (overflowing tiles
     scan all primitives of their view).
 
-    ``tile_log2`` (3/4/5) and ``threads_per_tri`` (power of two <= 32) are the
-    fine-raster tuning knobs (see ``diffrp_gb300.autotune``).  ``validate``
+    ``tile_log2`` (3/4/5: 8/16/32-pixel tiles) and ``threads_per_tri`` (0 =
+    pixel-parallel tiles, else a power of two <= 32 threads per primitive) are
+    the fine-raster tuning knobs (see ``diffrp_gb300.autotune``).  ``validate``
     makes every rasterisation synchronise and raise on out-of-range indices.
     """
 
-    def __init__(self, device=None, tile_log2=4, threads_per_tri=8, validate=False):
+    def __init__(self, device=None, tile_log2=4, threads_per_tri=0, validate=False):
         if device is None:
             device = torch.device("cuda", torch.cuda.current_device())
         else:
@@ -402,15 +404,23 @@ def interpolate(attr, rast, tri, rast_db=None, diff_attrs=None):
 # ---------------------------------------------------------------------------
 # Antialias
 # ---------------------------------------------------------------------------
-class _TopologyCache:
-    _ctx = {}
+class _Scratch(threading.local):
+    """Per-thread, per-device scratch buffers for the context-free ops
+    (topology construction and antialiasing)."""
 
-    @classmethod
-    def context(cls, device):
-        key = (device.type, device.index)
-        if key not in cls._ctx:
-            cls._ctx[key] = RasterizeCudaContext(device)
-        return cls._ctx[key]
+    def __init__(self):
+        self.buffers = {}
+
+    def get(self, device, name, nbytes):
+        key = (device.index, name)
+        buf = self.buffers.get(key)
+        if buf is None or buf.numel() < nbytes:
+            buf = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=device)
+            self.buffers[key] = buf
+        return buf
+
+
+_scratch = _Scratch()
 
 
 def antialias_construct_topology_hash(tri):
@@ -423,7 +433,7 @@ def antialias_construct_topology_hash(tri):
     F = tri.shape[0]
     nbr = torch.empty((F, 3), dtype=torch.int32, device=tri.device)
     if F:
-        ws = _TopologyCache.context(tri.device).topology_workspace(F)
+        ws = _scratch.get(tri.device, "topology", _ffi.size_out("drp_topology_workspace_size", F))
         _ffi.call("drp_antialias_topology", ws.data_ptr(), ws.numel(), tri.data_ptr(), F, nbr.data_ptr(),
                   _stream(tri.device))
     return nbr
@@ -435,8 +445,10 @@ class _AntialiasFn(torch.autograd.Function):
         B, H, W, C = color.shape
         stride = pos.shape[1] * 4 if pos.dim() == 3 else 0
         out = torch.empty_like(color)
-        _ffi.call("drp_antialias_fwd", color.data_ptr(), C, rast.data_ptr(), pos.data_ptr(), stride, pos.shape[-2],
-                  tri.data_ptr(), tri.shape[0], nbr.data_ptr(), B, H, W, out.data_ptr(), _stream(color.device))
+        ws = _scratch.get(color.device, "antialias", _ffi.size_out("drp_antialias_workspace_size", B, tri.shape[0]))
+        _ffi.call("drp_antialias_fwd", ws.data_ptr(), ws.numel(), color.data_ptr(), C, rast.data_ptr(),
+                  pos.data_ptr(), stride, pos.shape[-2], tri.data_ptr(), tri.shape[0], nbr.data_ptr(), B, H, W,
+                  out.data_ptr(), _stream(color.device))
         ctx.save_for_backward(color, rast, pos, tri, nbr)
         ctx.meta = (B, H, W, C, stride, boost)
         return out
@@ -449,9 +461,10 @@ class _AntialiasFn(torch.autograd.Function):
         grad_color = torch.empty_like(color)
         need_pos = ctx.needs_input_grad[2]
         grad_pos = torch.zeros_like(pos) if need_pos else None
-        _ffi.call("drp_antialias_bwd", color.data_ptr(), C, rast.data_ptr(), pos.data_ptr(), stride, pos.shape[-2],
-                  tri.data_ptr(), tri.shape[0], nbr.data_ptr(), B, H, W, grad_out.data_ptr(), float(boost),
-                  grad_color.data_ptr(), _ptr(grad_pos), _stream(color.device))
+        ws = _scratch.get(color.device, "antialias", _ffi.size_out("drp_antialias_workspace_size", B, tri.shape[0]))
+        _ffi.call("drp_antialias_bwd", ws.data_ptr(), ws.numel(), color.data_ptr(), C, rast.data_ptr(),
+                  pos.data_ptr(), stride, pos.shape[-2], tri.data_ptr(), tri.shape[0], nbr.data_ptr(), B, H, W,
+                  grad_out.data_ptr(), float(boost), grad_color.data_ptr(), _ptr(grad_pos), _stream(color.device))
         return grad_color, None, grad_pos, None, None, None
 
 

@@ -77,8 +77,11 @@ int drp_raster_workspace_size(int num_views, long long max_view_tris, int height
  *   ranges           device int32 [num_views][2] = (first triangle, count), or
  *                    NULL for all triangles in every view (instanced mode).
  *   max_view_tris    max over views of the triangle count.
- *   tile_log2        3, 4 or 5 (8, 16, 32 pixel tiles); threads_per_tri in
- *                    {1, 2, 4, 8, 16, 32}.
+ *   tile_log2        3, 4 or 5 (8, 16, 32 pixel tiles).
+ *   threads_per_tri  0: every thread owns pixels of the tile and tests them
+ *                    against each primitive (no atomics); 1, 2, 4, 8, 16 or
+ *                    32: that many threads walk one primitive's bounding box
+ *                    and resolve depth with shared-memory atomics.
  *   prev_key         previous layer's keys (depth peeling) or NULL.
  *   rast             out (B, H, W, 4); rast_db out (B, H, W, 4) or NULL;
  *   out_key          out (B, H, W) uint64 visibility keys or NULL.
@@ -153,21 +156,27 @@ int drp_topology_workspace_size(long long num_triangles, size_t* bytes);
 int drp_antialias_topology(void* workspace, size_t workspace_bytes, const int* tri, long long num_triangles,
                            int* nbr, void* stream);
 
+/* Workspace bytes for drp_antialias_fwd / drp_antialias_bwd (32 bytes per
+ * view and triangle: screen-space vertices and silhouette-edge mask). */
+int drp_antialias_workspace_size(int num_views, long long num_triangles, size_t* bytes);
+
 /*
  * dr.antialias(color, rast, pos, tri) (diffrp/rendering/surface_deferred.py:775).
  * color (B, H, W, C); nbr from drp_antialias_topology or NULL (every edge
- * is treated as a silhouette).
+ * is treated as a silhouette).  The workspace is scratch for this call only.
  */
-int drp_antialias_fwd(const float* color, int channels, const float* rast, const float* pos,
-                      long long pos_view_stride, long long num_vertices, const int* tri, long long num_triangles,
-                      const int* nbr, int num_views, int height, int width, float* out, void* stream);
+int drp_antialias_fwd(void* workspace, size_t workspace_bytes, const float* color, int channels, const float* rast,
+                      const float* pos, long long pos_view_stride, long long num_vertices, const int* tri,
+                      long long num_triangles, const int* nbr, int num_views, int height, int width, float* out,
+                      void* stream);
 
 /* Backward: grad_color overwritten, grad_pos accumulated (times
  * pos_gradient_boost); grad_pos may be NULL. */
-int drp_antialias_bwd(const float* color, int channels, const float* rast, const float* pos,
-                      long long pos_view_stride, long long num_vertices, const int* tri, long long num_triangles,
-                      const int* nbr, int num_views, int height, int width, const float* grad_out,
-                      float pos_gradient_boost, float* grad_color, float* grad_pos, void* stream);
+int drp_antialias_bwd(void* workspace, size_t workspace_bytes, const float* color, int channels, const float* rast,
+                      const float* pos, long long pos_view_stride, long long num_vertices, const int* tri,
+                      long long num_triangles, const int* nbr, int num_views, int height, int width,
+                      const float* grad_out, float pos_gradient_boost, float* grad_color, float* grad_pos,
+                      void* stream);
 
 #ifdef __cplusplus
 }
