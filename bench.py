@@ -178,7 +178,7 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10):
+def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None):
     """CUDA-event time of each C-ABI entry point of the step on the same
     inputs (current stream), L2 flushed between repetitions."""
     import torch
@@ -187,6 +187,9 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10):
     s = torch.cuda.current_stream(dev)
     sp = s.cuda_stream
     ctx = dr.RasterizeCudaContext(dev)
+    if tuned is not None:
+        from diffrp_gb300 import autotune
+        autotune.apply(ctx, tuned)
     tri = torch.from_numpy(f).to(dev)
     v_t = torch.from_numpy(verts).to(dev)
     clip = (torch.nn.functional.pad(v_t, (0, 1), value=1.0) @ torch.from_numpy(mvp).to(dev).T).contiguous()
@@ -322,6 +325,10 @@ def main():
 
     verts_np, f, attr_np, mvp, target = make_workload()
     step = Step(dev, f, mvp, target)
+    from diffrp_gb300 import autotune
+    with torch.no_grad():
+        clip0 = (torch.nn.functional.pad(torch.from_numpy(verts_np).to(dev), (0, 1), value=1.0) @ step.mvp.T)
+    tuned = autotune.tune_rasterizer(step.ctx, clip0.contiguous(), step.tri, (H, W), use_cache=False)
     verts = torch.from_numpy(verts_np).to(dev).requires_grad_(True)
     attr = torch.from_numpy(attr_np).to(dev).requires_grad_(True)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -394,7 +401,7 @@ def main():
     d2h = 4 + h_gv.numel() * 4 + h_ga.numel() * 4
 
     if rank == 0:
-        times, algo = kernel_breakdown(dev, verts_np, f, attr_np, mvp, target)
+        times, algo = kernel_breakdown(dev, verts_np, f, attr_np, mvp, target, tuned=tuned)
         dom = max(times, key=times.get)
         peak, peak_kind = _peaks()
         achieved = algo[dom] / (times[dom] / 1e3) / 1e9
@@ -412,7 +419,9 @@ def main():
                        "global_batch": world, "resolution": [H, W], "channels": C,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "flushed between steps (256 MiB write outside the timed events)",
-                       "path": "drop-in nvdr API ops, whole fwd+bwd step captured as one CUDA graph"},
+                       "path": "drop-in nvdr API ops, whole fwd+bwd step captured as one CUDA graph",
+                       "raster_tuning": {"tile": 1 << tuned["tile_log2"], "threads_per_tri": tuned["threads_per_tri"],
+                                         "list_capacity": tuned["list_capacity"]}},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,

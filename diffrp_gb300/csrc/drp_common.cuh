@@ -194,10 +194,21 @@ struct Shade {
     float X, Y, kx, ky;
 };
 
+// NDC coordinate of the centre of pixel column / row `p` at resolution `res`.
+__device__ __forceinline__ float pixel_ndc(int p, int res) { return (float)(2 * p + 1) / (float)res - 1.0f; }
+
+__device__ __forceinline__ void shade_eval_xy(const float4& p0, const float4& p1, const float4& p2, float X, float Y,
+                                              int W, int H, Shade& S);
+
 __device__ __forceinline__ void shade_eval(const float4& p0, const float4& p1, const float4& p2, int px, int py,
                                            int W, int H, Shade& S) {
-    S.X = (float)(2 * px + 1) / (float)W - 1.0f;
-    S.Y = (float)(2 * py + 1) / (float)H - 1.0f;
+    shade_eval_xy(p0, p1, p2, pixel_ndc(px, W), pixel_ndc(py, H), W, H, S);
+}
+
+__device__ __forceinline__ void shade_eval_xy(const float4& p0, const float4& p1, const float4& p2, float X, float Y,
+                                              int W, int H, Shade& S) {
+    S.X = X;
+    S.Y = Y;
     S.a[0] = p0.x - S.X * p0.w;
     S.a[1] = p1.x - S.X * p1.w;
     S.a[2] = p2.x - S.X * p2.w;

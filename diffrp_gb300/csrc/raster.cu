@@ -394,17 +394,19 @@ __device__ __forceinline__ unsigned long long tile_prim_key(const float4& z4, in
 //   TPT  > 0: groups of TPT threads walk one primitive's bbox within the tile
 //             and resolve keys with shared-memory atomicMin.
 template <int TILE_LOG2, int TPT>
-__global__ void __launch_bounds__((1 << (2 * TILE_LOG2)) < 256 ? (1 << (2 * TILE_LOG2)) : 256)
+__global__ void __launch_bounds__((1 << (2 * TILE_LOG2)) < 256 ? (1 << (2 * TILE_LOG2)) : 256,
+                                  TILE_LOG2 == 3 ? 12 : 3)
 fine_raster_kernel(RasterArgs a) {
     constexpr int T = 1 << TILE_LOG2;
     constexpr int NPIX = T * T;
     constexpr int NTHREADS = NPIX < 256 ? NPIX : 256;
     constexpr int PPT = NPIX / NTHREADS;
-    constexpr int CHUNK = NTHREADS;
+    constexpr int CHUNK = NTHREADS < 128 ? NTHREADS : 128;
     constexpr int GROUPS = TPT > 0 ? NTHREADS / TPT : 1;
     __shared__ unsigned long long keys[NPIX];
     __shared__ TilePrim prims[CHUNK];
     __shared__ int n_complex;
+    __shared__ float col_ndc[T], row_ndc[T];
 
     const int b = blockIdx.y;
     const int tile = blockIdx.x;
@@ -424,6 +426,8 @@ fine_raster_kernel(RasterArgs a) {
         if (TPT > 0) keys[i] = ~0ull;
     }
     if (tid == 0) n_complex = 0;
+    if (tid < T) col_ndc[tid] = pixel_ndc(tx0 + tid, a.W);
+    else if (tid < 2 * T) row_ndc[tid - T] = pixel_ndc(ty0 + tid - T, a.H);
 
     const long long tidx = (long long)b * a.tiles_x * a.tiles_y + tile;
     const uint32_t cnt = a.ws.tile_count[tidx];
@@ -437,7 +441,7 @@ fine_raster_kernel(RasterArgs a) {
 
     for (long long base = 0; base < total; base += CHUNK) {
         const int n = (int)min((long long)CHUNK, total - base);
-        if (tid < n) {
+        if (tid < n && tid < CHUNK) {
             const long long pidx = overflow ? pbase + base + tid : (long long)a.ws.tile_list[off + base + tid];
             prepare_tile_prim<T>(recs + pidx * 3, tx0, ty0, a.W, a.H, prims[tid]);
             if (prims[tid].e2.y & TP_COMPLEX) atomicAdd(&n_complex, 1);
@@ -529,7 +533,7 @@ fine_raster_kernel(RasterArgs a) {
             const int i0 = a.tri[3 * (long long)t], i1 = a.tri[3 * (long long)t + 1], i2 = a.tri[3 * (long long)t + 2];
             const float4 p0 = P[i0], p1 = P[i1], p2 = P[i2];
             Shade S;
-            shade_eval(p0, p1, p2, px, py, a.W, a.H, S);
+            shade_eval_xy(p0, p1, p2, col_ndc[i & (T - 1)], row_ndc[i >> TILE_LOG2], a.W, a.H, S);
             r = make_float4(S.u, S.v, S.zw, enc_triid(t + 1));
             if (a.rast_db) d = shade_db(S);
         }

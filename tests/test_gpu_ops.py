@@ -210,3 +210,18 @@ def test_sparse_interpolate(cuda_lib):
     _grad_close(vb_t.grad.cpu().numpy(), gvb)
     gu = (go * (vb[ti[:, 0]] - vb[ti[:, 2]])).sum(1)
     _grad_close(vi_t.grad.cpu().numpy()[:, 0], gu)
+
+
+def test_autotuner_choice_is_exact(cuda_lib, tmp_path, monkeypatch):
+    from diffrp_gb300 import autotune
+    monkeypatch.setenv("DRP_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    pos, tri = scenes.sphere_view(3, res=(96, 96), sigma=0.02, seed=5)
+    ctx = _ctx()
+    choice = autotune.tune_rasterizer(ctx, _t(pos), _t(tri), (96, 96), reps=2,
+                                      candidates=[(3, 0), (4, 0), (4, 8), (5, 1)])
+    assert (ctx.tile_log2, ctx.threads_per_tri) == (choice["tile_log2"], choice["threads_per_tri"])
+    rast, _ = _dr().rasterize(ctx, _t(pos), _t(tri), (96, 96), grad_db=False)
+    ref, _, _ = O.rasterize(pos, tri, (96, 96), grad_db=False)
+    np.testing.assert_array_equal(rast.cpu().numpy(), ref)
+    again = autotune.tune_rasterizer(_ctx(), _t(pos), _t(tri), (96, 96))
+    assert again["tile_log2"] == choice["tile_log2"] and again["threads_per_tri"] == choice["threads_per_tri"]
