@@ -180,7 +180,8 @@ def _peaks():
 
 def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None):
     """CUDA-event time of each C-ABI entry point of the step on the same
-    inputs (current stream), L2 flushed between repetitions."""
+    inputs: each entry point is captured alone in a CUDA graph and replayed
+    between events on the launching stream, L2 flushed before every replay."""
     import torch
     from diffrp_gb300 import _ffi
     from diffrp_gb300 import nvdr as dr
@@ -236,13 +237,21 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None):
     }
     times = {}
     for name, fn in ops.items():
+        # capture the entry point alone in a CUDA graph so that the timing is
+        # the device time of its kernels, not host launch overhead
         fn()
+        torch.cuda.synchronize(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            fn()
+        graph.replay()
+        torch.cuda.synchronize(dev)
         ts = []
         for _ in range(reps):
             flush.fill_(1)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(s)
-            fn()
+            graph.replay()
             e1.record(s)
             e1.synchronize()
             ts.append(e0.elapsed_time(e1))

@@ -388,6 +388,20 @@ __device__ __forceinline__ unsigned long long tile_prim_key(const float4& z4, in
     return ((unsigned long long)depth_order(z) << 32) | (unsigned long long)__float_as_uint(z4.w);
 }
 
+// Pixel q of thread tid inside a tile: warps own 8x4 pixel blocks (blocks
+// are numbered across the tile, then down), lanes are row-major inside the
+// block.  A warp can then skip a primitive whose bbox misses its block with
+// one uniform test.
+template <int TILE_LOG2, int NTHREADS>
+__device__ __forceinline__ void tile_pixel(int tid, int q, int& dx, int& dy, int& bx, int& by) {
+    constexpr int T = 1 << TILE_LOG2;
+    const int blk = (tid >> 5) + q * (NTHREADS >> 5);
+    bx = (blk % (T / 8)) * 8;
+    by = (blk / (T / 8)) * 4;
+    dx = bx + (tid & 7);
+    dy = by + ((tid >> 3) & 3);
+}
+
 // Fine raster + shade, one CTA per (tile, view).
 //   TPT == 0: every thread owns T*T/NTHREADS pixels and tests them against
 //             each primitive of the tile (keys in registers, no atomics);
@@ -418,12 +432,13 @@ fine_raster_kernel(RasterArgs a) {
     unsigned long long best[PPT], prevk[PPT];
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
-        const int i = tid + q * NTHREADS;
-        const int px = tx0 + (i & (T - 1)), py = ty0 + (i >> TILE_LOG2);
+        int dx, dy, bx, by;
+        tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+        const int px = tx0 + dx, py = ty0 + dy;
         best[q] = ~0ull;
         prevk[q] = 0;
         if (prev_g) prevk[q] = (px < a.W && py < a.H) ? prev_g[py * a.W + px] : ~0ull;
-        if (TPT > 0) keys[i] = ~0ull;
+        if (TPT > 0) keys[(dy << TILE_LOG2) + dx] = ~0ull;
     }
     if (tid == 0) n_complex = 0;
     if (tid < T) col_ndc[tid] = pixel_ndc(tx0 + tid, a.W);
@@ -452,11 +467,13 @@ fine_raster_kernel(RasterArgs a) {
                 const TilePrim& tp = prims[j];
                 const int4 e2 = tp.e2;
                 if (!(e2.y & TP_ACTIVE)) continue;
-                const int4 e0 = tp.e0, e1 = tp.e1;
+                const int4 e0 = tp.e0, e1 = tp.e1, v2b = tp.v2b;
+                const int x0 = v2b.z & 0xffff, x1 = v2b.z >> 16, y0 = v2b.w & 0xffff, y1 = v2b.w >> 16;
 #pragma unroll
                 for (int q = 0; q < PPT; ++q) {
-                    const int i = tid + q * NTHREADS;
-                    const int dx = i & (T - 1), dy = i >> TILE_LOG2;
+                    int dx, dy, bx, by;
+                    tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+                    if (x1 < bx || x0 > bx + 7 || y1 < by || y0 > by + 3) continue;  // warp-uniform
                     const int sx = (tx0 + dx) * DRP_SUBPIX + DRP_HALF_SUBPIX;
                     const int sy = (ty0 + dy) * DRP_SUBPIX + DRP_HALF_SUBPIX;
                     if (!tile_prim_covers(tp, e0, e1, e2, dx, dy, sx, sy)) continue;
@@ -493,7 +510,11 @@ fine_raster_kernel(RasterArgs a) {
     }
     if (TPT == 0) {
 #pragma unroll
-        for (int q = 0; q < PPT; ++q) keys[tid + q * NTHREADS] = best[q];
+        for (int q = 0; q < PPT; ++q) {
+            int dx, dy, bx, by;
+            tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+            keys[(dy << TILE_LOG2) + dx] = best[q];
+        }
     }
     __syncthreads();
     if (n_complex > 0) {
@@ -501,7 +522,11 @@ fine_raster_kernel(RasterArgs a) {
         __shared__ unsigned long long prev_s[NPIX];
         if (prev_g) {
 #pragma unroll
-            for (int q = 0; q < PPT; ++q) prev_s[tid + q * NTHREADS] = prevk[q];
+            for (int q = 0; q < PPT; ++q) {
+                int dx, dy, bx, by;
+                tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+                prev_s[(dy << TILE_LOG2) + dx] = prevk[q];
+            }
         }
         __syncthreads();
         constexpr int CG = 8;
@@ -522,8 +547,10 @@ fine_raster_kernel(RasterArgs a) {
     const float4* P = reinterpret_cast<const float4*>(a.pos + (long long)b * a.pos_view_stride);
 #pragma unroll
     for (int q = 0; q < PPT; ++q) {
-        const int i = tid + q * NTHREADS;
-        const int px = tx0 + (i & (T - 1)), py = ty0 + (i >> TILE_LOG2);
+        int dx, dy, bx, by;
+        tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+        const int i = (dy << TILE_LOG2) + dx;
+        const int px = tx0 + dx, py = ty0 + dy;
         if (px >= a.W || py >= a.H) continue;
         const long long o = (long long)b * npix_view + py * a.W + px;
         const unsigned long long k = keys[i];

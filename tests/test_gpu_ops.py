@@ -47,7 +47,7 @@ CASES = [
 ]
 
 
-@pytest.mark.parametrize("tile_log2,tpt", [(4, 8), (3, 1), (5, 32)])
+@pytest.mark.parametrize("tile_log2,tpt", [(4, 0), (3, 0), (5, 0), (4, 8), (3, 1), (5, 32)])
 @pytest.mark.parametrize("name,make,res,ranges", CASES, ids=[c[0] for c in CASES])
 def test_rasterize_bit_exact(cuda_lib, name, make, res, ranges, tile_log2, tpt):
     pos, tri = make()
