@@ -92,5 +92,5 @@ def test_session_clip_injected_bit_exact_visibility(cuda_lib):
     rp._cache = {SurfaceDeferredRenderSession.clip_space.__qualname__: torch.from_numpy(ref["clip"]).cuda()}
     rast = rp.rasterize()[0].cpu().numpy()
     np.testing.assert_array_equal(rast, ref["rast"])
-    n = rp.false_color_camera_space_normal().cpu().numpy()
+    n = rp.false_color_camera_space_normal().detach().cpu().numpy()
     np.testing.assert_allclose(n, ref["normals"], atol=2e-6)
