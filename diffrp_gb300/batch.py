@@ -1,0 +1,233 @@
+"""Batching form: many meshes x views x resolutions in one set of launches.
+
+``BatchRenderer`` renders a fixed set of items -- (mesh, view, resolution)
+triples -- through rasterize -> interpolate -> antialias in one launch
+sequence per forward (persistent fine-raster CTAs pulling (item, tile) work
+from a queue, interpolation fused into the raster's shading) and one fused
+backward pass.  Each item's output equals what the per-item drop-in calls
+(``nvdr.rasterize``, ``nvdr.interpolate``, ``nvdr.antialias`` with the mesh's
+topology) produce; the item structure (triangle counts, resolutions,
+channels) is static so the whole step can be captured in a CUDA graph.
+
+Packed layouts (see ``drp_batch_item`` in include/diffrp_gb300.h):
+  positions   (sum over items of the mesh's V, 4) clip-space rows, item order;
+  attributes  (sum over meshes of V * C,) floats, mesh order;
+  images      (sum over items of H * W * C,) floats, item order.
+``recompute=True`` keeps no per-pixel buffer between forward and backward:
+the backward re-runs the rasteriser (and the fused interpolation) instead.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _ffi
+from . import nvdr
+
+__all__ = ["BatchRenderer"]
+
+
+class _Item(ctypes.Structure):
+    _fields_ = [("pos_offset", ctypes.c_longlong), ("attr_offset", ctypes.c_longlong),
+                ("tri_first", ctypes.c_int), ("tri_count", ctypes.c_int), ("num_vertices", ctypes.c_int),
+                ("height", ctypes.c_int), ("width", ctypes.c_int), ("channels", ctypes.c_int),
+                ("tiles_x", ctypes.c_int), ("tiles_y", ctypes.c_int),
+                ("prim_offset", ctypes.c_longlong), ("tile_offset", ctypes.c_longlong),
+                ("pixel_offset", ctypes.c_longlong), ("image_offset", ctypes.c_longlong)]
+
+
+assert ctypes.sizeof(_Item) == 80
+
+
+def _register():
+    lib = _ffi.load()
+    P, LL, I, ULL = ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int, ctypes.c_ulonglong
+    sigs = {
+        "drp_batch_plan": [P, I, I, P],
+        "drp_batch_block_maps": [P, I, P, P],
+        "drp_batch_workspace_size": [LL, LL, ULL, ctypes.POINTER(ctypes.c_size_t)],
+        "drp_batch_forward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, I, I, ULL, P, P, P, P],
+        "drp_batch_backward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, P, P, P, P, P, P],
+    }
+    for name, args in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    return lib
+
+
+class BatchRenderer:
+    """Render many (mesh, view, resolution) items per launch.
+
+    meshes: list of (tri (F, 3) int32 CUDA tensor, num_vertices, channels).
+    items:  list of (mesh index, (height, width)).
+    tile_log2 / threads_per_tri: fine-raster shape (see nvdr.RasterizeCudaContext).
+    """
+
+    def __init__(self, meshes, items, device=None, tile_log2=4, threads_per_tri=0, recompute=False):
+        _register()
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.tile_log2 = int(tile_log2)
+        self.threads_per_tri = int(threads_per_tri)
+        self.recompute = bool(recompute)
+        self.meshes = meshes
+        tri_parts, nbr_parts = [], []
+        tri_first, attr_off = [], []
+        f0 = a0 = 0
+        for tri, V, C in meshes:
+            tri = tri.to(self.device, torch.int32).contiguous()
+            tri_parts.append(tri)
+            nbr_parts.append(nvdr.antialias_construct_topology_hash(tri))
+            tri_first.append(f0)
+            attr_off.append(a0)
+            f0 += tri.shape[0]
+            a0 += int(V) * int(C)
+        self.tri = torch.cat(tri_parts).contiguous()
+        self.nbr = torch.cat(nbr_parts).contiguous()
+        self.attr_floats = a0
+        self.attr_offsets = attr_off
+        arr = (_Item * len(items))()
+        p0 = 0
+        self.pos_offsets = []
+        for i, (m, (H, W)) in enumerate(items):
+            tri, V, C = meshes[m]
+            arr[i].pos_offset = p0
+            arr[i].attr_offset = attr_off[m]
+            arr[i].tri_first = tri_first[m]
+            arr[i].tri_count = int(tri.shape[0])
+            arr[i].num_vertices = int(V)
+            arr[i].height = int(H)
+            arr[i].width = int(W)
+            arr[i].channels = int(C)
+            self.pos_offsets.append(p0)
+            p0 += int(V)
+        self.pos_rows = p0
+        totals = (ctypes.c_longlong * 6)()
+        _ffi.call("drp_batch_plan", ctypes.addressof(arr), len(items), self.tile_log2, ctypes.addressof(totals))
+        (self.total_prims, self.total_tiles, self.total_pixels, self.image_floats, self.prim_blocks,
+         self.pixel_blocks) = [int(x) for x in totals]
+        pmap = (ctypes.c_int * max(2, 2 * self.prim_blocks))()
+        xmap = (ctypes.c_int * max(2, 2 * self.pixel_blocks))()
+        _ffi.call("drp_batch_block_maps", ctypes.addressof(arr), len(items), ctypes.addressof(pmap),
+                  ctypes.addressof(xmap))
+        self.items = items
+        self.item_table = arr
+        self._items_dev = torch.from_numpy(np.frombuffer(bytes(arr), dtype=np.uint8).copy()).to(self.device)
+        self._pmap = torch.from_numpy(np.frombuffer(bytes(pmap), dtype=np.int32).copy()).to(self.device)
+        self._xmap = torch.from_numpy(np.frombuffer(bytes(xmap), dtype=np.int32).copy()).to(self.device)
+        self._capacity = 0
+        self._ws = None
+        self.last_list_entries = 0
+
+    # -- layout helpers ---------------------------------------------------------
+    def pack_positions(self, per_item):
+        """List of (V, 4) clip positions, one per item -> packed (rows, 4)."""
+        return torch.cat([p.reshape(-1, 4) for p in per_item]).contiguous()
+
+    def pack_attributes(self, per_mesh):
+        """List of (V, C) attributes, one per mesh -> packed floats."""
+        return torch.cat([a.reshape(-1) for a in per_mesh]).contiguous()
+
+    def images(self, packed):
+        """Packed image floats -> list of (H, W, C) views, item order."""
+        out = []
+        for it in self.item_table:
+            n = it.height * it.width * it.channels
+            out.append(packed[it.image_offset:it.image_offset + n].view(it.height, it.width, it.channels))
+        return out
+
+    def rast_views(self, rast):
+        out = []
+        for it in self.item_table:
+            n = it.height * it.width
+            out.append(rast[it.pixel_offset:it.pixel_offset + n].view(it.height, it.width, 4))
+        return out
+
+    # -- execution -------------------------------------------------------------------
+    def _workspace(self, cap):
+        nbytes = _ffi.size_out("drp_batch_workspace_size", self.total_prims, self.total_tiles, cap)
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        return self._ws
+
+    def _forward_raw(self, pos, attr, rast, color, out):
+        cap = self._capacity if self._capacity else 4 * self.total_prims + 4096
+        ws = self._workspace(cap)
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        args = (self._items_dev.data_ptr(), len(self.items), self._pmap.data_ptr(), self.prim_blocks,
+                self._xmap.data_ptr(), self.pixel_blocks, self.total_prims, self.total_tiles, pos.data_ptr(),
+                self.tri.data_ptr(), attr.data_ptr(), self.nbr.data_ptr(), self.tile_log2, self.threads_per_tri)
+        _ffi.call("drp_batch_forward", ws.data_ptr(), ws.numel(), *args, cap, rast.data_ptr(), color.data_ptr(),
+                  out.data_ptr(), stream)
+        if not self._capacity:
+            torch.cuda.current_stream(self.device).synchronize()
+            stats = ws[:16].view(torch.int64).cpu()
+            needed = int(stats[0])
+            if int(stats[1]) & 1:
+                raise RuntimeError("BatchRenderer: triangle vertex index out of range")
+            self.last_list_entries = needed
+            self._capacity = max(cap, int(needed * 1.25) + 4096)
+            if needed > cap:
+                ws = self._workspace(self._capacity)
+                _ffi.call("drp_batch_forward", ws.data_ptr(), ws.numel(), *args, self._capacity, rast.data_ptr(),
+                          color.data_ptr(), out.data_ptr(), stream)
+
+    def _backward_raw(self, pos, attr, rast, color, grad_out, grad_pos, grad_attr):
+        ws = self._workspace(self._capacity)
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        _ffi.call("drp_batch_backward", ws.data_ptr(), ws.numel(), self._items_dev.data_ptr(), len(self.items),
+                  self._pmap.data_ptr(), self.prim_blocks, self._xmap.data_ptr(), self.pixel_blocks,
+                  self.total_prims, self.total_tiles, pos.data_ptr(), self.tri.data_ptr(), attr.data_ptr(),
+                  self.nbr.data_ptr(), rast.data_ptr(), color.data_ptr(), grad_out.data_ptr(), grad_pos.data_ptr(),
+                  grad_attr.data_ptr(), stream)
+
+    def _buffers(self):
+        rast = torch.empty((self.total_pixels, 4), dtype=torch.float32, device=self.device)
+        color = torch.empty(self.image_floats, dtype=torch.float32, device=self.device)
+        return rast, color
+
+    def __call__(self, pos, attr):
+        """pos: packed (rows, 4) clip positions; attr: packed attribute floats.
+        Returns packed antialiased images (differentiable w.r.t. both)."""
+        if pos.shape != (self.pos_rows, 4) or pos.dtype != torch.float32 or not pos.is_cuda:
+            raise RuntimeError("pos must be a float32 CUDA tensor of shape (%d, 4)" % self.pos_rows)
+        if attr.numel() != self.attr_floats or attr.dtype != torch.float32 or not attr.is_cuda:
+            raise RuntimeError("attr must hold %d float32 values on the GPU" % self.attr_floats)
+        return _BatchFn.apply(pos.contiguous(), attr.contiguous().reshape(-1), self)
+
+    def forward_buffers(self, pos, attr):
+        """Forward without autograd; returns (rast, colour, output) packed."""
+        rast, color = self._buffers()
+        out = torch.empty_like(color)
+        self._forward_raw(pos.contiguous(), attr.contiguous().reshape(-1), rast, color, out)
+        return rast, color, out
+
+
+class _BatchFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, pos, attr, renderer):
+        rast, color = renderer._buffers()
+        out = torch.empty_like(color)
+        renderer._forward_raw(pos, attr, rast, color, out)
+        ctx.renderer = renderer
+        if renderer.recompute:
+            ctx.save_for_backward(pos, attr)
+        else:
+            ctx.save_for_backward(pos, attr, rast, color)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        r = ctx.renderer
+        if r.recompute:
+            pos, attr = ctx.saved_tensors
+            rast, color = r._buffers()
+            scratch = torch.empty_like(color)
+            r._forward_raw(pos, attr, rast, color, scratch)
+            del scratch
+        else:
+            pos, attr, rast, color = ctx.saved_tensors
+        grad_pos = torch.zeros_like(pos)
+        grad_attr = torch.zeros_like(attr)
+        r._backward_raw(pos, attr, rast, color, grad_out.contiguous(), grad_pos, grad_attr)
+        return grad_pos, grad_attr, None

@@ -1,0 +1,273 @@
+// aa_core.cuh -- analytic silhouette antialiasing building blocks shared by
+// the plain antialias kernels (antialias.cu) and the batched pipeline
+// (batch.cu): the per-triangle screen-space record, the evaluation of one
+// 4-neighbour pixel pair, and the per-pixel forward / backward.
+#pragma once
+#include "drp_common.cuh"
+
+namespace drp {
+
+__device__ __forceinline__ bool project_vertex(const float4& p, int W, int H, float2& s) {
+    if (!(p.w > 0.0f)) return false;
+    s.x = (p.x / p.w + 1.0f) * ((float)W * 0.5f);
+    s.y = (p.y / p.w + 1.0f) * ((float)H * 0.5f);
+    return true;
+}
+
+__device__ __forceinline__ float edge_fn(const float2& a, const float2& b, const float2& p) {
+    return (b.x - a.x) * (p.y - a.y) - (b.y - a.y) * (p.x - a.x);
+}
+
+// Per-triangle record: rec[0] = (s0.x, s0.y, s1.x, s1.y), rec[1] = (s2.x,
+// s2.y, sgn, mask bits); sgn = 0 marks an unusable triangle (a vertex with
+// w <= 0, zero / NaN screen area); mask bit k: edge k (vertices k+1, k+2) is
+// a silhouette (no neighbour across it, or the neighbour's opposite vertex
+// projects to the same side of the edge as this triangle's).
+__device__ __forceinline__ void aa_tri_record(const float4* P, const int* tri, const int* nbr, long long t,
+                                              long long F, long long V, int W, int H, float4* rec) {
+    const int v[3] = {tri[3 * t], tri[3 * t + 1], tri[3 * t + 2]};
+    float2 s[3];
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        if (v[i] < 0 || v[i] >= V || !project_vertex(P[v[i]], W, H, s[i])) {
+            ok = false;
+            s[i] = make_float2(0.f, 0.f);
+        }
+    }
+    float sgn = 0.0f;
+    unsigned mask = 0;
+    if (ok) {
+        const float area = (s[1].x - s[0].x) * (s[2].y - s[0].y) - (s[1].y - s[0].y) * (s[2].x - s[0].x);
+        if (!(area == 0.0f || area != area)) sgn = area > 0.0f ? 1.0f : -1.0f;
+    }
+    if (sgn != 0.0f) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            bool sil = true;
+            const int N = nbr ? nbr[3 * t + k] : -1;
+            if (N >= 0 && N < F) {
+                const int ea = v[(k + 1) % 3], eb = v[(k + 2) % 3];
+                int opp = -1;
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const int x = tri[3 * (long long)N + i];
+                    if (x != ea && x != eb && x >= 0 && x < V) opp = x;
+                }
+                float2 so;
+                if (opp >= 0 && project_vertex(P[opp], W, H, so)) {
+                    const float2 qa = s[(k + 1) % 3], qb = s[(k + 2) % 3];
+                    const float dT = edge_fn(qa, qb, s[k]);
+                    const float dN = edge_fn(qa, qb, so);
+                    if ((dT > 0.0f && dN < 0.0f) || (dT < 0.0f && dN > 0.0f)) sil = false;
+                }
+            }
+            if (sil) mask |= 1u << k;
+        }
+    }
+    rec[0] = make_float4(s[0].x, s[0].y, s[1].x, s[1].y);
+    rec[1] = make_float4(s[2].x, s[2].y, sgn, __uint_as_float(mask));
+}
+
+struct AAPair {
+    bool valid, clamped;
+    int target, src;  // pixel indices within the view
+    float w, sign, sgn, eF, eO;
+    int T, k;
+    float2 s[3];
+    float2 cF, cO;
+};
+
+// Pair (A, B) with A the left / lower pixel; rA, rB their rast rows; rec the
+// view's triangle records (F triangles); W the view width.
+__device__ __forceinline__ void aa_pair(const float4* rec, long long F, int W, int A, int Bp, const float4& rA,
+                                        const float4& rB, AAPair& R) {
+    R.valid = false;
+    const int tA = rast_tri(rA.w), tB = rast_tri(rB.w);
+    const int cA = (tA >= 0 && tA < F) ? tA : -1;
+    const int cB = (tB >= 0 && tB < F) ? tB : -1;
+    if (cA == cB) return;
+    int Fp;
+    if (cA < 0) Fp = Bp;
+    else if (cB < 0) Fp = A;
+    else if (rA.z < rB.z) Fp = A;
+    else if (rB.z < rA.z) Fp = Bp;
+    else Fp = cA < cB ? A : Bp;
+    const int Op = (Fp == A) ? Bp : A;
+    const int T = (Fp == A) ? cA : cB;
+    const float4 q0 = rec[2 * (long long)T], q1 = rec[2 * (long long)T + 1];
+    const float sgn = q1.z;
+    if (sgn == 0.0f) return;
+    const unsigned mask = __float_as_uint(q1.w);
+    R.s[0] = make_float2(q0.x, q0.y);
+    R.s[1] = make_float2(q0.z, q0.w);
+    R.s[2] = make_float2(q1.x, q1.y);
+    R.cF = make_float2((float)(Fp % W) + 0.5f, (float)(Fp / W) + 0.5f);
+    R.cO = make_float2((float)(Op % W) + 0.5f, (float)(Op / W) + 0.5f);
+    int best = -1;
+    float bt = 0.f, beF = 0.f, beO = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float2 ea = R.s[(k + 1) % 3], eb = R.s[(k + 2) % 3];
+        const float eO = sgn * edge_fn(ea, eb, R.cO);
+        if (!(eO < 0.0f)) continue;
+        const float eF = sgn * edge_fn(ea, eb, R.cF);
+        const float t = eF / (eF - eO);
+        if (best < 0 || t < bt) {
+            best = k;
+            bt = t;
+            beF = eF;
+            beO = eO;
+        }
+    }
+    if (best < 0 || !((mask >> best) & 1u)) return;
+    R.clamped = false;
+    if (bt < 0.0f) { bt = 0.0f; R.clamped = true; }
+    if (bt > 1.0f) { bt = 1.0f; R.clamped = true; }
+    R.T = T;
+    R.k = best;
+    R.eF = beF;
+    R.eO = beO;
+    R.sgn = sgn;
+    if (bt > 0.5f) {
+        R.target = Op;
+        R.src = Fp;
+        R.w = bt - 0.5f;
+        R.sign = 1.0f;
+    } else {
+        R.target = Fp;
+        R.src = Op;
+        R.w = 0.5f - bt;
+        R.sign = -1.0f;
+    }
+    R.valid = true;
+}
+
+// Pair slot q of a pixel, in the fixed order left, right, below, above:
+// (first pixel, second pixel) with the first being the left / lower one.
+__device__ __forceinline__ bool pair_slot(int q, int pix, int px, int py, int W, int H, int& A, int& B) {
+    switch (q) {
+    case 0: A = pix - 1; B = pix; return px > 0;
+    case 1: A = pix; B = pix + 1; return px < W - 1;
+    case 2: A = pix - W; B = pix; return py > 0;
+    default: A = pix; B = pix + W; return py < H - 1;
+    }
+}
+
+// Forward of one pixel: out = c + sum over pair slots targeting this pixel of
+// w (c[src] - c), in slot order (fmaf).  R, Cc: the view's rast and colour.
+__device__ __forceinline__ void aa_fwd_pixel(const float4* R, const float* Cc, const float4* rec, long long F, int W,
+                                             int H, int C, int pix, float* o) {
+    const int py = pix / W, px = pix - py * W;
+    const float* cs = Cc + (long long)pix * C;
+    const float4 rs = R[pix];
+    int src[4];
+    float wt[4];
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        src[q] = -1;
+        wt[q] = 0.f;
+        int A, B;
+        if (!pair_slot(q, pix, px, py, W, H, A, B)) continue;
+        const int other = A == pix ? B : A;
+        const float4 ro = R[other];
+        if (ro.w == rs.w) continue;
+        AAPair pr;
+        aa_pair(rec, F, W, A, B, A == pix ? rs : ro, A == pix ? ro : rs, pr);
+        if (pr.valid && pr.target == pix) {
+            src[q] = pr.src;
+            wt[q] = pr.w;
+            any = true;
+        }
+    }
+    if (!any) {
+        if ((C & 3) == 0 && (((uintptr_t)cs | (uintptr_t)o) & 15) == 0) {
+            for (int c = 0; c < C; c += 4)
+                *reinterpret_cast<float4*>(o + c) = *reinterpret_cast<const float4*>(cs + c);
+        } else {
+            for (int c = 0; c < C; ++c) o[c] = cs[c];
+        }
+        return;
+    }
+    for (int c = 0; c < C; ++c) {
+        float v = cs[c];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (src[q] >= 0) v = fmaf(wt[q], Cc[(long long)src[q] * C + c] - cs[c], v);
+        o[c] = v;
+    }
+}
+
+// Backward pair terms of one pixel.  For every pair slot: role (0 none, 1 this
+// pixel is the blend target, 2 the source), the target pixel and the weight;
+// the edge-vertex gradients of each pair are scattered here, once per pair
+// (by its first pixel), into GP (may be null).
+struct AATerms {
+    int role[4], tgt[4];
+    float wt[4];
+    bool any;
+};
+
+__device__ __forceinline__ void aa_bwd_terms(const float4* R, const float* Cc, const float* Gd, const float4* rec,
+                                             long long F, int W, int H, int C, const float4* P, const int* tri,
+                                             float4* GP, float boost, int pix, AATerms& at) {
+    const int py = pix / W, px = pix - py * W;
+    const float4 rs = R[pix];
+    at.any = false;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        at.role[q] = 0;
+        at.tgt[q] = 0;
+        at.wt[q] = 0.f;
+        int A, B;
+        if (!pair_slot(q, pix, px, py, W, H, A, B)) continue;
+        const int other = A == pix ? B : A;
+        const float4 ro = R[other];
+        if (ro.w == rs.w) continue;
+        AAPair p;
+        aa_pair(rec, F, W, A, B, A == pix ? rs : ro, A == pix ? ro : rs, p);
+        if (!p.valid) continue;
+        at.role[q] = p.target == pix ? 1 : 2;
+        at.tgt[q] = p.target;
+        at.wt[q] = p.w;
+        at.any = true;
+        if (!GP || A != pix || p.clamped) continue;
+        float dLdw = 0.f;
+        for (int c = 0; c < C; ++c)
+            dLdw = fmaf(Gd[(long long)p.target * C + c], Cc[(long long)p.src * C + c] - Cc[(long long)p.target * C + c],
+                        dLdw);
+        const float dLdt = dLdw * p.sign * boost;
+        const float den = p.eF - p.eO;
+        const float inv2 = 1.0f / (den * den);
+        const float dtF = -p.eO * inv2, dtO = p.eF * inv2;
+        const float2 ea = p.s[(p.k + 1) % 3], eb = p.s[(p.k + 2) % 3];
+        const float fF = dLdt * dtF * p.sgn, fO = dLdt * dtO * p.sgn;
+        const float gA0 = fmaf(fF, eb.y - p.cF.y, fO * (eb.y - p.cO.y));
+        const float gA1 = fmaf(fF, p.cF.x - eb.x, fO * (p.cO.x - eb.x));
+        const float gB0 = fmaf(fF, p.cF.y - ea.y, fO * (p.cO.y - ea.y));
+        const float gB1 = fmaf(fF, ea.x - p.cF.x, fO * (ea.x - p.cO.x));
+        const int vA = tri[3 * (long long)p.T + (p.k + 1) % 3], vB = tri[3 * (long long)p.T + (p.k + 2) % 3];
+        const float hx = 0.5f * (float)W, hy = 0.5f * (float)H;
+        const float4 pA = P[vA], pB = P[vB];
+        const float iwA = 1.0f / pA.w, iwB = 1.0f / pB.w;
+        atomic_add4(GP + vA, make_float4(gA0 * hx * iwA, gA1 * hy * iwA, 0.f,
+                                         -(gA0 * hx * pA.x + gA1 * hy * pA.y) * iwA * iwA));
+        atomic_add4(GP + vB, make_float4(gB0 * hx * iwB, gB1 * hy * iwB, 0.f,
+                                         -(gB0 * hx * pB.x + gB1 * hy * pB.y) * iwB * iwB));
+    }
+}
+
+// Colour gradient of channel c of a pixel from its terms (slot order).
+__device__ __forceinline__ float aa_bwd_channel(const AATerms& at, const float* Gd, int C, int pix, int c) {
+    const float gs = Gd[(long long)pix * C + c];
+    float v = gs;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        if (at.role[q] == 1) v = fmaf(-at.wt[q], gs, v);
+        else if (at.role[q] == 2) v = fmaf(at.wt[q], Gd[(long long)at.tgt[q] * C + c], v);
+    }
+    return v;
+}
+
+}  // namespace drp

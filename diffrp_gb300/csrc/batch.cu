@@ -1,0 +1,524 @@
+// batch.cu -- the batching form: many meshes x views x resolutions in one
+// set of launches, with raster + interpolation fused and the whole backward
+// (antialias, interpolation, rasterisation) fused into one pixel pass.
+//
+// An item is one (mesh, view, resolution) render: its clip vertices, its
+// mesh's triangles and attributes, and its own output image.  All items'
+// data live in packed buffers addressed through a device item table
+// (drp_batch_item); host-built block maps send every 256-wide block of
+// primitives or pixels to one item, so no thread searches for its item.
+//
+// Forward launches (independent of the number of items):
+//   setup/count -> scan -> setup/fill  (tile lists for every item's tiles)
+//   fine raster: persistent CTAs pull (item, tile) work from an atomic queue,
+//                resolve visibility, write rast and the interpolated colour
+//   antialias:   per-triangle records, then the per-pixel silhouette blend
+// Backward: per-triangle records, then one fused pixel pass computing the
+// antialias colour gradient, the attribute gradient (interpolation backward)
+// and the vertex gradient (rasterisation backward), scattered with
+// warp-segmented float4 atomics.
+#include "../../include/diffrp_gb300.h"
+#include "aa_core.cuh"
+#include "drp_internal.h"
+#include "raster_core.cuh"
+
+namespace drp {
+
+struct BatchArgs {
+    const drp_batch_item* items;
+    int num_items;
+    const int2* prim_blocks;  // (item, local block) per 256 triangle slots
+    long long n_prim_blocks;
+    const int2* pix_blocks;   // (item, local block) per 256 pixels
+    long long n_pix_blocks;
+    long long total_prims, total_tiles;
+    const float* pos;
+    const int* tri;
+    const float* attr;
+    const int* nbr;
+    int tile_log2, tpt;
+    unsigned long long list_capacity;
+    float* rast;
+    float* color;
+    float* out;
+    const float* grad_out;
+    float* grad_pos;
+    float* grad_attr;
+    // workspace
+    uint32_t* stats;
+    uint32_t* queue;
+    int4* prims;
+    uint32_t *tile_count, *tile_offset, *tile_cursor, *tile_list;
+    float4* aa_rec;
+};
+
+template <int TILE_LOG2, bool FILL>
+__global__ void __launch_bounds__(256) batch_setup_bin_kernel(BatchArgs a) {
+    const int2 blk = a.prim_blocks[blockIdx.x];
+    const drp_batch_item& it = a.items[blk.x];
+    const long long j = (long long)blk.y * 256 + threadIdx.x;
+    if (j >= it.tri_count) return;
+    const long long pidx = it.prim_offset + j;
+    int4* rec = a.prims + pidx * 3;
+    PrimBox bx;
+    bool live = false;
+    if (FILL) {
+        bx = unpack_box(rec[1], rec[2]);
+        live = bx.px0 <= bx.px1;
+    } else {
+        bx.px0 = 1;
+        bx.px1 = bx.py0 = bx.py1 = 0;
+        const long long t = (long long)it.tri_first + j;
+        const int i0 = a.tri[3 * t], i1 = a.tri[3 * t + 1], i2 = a.tri[3 * t + 2];
+        if (i0 < 0 || i1 < 0 || i2 < 0 || i0 >= it.num_vertices || i1 >= it.num_vertices || i2 >= it.num_vertices) {
+            atomicOr(a.stats + 2, DRP_DEVERR_BAD_INDEX);
+        } else {
+            const float4* P = reinterpret_cast<const float4*>(a.pos) + it.pos_offset;
+            live = build_prim(P[i0], P[i1], P[i2], j, it.width, it.height, rec, bx);
+        }
+        if (!live) {
+            rec[0] = make_int4(0, 0, 0, 0);
+            rec[1] = make_int4(0, 0, 0, 1);
+            rec[2] = make_int4(0, 0, 0, 0);
+        }
+    }
+    if (FILL)
+        bin_box<TILE_LOG2>(bx, live, it.tiles_x, a.tile_cursor + it.tile_offset, a.tile_list, a.list_capacity,
+                           (uint32_t)pidx);
+    else
+        bin_box<TILE_LOG2>(bx, live, it.tiles_x, a.tile_count + it.tile_offset, nullptr, 0, 0);
+}
+
+// rast + interpolated attributes of one pixel (interpolator.py:45 order).
+struct BatchEmit {
+    const float4* P;
+    const int* tri;  // the item's mesh triangles (local vertex indices)
+    const float* A;  // the item's mesh attributes
+    int W, H, C;
+    float4* rast;
+    float* color;
+    __device__ __forceinline__ void operator()(int px, int py, unsigned long long k, float X, float Y) const {
+        const long long o = (long long)py * W + px;
+        float* col = color + o * C;
+        if (k == ~0ull) {
+            rast[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int c = 0; c < C; ++c) col[c] = 0.f;
+            return;
+        }
+        const int t = (int)(uint32_t)(k & 0xffffffffu);
+        const int i0 = tri[3 * (long long)t], i1 = tri[3 * (long long)t + 1], i2 = tri[3 * (long long)t + 2];
+        Shade S;
+        shade_eval_xy(P[i0], P[i1], P[i2], X, Y, W, H, S);
+        rast[o] = make_float4(S.u, S.v, S.zw, enc_triid(t + 1));
+        const float* a0 = A + (long long)i0 * C;
+        const float* a1 = A + (long long)i1 * C;
+        const float* a2 = A + (long long)i2 * C;
+        for (int c = 0; c < C; ++c) col[c] = fmaf(a0[c] - a2[c], S.u, fmaf(a1[c] - a2[c], S.v, a2[c]));
+    }
+};
+
+__device__ __forceinline__ int find_item_by_tile(const drp_batch_item* items, int n, long long tile) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (items[mid].tile_offset <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int TILE_LOG2, int TPT>
+__global__ void __launch_bounds__((1 << (2 * TILE_LOG2)) < 256 ? (1 << (2 * TILE_LOG2)) : 256,
+                                  TILE_LOG2 == 3 ? 12 : 3)
+batch_fine_kernel(BatchArgs a) {
+    __shared__ long long job;
+    __shared__ int job_item;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            job = (long long)atomicAdd(a.queue, 1u);
+            job_item = job < a.total_tiles ? find_item_by_tile(a.items, a.num_items, job) : -1;
+        }
+        __syncthreads();
+        const long long t = job;
+        const int ii = job_item;
+        __syncthreads();
+        if (t >= a.total_tiles) break;
+        const drp_batch_item& it = a.items[ii];
+        const int tile = (int)(t - it.tile_offset);
+        FineTile ft;
+        ft.recs = a.prims;
+        const uint32_t off = a.tile_offset[t];
+        ft.cnt = a.tile_count[t];
+        ft.list = a.tile_list + off;
+        ft.overflow = (unsigned long long)off + ft.cnt > a.list_capacity;
+        ft.scan_base = it.prim_offset;
+        ft.scan_count = it.tri_count;
+        ft.tx0 = (tile % it.tiles_x) << TILE_LOG2;
+        ft.ty0 = (tile / it.tiles_x) << TILE_LOG2;
+        ft.W = it.width;
+        ft.H = it.height;
+        ft.P = reinterpret_cast<const float4*>(a.pos) + it.pos_offset;
+        ft.tri = a.tri + 3 * (long long)it.tri_first;
+        ft.prev = nullptr;
+        ft.stats = a.stats;
+        BatchEmit e;
+        e.P = ft.P;
+        e.tri = ft.tri;
+        e.A = a.attr + it.attr_offset;
+        e.W = it.width;
+        e.H = it.height;
+        e.C = it.channels;
+        e.rast = reinterpret_cast<float4*>(a.rast) + it.pixel_offset;
+        e.color = a.color + it.image_offset;
+        fine_tile<TILE_LOG2, TPT>(ft, e);
+    }
+}
+
+__global__ void __launch_bounds__(256) batch_aa_setup_kernel(BatchArgs a) {
+    const int2 blk = a.prim_blocks[blockIdx.x];
+    const drp_batch_item& it = a.items[blk.x];
+    const long long j = (long long)blk.y * 256 + threadIdx.x;
+    if (j >= it.tri_count) return;
+    const float4* P = reinterpret_cast<const float4*>(a.pos) + it.pos_offset;
+    aa_tri_record(P, a.tri + 3 * (long long)it.tri_first, a.nbr ? a.nbr + 3 * (long long)it.tri_first : nullptr, j,
+                  it.tri_count, it.num_vertices, it.width, it.height, a.aa_rec + (it.prim_offset + j) * 2);
+}
+
+__global__ void __launch_bounds__(256) batch_aa_fwd_kernel(BatchArgs a) {
+    const int2 blk = a.pix_blocks[blockIdx.x];
+    const drp_batch_item& it = a.items[blk.x];
+    const int pix = blk.y * 256 + threadIdx.x;
+    if (pix >= it.width * it.height) return;
+    const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
+    aa_fwd_pixel(R, a.color + it.image_offset, a.aa_rec + it.prim_offset * 2, it.tri_count, it.width, it.height,
+                 it.channels, pix, a.out + it.image_offset + (long long)pix * it.channels);
+}
+
+// Fused backward of one pixel: antialias colour gradient -> interpolation
+// backward (attribute gradients, d/du, d/dv) -> rasterisation backward
+// (vertex gradients).  Warps never straddle items (256-pixel blocks).
+__global__ void __launch_bounds__(256) batch_bwd_kernel(BatchArgs a) {
+    const int2 blk = a.pix_blocks[blockIdx.x];
+    const drp_batch_item& it = a.items[blk.x];
+    const int pix = blk.y * 256 + threadIdx.x;
+    const int W = it.width, H = it.height, C = it.channels;
+    const bool in = pix < W * H;
+    const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
+    const float* Cc = a.color + it.image_offset;
+    const float* Gd = a.grad_out + it.image_offset;
+    const float4* P = reinterpret_cast<const float4*>(a.pos) + it.pos_offset;
+    float4* GP = reinterpret_cast<float4*>(a.grad_pos) + it.pos_offset;
+    const int* tri = a.tri + 3 * (long long)it.tri_first;
+    const float* A = a.attr + it.attr_offset;
+    float* GA = a.grad_attr + it.attr_offset;
+    const float4* rec = a.aa_rec + it.prim_offset * 2;
+
+    AATerms at;
+    at.any = false;
+    int t = -1, i0 = 0, i1 = 0, i2 = 0;
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (in) {
+        aa_bwd_terms(R, Cc, Gd, rec, it.tri_count, W, H, C, P, tri, GP, 1.0f, pix, at);
+        r = R[pix];
+        t = checked_tri(r.w, tri, it.tri_count, it.num_vertices, i0, i1, i2);
+    }
+    const Seg seg = seg_setup(t >= 0 ? (long long)t : (long long)(-1 - lane_id()));
+    const float u = r.x, v = r.y, w = 1.0f - u - v;
+    float gu = 0.f, gv = 0.f;
+    for (int c0 = 0; c0 < C; c0 += 4) {
+        float val[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) val[k] = 0.f;
+        if (t >= 0) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int c = c0 + k;
+                if (c >= C) break;
+                const float g = at.any ? aa_bwd_channel(at, Gd, C, pix, c) : Gd[(long long)pix * C + c];
+                const float x0 = A[(long long)i0 * C + c], x1 = A[(long long)i1 * C + c], x2 = A[(long long)i2 * C + c];
+                val[k] = g * u;
+                val[4 + k] = g * v;
+                val[8 + k] = g * w;
+                gu = fmaf(g, x0 - x2, gu);
+                gv = fmaf(g, x1 - x2, gv);
+            }
+        }
+        seg_reduce<12>(seg, val);
+        if (t >= 0 && seg.head) {
+            for (int k = 0; k < 4 && c0 + k < C; ++k) {
+                atomicAdd(GA + (long long)i0 * C + c0 + k, val[k]);
+                atomicAdd(GA + (long long)i1 * C + c0 + k, val[4 + k]);
+                atomicAdd(GA + (long long)i2 * C + c0 + k, val[8 + k]);
+            }
+        }
+    }
+    float pv[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) pv[k] = 0.f;
+    if (t >= 0) {
+        const int py = pix / W, px = pix - py * W;
+        const float4 p0 = P[i0], p1 = P[i1], p2 = P[i2];
+        Shade S;
+        shade_eval(p0, p1, p2, px, py, W, H, S);
+        float4 g3[3];
+        shade_grad(p0, p1, p2, S, gu, gv, 0.f, nullptr, g3);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            pv[4 * k] = g3[k].x;
+            pv[4 * k + 1] = g3[k].y;
+            pv[4 * k + 2] = g3[k].z;
+            pv[4 * k + 3] = g3[k].w;
+        }
+    }
+    seg_reduce<12>(seg, pv);
+    if (t >= 0 && seg.head) {
+        atomic_add4(GP + i0, make_float4(pv[0], pv[1], pv[2], pv[3]));
+        atomic_add4(GP + i1, make_float4(pv[4], pv[5], pv[6], pv[7]));
+        atomic_add4(GP + i2, make_float4(pv[8], pv[9], pv[10], pv[11]));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+struct BatchLayout {
+    size_t stats, queue, prims, count, offset, cursor, list, aa, total;
+};
+
+BatchLayout batch_layout(long long total_prims, long long total_tiles, unsigned long long cap) {
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    BatchLayout L;
+    L.stats = 0;
+    L.queue = 64;
+    L.prims = 256;
+    L.count = up(L.prims + (size_t)total_prims * 48);
+    L.offset = up(L.count + (size_t)total_tiles * 4);
+    L.cursor = up(L.offset + (size_t)total_tiles * 4);
+    L.list = up(L.cursor + (size_t)total_tiles * 4);
+    L.aa = up(L.list + (size_t)cap * 4);
+    L.total = up(L.aa + (size_t)total_prims * 32);
+    return L;
+}
+
+static void carve(BatchArgs& a, void* ws, const BatchLayout& L) {
+    char* w = static_cast<char*>(ws);
+    a.stats = reinterpret_cast<uint32_t*>(w + L.stats);
+    a.queue = reinterpret_cast<uint32_t*>(w + L.queue);
+    a.prims = reinterpret_cast<int4*>(w + L.prims);
+    a.tile_count = reinterpret_cast<uint32_t*>(w + L.count);
+    a.tile_offset = reinterpret_cast<uint32_t*>(w + L.offset);
+    a.tile_cursor = reinterpret_cast<uint32_t*>(w + L.cursor);
+    a.tile_list = reinterpret_cast<uint32_t*>(w + L.list);
+    a.aa_rec = reinterpret_cast<float4*>(w + L.aa);
+}
+
+template <int TL, int TPT>
+static void launch_batch_fine(const BatchArgs& a, cudaStream_t s) {
+    constexpr int NT = (1 << (2 * TL)) < 256 ? (1 << (2 * TL)) : 256;
+    static int grid = 0;
+    if (grid == 0) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_fine_kernel<TL, TPT>, NT, 0);
+        grid = sms * (per > 0 ? per : 1);
+    }
+    const long long g = a.total_tiles < grid ? a.total_tiles : grid;
+    if (g > 0) batch_fine_kernel<TL, TPT><<<(unsigned)g, NT, 0, s>>>(a);
+}
+
+template <int TL>
+static void launch_batch_raster(const BatchArgs& a, cudaStream_t s) {
+    if (a.n_prim_blocks > 0) {
+        batch_setup_bin_kernel<TL, false><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+        scan_tiles_kernel<<<1, 1024, 0, s>>>(a.tile_count, a.tile_offset, a.tile_cursor, a.total_tiles,
+                                             reinterpret_cast<unsigned long long*>(a.stats));
+        batch_setup_bin_kernel<TL, true><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+    } else {
+        cudaMemsetAsync(a.tile_offset, 0, sizeof(uint32_t) * a.total_tiles, s);
+    }
+    switch (a.tpt) {
+    case 0: launch_batch_fine<TL, 0>(a, s); break;
+    case 1: launch_batch_fine<TL, 1>(a, s); break;
+    case 2: launch_batch_fine<TL, 2>(a, s); break;
+    case 4: launch_batch_fine<TL, 4>(a, s); break;
+    case 8: launch_batch_fine<TL, 8>(a, s); break;
+    case 16: launch_batch_fine<TL, 16>(a, s); break;
+    default: launch_batch_fine<TL, 32>(a, s); break;
+    }
+}
+
+int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream_t s) {
+    carve(a, ws, L);
+    cudaMemsetAsync(a.stats, 0, 256, s);  // stats and work queue
+    cudaMemsetAsync(a.tile_count, 0, sizeof(uint32_t) * a.total_tiles, s);
+    switch (a.tile_log2) {
+    case 3: launch_batch_raster<3>(a, s); break;
+    case 5: launch_batch_raster<5>(a, s); break;
+    default: launch_batch_raster<4>(a, s); break;
+    }
+    if (a.n_prim_blocks > 0) batch_aa_setup_kernel<<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+    if (a.n_pix_blocks > 0) batch_aa_fwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+    return 0;
+}
+
+int launch_batch_backward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream_t s) {
+    carve(a, ws, L);
+    if (a.n_prim_blocks > 0) batch_aa_setup_kernel<<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+    if (a.n_pix_blocks > 0) batch_bwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+    return 0;
+}
+
+}  // namespace drp
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+#define DRP_API extern "C" __attribute__((visibility("default")))
+
+namespace {
+int bfail(const char* msg) {
+    drp_set_last_error(msg);
+    return DRP_STATUS_INVALID_ARGUMENT;
+}
+}  // namespace
+
+DRP_API int drp_batch_plan(drp_batch_item* items, int num_items, int tile_log2, long long* totals) {
+    if (!items || num_items <= 0 || !totals) return bfail("drp_batch_plan: bad arguments");
+    if (tile_log2 < 3 || tile_log2 > 5) return bfail("drp_batch_plan: tile_log2 must be 3, 4 or 5");
+    long long prims = 0, tiles = 0, pixels = 0, floats = 0, pblocks = 0, xblocks = 0;
+    for (int i = 0; i < num_items; ++i) {
+        drp_batch_item& it = items[i];
+        if (it.height <= 0 || it.width <= 0 || it.height > DRP_MAX_RESOLUTION || it.width > DRP_MAX_RESOLUTION ||
+            it.channels <= 0 || it.tri_count < 0 || it.tri_first < 0 || it.num_vertices < 0 || it.pos_offset < 0 ||
+            it.attr_offset < 0)
+            return bfail("drp_batch_plan: item with invalid size, resolution or offset");
+        it.tiles_x = (it.width + (1 << tile_log2) - 1) >> tile_log2;
+        it.tiles_y = (it.height + (1 << tile_log2) - 1) >> tile_log2;
+        it.prim_offset = prims;
+        it.tile_offset = tiles;
+        it.pixel_offset = pixels;
+        it.image_offset = floats;
+        prims += it.tri_count;
+        tiles += (long long)it.tiles_x * it.tiles_y;
+        pixels += (long long)it.width * it.height;
+        floats += (long long)it.width * it.height * it.channels;
+        pblocks += (it.tri_count + 255) / 256;
+        xblocks += ((long long)it.width * it.height + 255) / 256;
+    }
+    totals[0] = prims;
+    totals[1] = tiles;
+    totals[2] = pixels;
+    totals[3] = floats;
+    totals[4] = pblocks;
+    totals[5] = xblocks;
+    return DRP_STATUS_OK;
+}
+
+DRP_API int drp_batch_block_maps(const drp_batch_item* items, int num_items, int* prim_block_map,
+                                 int* pixel_block_map) {
+    if (!items || num_items <= 0 || !prim_block_map || !pixel_block_map) return bfail("drp_batch_block_maps: null");
+    long long p = 0, x = 0;
+    for (int i = 0; i < num_items; ++i) {
+        const long long nb = (items[i].tri_count + 255) / 256;
+        for (long long k = 0; k < nb; ++k, ++p) {
+            prim_block_map[2 * p] = i;
+            prim_block_map[2 * p + 1] = (int)k;
+        }
+        const long long xb = ((long long)items[i].width * items[i].height + 255) / 256;
+        for (long long k = 0; k < xb; ++k, ++x) {
+            pixel_block_map[2 * x] = i;
+            pixel_block_map[2 * x + 1] = (int)k;
+        }
+    }
+    return DRP_STATUS_OK;
+}
+
+DRP_API int drp_batch_workspace_size(long long total_prims, long long total_tiles, unsigned long long list_capacity,
+                                     size_t* bytes) {
+    if (!bytes || total_prims < 0 || total_tiles < 0 || list_capacity > 0x7fffffffull)
+        return bfail("drp_batch_workspace_size: bad arguments");
+    *bytes = drp::batch_layout(total_prims, total_tiles, list_capacity).total;
+    return DRP_STATUS_OK;
+}
+
+static int batch_common(void* ws, size_t ws_bytes, const drp_batch_item* items, int num_items,
+                        const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
+                        long long pixel_blocks, long long total_prims, long long total_tiles,
+                        unsigned long long list_capacity, const float* pos, const int* tri, const float* attr,
+                        drp::BatchArgs& a, drp::BatchLayout& L) {
+    if (!ws || (reinterpret_cast<uintptr_t>(ws) & 255)) return bfail("batch: workspace must be 256-byte aligned");
+    if (!items || num_items <= 0 || !pos || !tri || !attr) return bfail("batch: null table or buffer");
+    if ((prim_blocks > 0 && !prim_block_map) || (pixel_blocks > 0 && !pixel_block_map) || prim_blocks < 0 ||
+        pixel_blocks < 0 || prim_blocks > 0x7fffffffll || pixel_blocks > 0x7fffffffll)
+        return bfail("batch: bad block maps");
+    if ((reinterpret_cast<uintptr_t>(pos) & 15)) return bfail("batch: pos must be 16-byte aligned");
+    if (list_capacity > 0x7fffffffull) return bfail("batch: list_capacity above 2^31 - 1");
+    L = drp::batch_layout(total_prims, total_tiles, list_capacity);
+    if (ws_bytes < L.total) {
+        drp_set_last_error("batch: workspace too small");
+        return DRP_STATUS_WORKSPACE_TOO_SMALL;
+    }
+    a = drp::BatchArgs{};
+    a.items = items;
+    a.num_items = num_items;
+    a.prim_blocks = reinterpret_cast<const int2*>(prim_block_map);
+    a.n_prim_blocks = prim_blocks;
+    a.pix_blocks = reinterpret_cast<const int2*>(pixel_block_map);
+    a.n_pix_blocks = pixel_blocks;
+    a.total_prims = total_prims;
+    a.total_tiles = total_tiles;
+    a.pos = pos;
+    a.tri = tri;
+    a.attr = attr;
+    a.list_capacity = list_capacity;
+    return DRP_STATUS_OK;
+}
+
+DRP_API int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
+                              const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
+                              long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
+                              const int* tri, const float* attr, const int* nbr, int tile_log2, int threads_per_tri,
+                              unsigned long long list_capacity, float* rast, float* color, float* out,
+                              void* stream) {
+    drp::BatchArgs a;
+    drp::BatchLayout L;
+    int st = batch_common(workspace, workspace_bytes, items, num_items, prim_block_map, prim_blocks, pixel_block_map,
+                          pixel_blocks, total_prims, total_tiles, list_capacity, pos, tri, attr, a, L);
+    if (st) return st;
+    if (tile_log2 < 3 || tile_log2 > 5) return bfail("batch: tile_log2 must be 3, 4 or 5");
+    if (threads_per_tri < 0 || threads_per_tri > 32 || (threads_per_tri & (threads_per_tri - 1)))
+        return bfail("batch: threads_per_tri must be 0 or a power of two <= 32");
+    if (!rast || !color || !out || (reinterpret_cast<uintptr_t>(rast) & 15)) return bfail("batch: bad outputs");
+    a.nbr = nbr;
+    a.tile_log2 = tile_log2;
+    a.tpt = threads_per_tri;
+    a.rast = rast;
+    a.color = color;
+    a.out = out;
+    drp::launch_batch_forward(a, workspace, L, static_cast<cudaStream_t>(stream));
+    return drp_check_launch("drp_batch_forward");
+}
+
+DRP_API int drp_batch_backward(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
+                               const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
+                               long long pixel_blocks, long long total_prims, long long total_tiles,
+                               const float* pos, const int* tri, const float* attr, const int* nbr,
+                               const float* rast, const float* color, const float* grad_out, float* grad_pos,
+                               float* grad_attr, void* stream) {
+    drp::BatchArgs a;
+    drp::BatchLayout L;
+    int st = batch_common(workspace, workspace_bytes, items, num_items, prim_block_map, prim_blocks, pixel_block_map,
+                          pixel_blocks, total_prims, total_tiles, 0, pos, tri, attr, a, L);
+    if (st) return st;
+    if (!rast || !color || !grad_out || !grad_pos || !grad_attr || (reinterpret_cast<uintptr_t>(grad_pos) & 15))
+        return bfail("batch: bad gradient buffers");
+    a.nbr = nbr;
+    a.rast = const_cast<float*>(rast);
+    a.color = const_cast<float*>(color);
+    a.grad_out = grad_out;
+    a.grad_pos = grad_pos;
+    a.grad_attr = grad_attr;
+    drp::launch_batch_backward(a, workspace, L, static_cast<cudaStream_t>(stream));
+    return drp_check_launch("drp_batch_backward");
+}

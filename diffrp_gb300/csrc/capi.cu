@@ -57,6 +57,10 @@ RasterLayout raster_layout(int B, long long maxT, int H, int W, int tile_log2, u
 
 }  // namespace
 
+void drp_set_last_error(const char* msg) { snprintf(g_last_error, sizeof(g_last_error), "%s", msg); }
+
+int drp_check_launch(const char* what) { return check_launch(what); }
+
 DRP_API int drp_abi_version(void) { return DRP_ABI_VERSION; }
 
 DRP_API const char* drp_status_string(int status) {

@@ -116,3 +116,8 @@ int launch_aa_fwd(const AAArgs& a, cudaStream_t s);
 int launch_aa_bwd(const AAArgs& a, cudaStream_t s);
 
 }  // namespace drp
+
+// Thread-local error message of the C ABI (capi.cu).
+void drp_set_last_error(const char* msg);
+// DRP_STATUS_OK, or DRP_STATUS_CUDA_ERROR with the message set, after a launch.
+int drp_check_launch(const char* what);

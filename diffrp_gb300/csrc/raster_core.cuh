@@ -1,0 +1,507 @@
+// raster_core.cuh -- rasterisation building blocks shared by the plain
+// (per-call) pipeline in raster.cu and the batched pipeline in batch.cu:
+// triangle setup into 48-byte primitive records, tile binning, per-tile
+// primitive preparation (int32 edge steps with trivial accept / reject) and
+// the fine raster of one tile by one CTA.
+#pragma once
+#include "drp_common.cuh"
+
+namespace drp {
+
+// Primitive record (3 x int4 = 48 bytes).
+//   r0 = {X0, Y0, X1, Y1}                 fixed-point vertices
+//   r1 = {X2, Y2, tri, px0 | px1 << 16}
+//   r2 = {Z0, A, B (float bits), py0 | py1 << 16 | COMPLEX << 31}
+// A culled record has px0 = 1, px1 = 0 (empty range).  COMPLEX records were
+// clipped; the fine raster re-derives their polygon from the clip vertices.
+#define PRIM_COMPLEX 0x80000000u
+
+struct PrimBox {
+    int px0, px1, py0, py1;
+    bool complex_;
+};
+
+__device__ __forceinline__ PrimBox unpack_box(const int4& r1, const int4& r2) {
+    PrimBox b;
+    uint32_t xs = (uint32_t)r1.w, ys = (uint32_t)r2.w;
+    b.px0 = xs & 0xffff;
+    b.px1 = xs >> 16;
+    b.py0 = ys & 0x7fff;
+    b.py1 = (ys >> 16) & 0x7fff;
+    b.complex_ = (ys & PRIM_COMPLEX) != 0;
+    return b;
+}
+
+// Warp-aggregated increment of counter[idx] by 1; returns the old value for
+// this lane (its slot).  All lanes in `active` must call it.
+__device__ __forceinline__ uint32_t warp_agg_inc(uint32_t* counter, uint32_t idx, unsigned active) {
+    unsigned peers = __match_any_sync(active, idx);
+    int leader = __ffs(peers) - 1;
+    int lane = lane_id();
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter + idx, (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+}
+
+// Triangle setup into a primitive record.  P: the view's clip vertices,
+// t: the triangle's index in `tri` (written into the record and used as the
+// visibility id), vertex indices already validated.  Returns false when the
+// triangle covers no pixel centre (culled record).
+__device__ __forceinline__ bool build_prim(const float4& p0, const float4& p1, const float4& p2, long long t, int W,
+                                           int H, int4* rec, PrimBox& box) {
+    int4 r0 = make_int4(0, 0, 0, 0), r1 = make_int4(0, 0, (int)t, 0), r2 = make_int4(0, 0, 0, 0);
+    const int kind = needs_clip_or_cull(p0, p1, p2);
+    int64_t mnx = 0, mxx = -1, mny = 0, mxy = -1;
+    bool ok = false;
+    if (kind == 1) {
+        const int32_t X0 = snap_coord(p0.x, p0.w, W), Y0 = snap_coord(p0.y, p0.w, H);
+        const int32_t X1 = snap_coord(p1.x, p1.w, W), Y1 = snap_coord(p1.y, p1.w, H);
+        const int32_t X2 = snap_coord(p2.x, p2.w, W), Y2 = snap_coord(p2.y, p2.w, H);
+        const float Z0 = p0.z / p0.w, Z1 = p1.z / p1.w, Z2 = p2.z / p2.w;
+        const int64_t area2 = (int64_t)(X1 - X0) * (int64_t)(Y2 - Y0) - (int64_t)(Y1 - Y0) * (int64_t)(X2 - X0);
+        if (area2 != 0) {
+            Plane pl = depth_plane(X0, Y0, Z0, X1, Y1, Z1, X2, Y2, Z2, area2);
+            r0 = make_int4(X0, Y0, X1, Y1);
+            r1 = make_int4(X2, Y2, (int)t, 0);
+            r2 = make_int4(__float_as_int(pl.Z0), __float_as_int(pl.A), __float_as_int(pl.B), 0);
+            mnx = min(min(X0, X1), X2);
+            mxx = max(max(X0, X1), X2);
+            mny = min(min(Y0, Y1), Y2);
+            mxy = max(max(Y0, Y1), Y2);
+            ok = true;
+        }
+    } else if (kind == 2) {
+        Poly poly;
+        setup_clipped(p0, p1, p2, W, H, poly);
+        if (poly.n >= 3) {
+            mnx = mxx = poly.X[0];
+            mny = mxy = poly.Y[0];
+            for (int i = 1; i < poly.n; ++i) {
+                mnx = min(mnx, (int64_t)poly.X[i]);
+                mxx = max(mxx, (int64_t)poly.X[i]);
+                mny = min(mny, (int64_t)poly.Y[i]);
+                mxy = max(mxy, (int64_t)poly.Y[i]);
+            }
+            ok = true;
+        }
+    }
+    bool live = false;
+    box.px0 = 1;
+    box.px1 = 0;
+    box.py0 = box.py1 = 0;
+    box.complex_ = kind == 2;
+    if (ok) {
+        int64_t x0 = ceil_shift(mnx - DRP_HALF_SUBPIX), x1 = floor_shift(mxx - DRP_HALF_SUBPIX);
+        int64_t y0 = ceil_shift(mny - DRP_HALF_SUBPIX), y1 = floor_shift(mxy - DRP_HALF_SUBPIX);
+        x0 = max(x0, (int64_t)0);
+        x1 = min(x1, (int64_t)(W - 1));
+        y0 = max(y0, (int64_t)0);
+        y1 = min(y1, (int64_t)(H - 1));
+        if (x0 <= x1 && y0 <= y1) {
+            box.px0 = (int)x0;
+            box.px1 = (int)x1;
+            box.py0 = (int)y0;
+            box.py1 = (int)y1;
+            live = true;
+            r2.w = (int)((uint32_t)box.py0 | ((uint32_t)box.py1 << 16) | (kind == 2 ? PRIM_COMPLEX : 0u));
+        }
+    }
+    if (!live) {
+        r2.w = 0;
+        box.px0 = 1;
+        box.px1 = 0;
+    }
+    r1.w = (int)((uint32_t)box.px0 | ((uint32_t)box.px1 << 16));
+    rec[0] = r0;
+    rec[1] = r1;
+    rec[2] = r2;
+    return live;
+}
+
+// For every tile the box overlaps: count (list == null) or append `pidx` to
+// the tile's list through the cursors (warp-aggregated slots; entries past
+// `capacity` are dropped and the tile falls back to a full scan).  Every
+// lane of the warp must call this (n = 0 for lanes with nothing to bin).
+template <int TILE_LOG2>
+__device__ __forceinline__ void bin_box(const PrimBox& bx, bool live, int tiles_x, uint32_t* counters,
+                                        uint32_t* list, unsigned long long capacity, uint32_t pidx) {
+    const int tx0 = bx.px0 >> TILE_LOG2, tx1 = bx.px1 >> TILE_LOG2, ty0 = bx.py0 >> TILE_LOG2,
+              ty1 = bx.py1 >> TILE_LOG2;
+    const int n = live ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0;
+    const int w = tx1 - tx0 + 1;
+    for (int i = 0;; ++i) {
+        const unsigned active = __ballot_sync(__activemask(), i < n);
+        if (i >= n) break;
+        const uint32_t tile = (uint32_t)((ty0 + i / w) * tiles_x + tx0 + i % w);
+        const uint32_t slot = warp_agg_inc(counters, tile, active);
+        if (list && slot < capacity) list[slot] = pidx;
+    }
+}
+
+// Rasterise one fan sub-triangle into the tile's key buffer (group-strided,
+// shared-memory atomicMin).  Used for clipped polygons, whose fan
+// sub-triangles each carry their own depth plane.
+template <int TILE_LOG2>
+__device__ __forceinline__ void raster_subtri_tile(int64_t X0, int64_t Y0, int64_t X1, int64_t Y1, int64_t X2,
+                                                   int64_t Y2, const Plane& pl, uint32_t tri, int tx0, int ty0,
+                                                   int W, int H, int rank, int group, unsigned long long* keys,
+                                                   const unsigned long long* prev) {
+    constexpr int T = 1 << TILE_LOG2;
+    const int64_t area2 = (X1 - X0) * (Y2 - Y0) - (Y1 - Y0) * (X2 - X0);
+    if (area2 == 0) return;
+    int64_t ax = X0, ay = Y0, bx = X1, by = Y1, cx = X2, cy = Y2;
+    if (area2 < 0) {
+        bx = X2; by = Y2; cx = X1; cy = Y1;
+    }
+    int64_t mnx = min(min(X0, X1), X2), mxx = max(max(X0, X1), X2);
+    int64_t mny = min(min(Y0, Y1), Y2), mxy = max(max(Y0, Y1), Y2);
+    const int x0 = (int)max(ceil_shift(mnx - DRP_HALF_SUBPIX), (int64_t)tx0);
+    const int x1 = (int)min(floor_shift(mxx - DRP_HALF_SUBPIX), (int64_t)min(tx0 + T - 1, W - 1));
+    const int y0 = (int)max(ceil_shift(mny - DRP_HALF_SUBPIX), (int64_t)ty0);
+    const int y1 = (int)min(floor_shift(mxy - DRP_HALF_SUBPIX), (int64_t)min(ty0 + T - 1, H - 1));
+    if (x0 > x1 || y0 > y1) return;
+    const int w = x1 - x0 + 1;
+    const int n = w * (y1 - y0 + 1);
+    for (int i = rank; i < n; i += group) {
+        const int px = x0 + i % w, py = y0 + i / w;
+        const int64_t sx = (int64_t)px * DRP_SUBPIX + DRP_HALF_SUBPIX;
+        const int64_t sy = (int64_t)py * DRP_SUBPIX + DRP_HALF_SUBPIX;
+        if (!edge_inside(bx, by, cx, cy, sx, sy)) continue;
+        if (!edge_inside(cx, cy, ax, ay, sx, sy)) continue;
+        if (!edge_inside(ax, ay, bx, by, sx, sy)) continue;
+        const float z = (pl.Z0 + pl.A * (float)(sx - X0)) + pl.B * (float)(sy - Y0);
+        if (!(z >= -1.0f && z <= 1.0f)) continue;
+        const unsigned long long k = ((unsigned long long)depth_order(z) << 32) | (unsigned long long)tri;
+        const int li = ((py - ty0) << TILE_LOG2) + (px - tx0);
+        if (prev && !(k > prev[li])) continue;
+        if (k < keys[li]) atomicMin(keys + li, k);
+    }
+}
+
+template <int TILE_LOG2>
+__device__ __noinline__ void raster_complex_tile(const float4* P, const int* tri_idx, int W, int H, uint32_t tri,
+                                                 int tx0, int ty0, int rank, int group, unsigned long long* keys,
+                                                 const unsigned long long* prev) {
+    const int i0 = tri_idx[3 * (long long)tri], i1 = tri_idx[3 * (long long)tri + 1],
+              i2 = tri_idx[3 * (long long)tri + 2];
+    Poly poly;
+    setup_clipped(P[i0], P[i1], P[i2], W, H, poly);
+    for (int i = 1; i + 1 < poly.n; ++i) {
+        const int64_t X0 = poly.X[0], Y0 = poly.Y[0], X1 = poly.X[i], Y1 = poly.Y[i];
+        const int64_t X2 = poly.X[i + 1], Y2 = poly.Y[i + 1];
+        const int64_t area2 = (X1 - X0) * (Y2 - Y0) - (Y1 - Y0) * (X2 - X0);
+        if (area2 == 0) continue;
+        const Plane pl = depth_plane(X0, Y0, poly.Z[0], X1, Y1, poly.Z[i], X2, Y2, poly.Z[i + 1], area2);
+        raster_subtri_tile<TILE_LOG2>(X0, Y0, X1, Y1, X2, Y2, pl, tri, tx0, ty0, W, H, rank, group, keys, prev);
+    }
+}
+
+// A primitive prepared for one tile.  Edge k passes at tile pixel (dx, dy)
+// when C[k] + A[k] dx + B[k] dy >= 0 (top-left bias folded into C).  Edges
+// that accept every pixel of the tile are reduced to A = B = C = 0.  BIG
+// primitives have an edge too long for 32-bit steps and are tested in 64-bit
+// from the (oriented) vertices.
+#define TP_ACTIVE 1
+#define TP_BIG 2
+#define TP_COMPLEX 4
+
+struct __align__(16) TilePrim {
+    int4 e0;    // A0, B0, C0, A1
+    int4 e1;    // B1, C1, A2, B2
+    int4 e2;    // C2, flags, X0, Y0
+    float4 z;   // Z0, Az, Bz, tri (bits)
+    int4 v01;   // oriented vertices for the BIG path: x0, y0, x1, y1
+    int4 v2b;   // x2, y2, local bbox x0 | x1 << 16, y0 | y1 << 16
+};
+
+template <int T>
+__device__ __forceinline__ void prepare_tile_prim(const int4* rec, int tx0, int ty0, int W, int H, TilePrim& tp) {
+    tp.e2.y = 0;
+    const int4 r1 = rec[1], r2 = rec[2];
+    const PrimBox bx = unpack_box(r1, r2);
+    if (bx.px0 > bx.px1 || bx.px1 < tx0 || bx.px0 >= tx0 + T || bx.py1 < ty0 || bx.py0 >= ty0 + T) return;
+    tp.z.w = __int_as_float(r1.z);
+    const int lx0 = max(bx.px0, tx0) - tx0, lx1 = min(min(bx.px1, tx0 + T - 1), W - 1) - tx0;
+    const int ly0 = max(bx.py0, ty0) - ty0, ly1 = min(min(bx.py1, ty0 + T - 1), H - 1) - ty0;
+    tp.v2b.z = lx0 | (lx1 << 16);
+    tp.v2b.w = ly0 | (ly1 << 16);
+    if (bx.complex_) {
+        tp.e2.y = TP_COMPLEX;
+        return;
+    }
+    const int4 r0 = rec[0];
+    const int64_t X0 = r0.x, Y0 = r0.y, X1 = r0.z, Y1 = r0.w, X2 = r1.x, Y2 = r1.y;
+    const int64_t area2 = (X1 - X0) * (Y2 - Y0) - (Y1 - Y0) * (X2 - X0);
+    int64_t vx[3] = {X0, X1, X2}, vy[3] = {Y0, Y1, Y2};
+    if (area2 < 0) {
+        vx[1] = X2; vy[1] = Y2; vx[2] = X1; vy[2] = Y1;
+    }
+    const int64_t ox = (int64_t)tx0 * DRP_SUBPIX + DRP_HALF_SUBPIX;
+    const int64_t oy = (int64_t)ty0 * DRP_SUBPIX + DRP_HALF_SUBPIX;
+    bool big = false;
+    int A[3], B[3], C[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int p = (k + 1) % 3, q = (k + 2) % 3;  // edges b->c, c->a, a->b
+        const int64_t dx = vx[q] - vx[p], dy = vy[q] - vy[p];
+        const bool tl = (dy < 0) || (dy == 0 && dx < 0);
+        const int64_t Cb = dx * (oy - vy[p]) - dy * (ox - vx[p]) - (tl ? 0 : 1);
+        const int64_t SX = -dy * DRP_SUBPIX, SY = dx * DRP_SUBPIX;
+        const int64_t lo = (min(SX, (int64_t)0) + min(SY, (int64_t)0)) * (T - 1);
+        const int64_t hi = (max(SX, (int64_t)0) + max(SY, (int64_t)0)) * (T - 1);
+        A[k] = B[k] = C[k] = 0;
+        if (Cb + hi < 0) return;  // no pixel centre of the tile is inside this edge
+        if (Cb + lo >= 0) continue;  // every pixel centre of the tile is inside
+        if (hi - lo < ((int64_t)1 << 30)) {
+            A[k] = (int)SX;
+            B[k] = (int)SY;
+            C[k] = (int)Cb;
+        } else {
+            big = true;
+        }
+    }
+    tp.e0 = make_int4(A[0], B[0], C[0], A[1]);
+    tp.e1 = make_int4(B[1], C[1], A[2], B[2]);
+    tp.e2 = make_int4(C[2], TP_ACTIVE | (big ? TP_BIG : 0), (int)X0, (int)Y0);
+    tp.z.x = __int_as_float(r2.x);
+    tp.z.y = __int_as_float(r2.y);
+    tp.z.z = __int_as_float(r2.z);
+    tp.v01 = make_int4((int)vx[0], (int)vy[0], (int)vx[1], (int)vy[1]);
+    tp.v2b.x = (int)vx[2];
+    tp.v2b.y = (int)vy[2];
+}
+
+__device__ __forceinline__ bool tile_prim_covers(const TilePrim& tp, const int4& e0, const int4& e1, const int4& e2,
+                                                 int dx, int dy, int sx, int sy) {
+    if (!(e2.y & TP_BIG)) {
+        return (e0.z + e0.x * dx + e0.y * dy >= 0) && (e1.y + e0.w * dx + e1.x * dy >= 0) &&
+               (e2.x + e1.z * dx + e1.w * dy >= 0);
+    }
+    const int4 v01 = tp.v01, v2b = tp.v2b;
+    return edge_inside(v01.z, v01.w, v2b.x, v2b.y, sx, sy) && edge_inside(v2b.x, v2b.y, v01.x, v01.y, sx, sy) &&
+           edge_inside(v01.x, v01.y, v01.z, v01.w, sx, sy);
+}
+
+__device__ __forceinline__ unsigned long long tile_prim_key(const float4& z4, int X0, int Y0, int sx, int sy,
+                                                            bool& ok) {
+    const float z = (z4.x + z4.y * (float)(sx - X0)) + z4.z * (float)(sy - Y0);
+    ok = (z >= -1.0f && z <= 1.0f);
+    return ((unsigned long long)depth_order(z) << 32) | (unsigned long long)__float_as_uint(z4.w);
+}
+
+// Pixel q of thread tid inside a tile: warps own 8x4 pixel blocks (blocks
+// are numbered across the tile, then down), lanes are row-major inside the
+// block.  A warp can then skip a primitive whose bbox misses its block with
+// one uniform test.
+template <int TILE_LOG2, int NTHREADS>
+__device__ __forceinline__ void tile_pixel(int tid, int q, int& dx, int& dy, int& bx, int& by) {
+    constexpr int T = 1 << TILE_LOG2;
+    const int blk = (tid >> 5) + q * (NTHREADS >> 5);
+    bx = (blk % (T / 8)) * 8;
+    by = (blk / (T / 8)) * 4;
+    dx = bx + (tid & 7);
+    dy = by + ((tid >> 3) & 3);
+}
+
+// One tile's work for the fine raster.
+struct FineTile {
+    const int4* recs;           // primitive records
+    const uint32_t* list;       // this tile's list entries (first entry)
+    uint32_t cnt;               // list length
+    bool overflow;              // list incomplete: scan [scan_base, scan_base + scan_count)
+    long long scan_base, scan_count;
+    int tx0, ty0, W, H;
+    const float4* P;            // the view's clip vertices (complex primitives)
+    const int* tri;
+    const unsigned long long* prev;  // the view's previous-layer keys or null
+    uint32_t* stats;            // device error bits or null
+};
+
+// Fine raster of one tile by one CTA, then emit(px, py, local index, key,
+// ndc x, ndc y) for every pixel of the tile inside the viewport.
+//   TPT == 0: every thread owns T*T/NTHREADS pixels (8x4 blocks per warp)
+//             and tests them against each primitive of the tile (keys in
+//             registers, no atomics);
+//   TPT  > 0: groups of TPT threads walk one primitive's bbox within the tile
+//             and resolve keys with shared-memory atomicMin.
+template <int TILE_LOG2, int TPT, class Emit>
+__device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
+    constexpr int T = 1 << TILE_LOG2;
+    constexpr int NPIX = T * T;
+    constexpr int NTHREADS = NPIX < 256 ? NPIX : 256;
+    constexpr int PPT = NPIX / NTHREADS;
+    constexpr int CHUNK = NTHREADS < 128 ? NTHREADS : 128;
+    constexpr int GROUPS = TPT > 0 ? NTHREADS / TPT : 1;
+    __shared__ unsigned long long keys[NPIX];
+    __shared__ TilePrim prims[CHUNK];
+    __shared__ int n_complex;
+    __shared__ float col_ndc[T], row_ndc[T];
+
+    const int tx0 = ft.tx0, ty0 = ft.ty0, W = ft.W, H = ft.H;
+    const int tid = threadIdx.x;
+    const unsigned long long* prev_g = ft.prev;
+
+    unsigned long long best[PPT], prevk[PPT];
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+        int dx, dy, bx, by;
+        tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+        const int px = tx0 + dx, py = ty0 + dy;
+        best[q] = ~0ull;
+        prevk[q] = 0;
+        if (prev_g) prevk[q] = (px < W && py < H) ? prev_g[py * W + px] : ~0ull;
+        if (TPT > 0) keys[(dy << TILE_LOG2) + dx] = ~0ull;
+    }
+    if (tid == 0) n_complex = 0;
+    if (tid < T) col_ndc[tid] = pixel_ndc(tx0 + tid, W);
+    else if (tid < 2 * T) row_ndc[tid - T] = pixel_ndc(ty0 + tid - T, H);
+
+    const bool overflow = ft.overflow;
+    const long long pbase = ft.scan_base;
+    const long long total = overflow ? ft.scan_count : (long long)ft.cnt;
+    const int4* recs = ft.recs;
+    if (overflow && tid == 0 && ft.stats) atomicOr(ft.stats + 2, DRP_DEVERR_LIST_OVERFLOW);
+    __syncthreads();
+
+    for (long long base = 0; base < total; base += CHUNK) {
+        const int n = (int)min((long long)CHUNK, total - base);
+        if (tid < n && tid < CHUNK) {
+            const long long pidx = overflow ? pbase + base + tid : (long long)ft.list[base + tid];
+            prepare_tile_prim<T>(recs + pidx * 3, tx0, ty0, W, H, prims[tid]);
+            if (prims[tid].e2.y & TP_COMPLEX) atomicAdd(&n_complex, 1);
+        }
+        __syncthreads();
+        if (TPT == 0) {
+            for (int j = 0; j < n; ++j) {
+                const TilePrim& tp = prims[j];
+                const int4 e2 = tp.e2;
+                if (!(e2.y & TP_ACTIVE)) continue;
+                const int4 e0 = tp.e0, e1 = tp.e1, v2b = tp.v2b;
+                const int x0 = v2b.z & 0xffff, x1 = v2b.z >> 16, y0 = v2b.w & 0xffff, y1 = v2b.w >> 16;
+#pragma unroll
+                for (int q = 0; q < PPT; ++q) {
+                    int dx, dy, bx, by;
+                    tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+                    if (x1 < bx || x0 > bx + 7 || y1 < by || y0 > by + 3) continue;  // warp-uniform
+                    const int sx = (tx0 + dx) * DRP_SUBPIX + DRP_HALF_SUBPIX;
+                    const int sy = (ty0 + dy) * DRP_SUBPIX + DRP_HALF_SUBPIX;
+                    if (!tile_prim_covers(tp, e0, e1, e2, dx, dy, sx, sy)) continue;
+                    bool ok;
+                    const unsigned long long k = tile_prim_key(tp.z, e2.z, e2.w, sx, sy, ok);
+                    if (ok && k < best[q] && (!prev_g || k > prevk[q])) best[q] = k;
+                }
+            }
+        } else {
+            constexpr int G = TPT > 0 ? TPT : 1;
+            const int rank = tid % G;
+            for (int j = tid / G; j < n; j += GROUPS) {
+                const TilePrim& tp = prims[j];
+                const int4 e2 = tp.e2;
+                if (!(e2.y & TP_ACTIVE)) continue;
+                const int4 e0 = tp.e0, e1 = tp.e1, v2b = tp.v2b;
+                const int x0 = v2b.z & 0xffff, x1 = v2b.z >> 16, y0 = v2b.w & 0xffff, y1 = v2b.w >> 16;
+                for (int dy = y0; dy <= y1; ++dy) {
+                    for (int dx = x0 + rank; dx <= x1; dx += G) {
+                        const int sx = (tx0 + dx) * DRP_SUBPIX + DRP_HALF_SUBPIX;
+                        const int sy = (ty0 + dy) * DRP_SUBPIX + DRP_HALF_SUBPIX;
+                        if (!tile_prim_covers(tp, e0, e1, e2, dx, dy, sx, sy)) continue;
+                        bool ok;
+                        const unsigned long long k = tile_prim_key(tp.z, e2.z, e2.w, sx, sy, ok);
+                        if (!ok) continue;
+                        const int li = (dy << TILE_LOG2) + dx;
+                        if (prev_g && !(k > prev_g[(ty0 + dy) * W + tx0 + dx])) continue;
+                        if (k < keys[li]) atomicMin(keys + li, k);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (TPT == 0) {
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            int dx, dy, bx, by;
+            tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+            keys[(dy << TILE_LOG2) + dx] = best[q];
+        }
+    }
+    __syncthreads();
+    if (n_complex > 0) {
+        // Clipped polygons (rare): second pass over the list, group-parallel.
+        __shared__ unsigned long long prev_s[NPIX];
+        if (prev_g) {
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) {
+                int dx, dy, bx, by;
+                tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+                prev_s[(dy << TILE_LOG2) + dx] = prevk[q];
+            }
+        }
+        __syncthreads();
+        constexpr int CG = 8;
+        for (long long j = tid / CG; j < total; j += NTHREADS / CG) {
+            const long long pidx = overflow ? pbase + j : (long long)ft.list[j];
+            const int4 r1 = recs[pidx * 3 + 1], r2 = recs[pidx * 3 + 2];
+            const PrimBox bx = unpack_box(r1, r2);
+            if (!bx.complex_ || bx.px0 > bx.px1 || bx.px1 < tx0 || bx.px0 >= tx0 + T || bx.py1 < ty0 ||
+                bx.py0 >= ty0 + T)
+                continue;
+            raster_complex_tile<TILE_LOG2>(ft.P, ft.tri, W, H, (uint32_t)r1.z, tx0, ty0, tid % CG, CG, keys,
+                                           prev_g ? prev_s : nullptr);
+        }
+        __syncthreads();
+    }
+
+    // Emit.
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+        int dx, dy, bx, by;
+        tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+        const int px = tx0 + dx, py = ty0 + dy;
+        if (px >= W || py >= H) continue;
+        emit(px, py, keys[(dy << TILE_LOG2) + dx], col_ndc[dx], row_ndc[dy]);
+    }
+}
+
+// Exclusive scan of tile counts -> offsets (and cursors); total entries -> stats.
+static __global__ void __launch_bounds__(1024) scan_tiles_kernel(const uint32_t* counts, uint32_t* offsets,
+                                                          uint32_t* cursors, long long n,
+                                                          unsigned long long* total) {
+    __shared__ unsigned long long warp_sums[32];
+    const int tid = threadIdx.x;
+    const long long per = (n + blockDim.x - 1) / blockDim.x;
+    const long long lo = min(n, per * tid), hi = min(n, lo + per);
+    unsigned long long s = 0;
+    for (long long i = lo; i < hi; ++i) s += counts[i];
+    // block exclusive scan of s
+    unsigned long long x = s;
+    const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long v = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            unsigned long long y = __shfl_up_sync(0xffffffffu, v, off);
+            if (lane >= off) v += y;
+        }
+        warp_sums[lane] = v;
+    }
+    __syncthreads();
+    unsigned long long base = (warp ? warp_sums[warp - 1] : 0) + x - s;
+    for (long long i = lo; i < hi; ++i) {
+        uint32_t o = (uint32_t)min(base, (unsigned long long)0xffffffffu);
+        offsets[i] = o;
+        cursors[i] = o;
+        base += counts[i];
+    }
+    if (tid == blockDim.x - 1) *total = base;
+}
+
+}  // namespace drp

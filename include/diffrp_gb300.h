@@ -178,6 +178,64 @@ int drp_antialias_bwd(void* workspace, size_t workspace_bytes, const float* colo
                       const float* grad_out, float pos_gradient_boost, float* grad_color, float* grad_pos,
                       void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Batching form: many (mesh, view, resolution) items per launch             */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * One item = one render of a mesh from one view at its own resolution.  The
+ * caller fills the first group of fields; drp_batch_plan fills the rest.
+ * Packed buffers: pos (rows of float4 clip vertices, the item's vertex 0 at
+ * row pos_offset), tri (int32 triples, the item's mesh triangles at
+ * [tri_first, tri_first + tri_count), vertex indices local to the item),
+ * attr (floats, the mesh's V x channels attributes from attr_offset), and the
+ * per-item outputs at pixel_offset (rast rows) / image_offset (floats).
+ * No counterpart in the reference: diffrp renders one session (one view) per
+ * call; this is the batched form of the same rasterize -> interpolate ->
+ * antialias chain (rast, interpolated colour and antialiased output per item
+ * are identical to the per-item calls).
+ */
+typedef struct drp_batch_item {
+    long long pos_offset;   /* in float4 rows */
+    long long attr_offset;  /* in floats */
+    int tri_first, tri_count, num_vertices, height, width, channels;
+    /* filled by drp_batch_plan: */
+    int tiles_x, tiles_y;
+    long long prim_offset, tile_offset, pixel_offset, image_offset;
+} drp_batch_item;
+
+/* Fill the derived fields of items[] (in place, host memory) for the given
+ * tile size; totals[6] = {primitives, tiles, pixels, image floats,
+ * primitive blocks, pixel blocks}. */
+int drp_batch_plan(drp_batch_item* items, int num_items, int tile_log2, long long* totals);
+
+/* Host-side block maps (int pairs: item, block within the item) of 256
+ * triangle slots / 256 pixels; sizes from totals[4] / totals[5]. */
+int drp_batch_block_maps(const drp_batch_item* items, int num_items, int* prim_block_map, int* pixel_block_map);
+
+int drp_batch_workspace_size(long long total_prims, long long total_tiles, unsigned long long list_capacity,
+                             size_t* bytes);
+
+/*
+ * Forward of every item: rasterise (persistent CTAs over an (item, tile)
+ * work queue), interpolate attr into colour (fused), antialias into out.
+ * items / block maps are device copies.  nbr: per-mesh topology from
+ * drp_antialias_topology at the mesh's triangle offset, or NULL.
+ */
+int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
+                      const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
+                      long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
+                      const int* tri, const float* attr, const int* nbr, int tile_log2, int threads_per_tri,
+                      unsigned long long list_capacity, float* rast, float* color, float* out, void* stream);
+
+/* Fused backward: grad_out (image floats) -> grad_pos (accumulated, pos
+ * layout) and grad_attr (accumulated, attr layout). */
+int drp_batch_backward(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
+                       const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
+                       long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
+                       const int* tri, const float* attr, const int* nbr, const float* rast, const float* color,
+                       const float* grad_out, float* grad_pos, float* grad_attr, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
