@@ -26,6 +26,7 @@ not exist on this machine) with all host threads on the same workload.
 the data path).
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -122,10 +123,234 @@ class GraphedStep:
         return self.loss
 
 
+class BatchStep:
+    """The same step through the batching form (one item): fused raster +
+    interpolation, antialias, fused backward (diffrp_gb300.batch)."""
+
+    def __init__(self, dev, f, mvp, target, V, C, tile=(4, 0)):
+        import torch
+        from diffrp_gb300.batch import BatchRenderer
+        self.torch = torch
+        self.tri = torch.from_numpy(f).to(dev)
+        self.mvp = torch.from_numpy(mvp).to(dev)
+        self.target = torch.from_numpy(target).to(dev).reshape(-1)
+        self.renderer = BatchRenderer([(self.tri, V, C)], [(0, (H, W))], device=dev, tile_log2=tile[0],
+                                      threads_per_tri=tile[1])
+
+    def __call__(self, verts, attr):
+        torch = self.torch
+        verts.grad = None
+        attr.grad = None
+        clip = torch.nn.functional.pad(verts, (0, 1), value=1.0) @ self.mvp.T
+        out = self.renderer(clip, attr.reshape(-1))
+        loss = (out - self.target).abs().mean()
+        loss.backward()
+        return loss
+
+
 # Kernel launches of ours per step: rasterize (setup, scan, fill, fine) = 4,
 # interpolate fwd/bwd = 2, antialias fwd/bwd = 2 + 2 triangle setups,
 # rasterize bwd = 1.
 LAUNCHES_PER_STEP = 11
+# Batching form per step: setup/count, scan, setup/fill, fine, AA setup, AA
+# forward; backward: AA setup, fused backward.
+BATCH_LAUNCHES_PER_STEP = 8
+
+
+# ---------------------------------------------------------------------------
+# Batched workloads (the batching form against plain per-item launches)
+# ---------------------------------------------------------------------------
+def _graph(fn, dev, warm=3):
+    """Capture fn (a fwd+bwd step) in a CUDA graph after warm-up on a side stream."""
+    import torch
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(side):
+        for _ in range(warm):
+            fn()
+    torch.cuda.current_stream(dev).wait_stream(side)
+    torch.cuda.synchronize(dev)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        fn()
+    torch.cuda.synchronize(dev)
+    return g
+
+
+class MultiViewWorkload:
+    """items = (mesh, view, resolution) renders with per-mesh attributes;
+    clip positions come from per-item MVPs applied to the mesh vertices (so
+    gradients reach the vertices).  Provides the batched step and the plain
+    per-item step over the drop-in nvdr calls, both L1 to a seeded target."""
+
+    def __init__(self, dev, meshes, items, seed=0, recompute=False, tile=None):
+        import torch
+        from diffrp_gb300.batch import BatchRenderer
+        self.torch = torch
+        self.dev = dev
+        rng = np.random.default_rng(seed)
+        self.verts = [torch.from_numpy(v).to(dev).requires_grad_(True) for v, _, _ in meshes]
+        self.attrs = [torch.from_numpy(rng.uniform(0, 1, (len(v), c)).astype(np.float32)).to(dev).requires_grad_(True)
+                      for v, _, c in meshes]
+        self.tris = [torch.from_numpy(f).to(dev) for _, f, _ in meshes]
+        self.items = [(m, (H, W)) for m, (H, W), _ in items]
+        self.mvps = [torch.from_numpy(mvp.astype(np.float32)).to(dev) for _, _, mvp in items]
+        self.pixels = sum(H * W for _, (H, W), _ in items)
+        self.channels = [meshes[m][2] for m, _, _ in items]
+        tl, tpt = (tile if tile is not None else (4, 0))
+        self.renderer = BatchRenderer([(t, len(v), c) for t, (v, _, c) in zip(self.tris, meshes)], self.items,
+                                      device=dev, tile_log2=tl, threads_per_tri=tpt, recompute=recompute)
+        self.target = torch.from_numpy(rng.uniform(0, 1, self.renderer.image_floats).astype(np.float32)).to(dev)
+        self.targets = self.renderer.images(self.target)
+        from diffrp_gb300 import nvdr
+        self.nvdr = nvdr
+        self.ctx = nvdr.RasterizeCudaContext(dev)
+        self.topos = [nvdr.antialias_construct_topology_hash(t) for t in self.tris]
+
+    def _clip(self, m, k):
+        torch = self.torch
+        return torch.nn.functional.pad(self.verts[m], (0, 1), value=1.0) @ self.mvps[k].T
+
+    def _zero(self):
+        for t in self.verts + self.attrs:
+            t.grad = None
+
+    def batched_step(self):
+        self._zero()
+        pos = self.torch.cat([self._clip(m, k) for k, (m, _) in enumerate(self.items)])
+        attr = self.torch.cat([a.reshape(-1) for a in self.attrs])
+        out = self.renderer(pos, attr)
+        loss = (out - self.target).abs().sum() / out.numel()
+        loss.backward()
+        return loss
+
+    def plain_step(self):
+        self._zero()
+        dr = self.nvdr
+        loss = 0
+        n = self.renderer.image_floats
+        for k, (m, (H, W)) in enumerate(self.items):
+            clip = self._clip(m, k)
+            rast, _ = dr.rasterize(self.ctx, clip, self.tris[m], (H, W), grad_db=False)
+            col, _ = dr.interpolate(self.attrs[m], rast, self.tris[m])
+            aa = dr.antialias(col, rast, clip, self.tris[m], topology_hash=self.topos[m])
+            loss = loss + (aa[0] - self.targets[k]).abs().sum() / n
+        loss.backward()
+        return loss
+
+
+def views64_workload(dev):
+    """64 views of the icosphere-3 mesh (642 verts, 1280 tris, radius 0.8),
+    eyes uniform on a radius-3.2 sphere (seed 0), fov 30, 512x512, 8 channels."""
+    from diffrp_gb300 import synthetic as S
+    v, f = S.icosphere(3, 0.8)
+    P = S.perspective(30.0, 512, 512, 0.1, 100.0).astype(np.float64)
+    items = [(0, (512, 512), P @ S.view_matrix(S.lookat_pose(e)).astype(np.float64))
+             for e in S.sphere_eyes(64, 3.2, seed=0)]
+    return [(v, f, 8)], items
+
+
+def uneven48_workload(dev, seed=0):
+    """48 meshes (icospheres or displaced grids, triangle counts log-uniform in
+    [1e3, 5e5]), random rotation, scale U(0.5, 1.2), 1-4 views each from
+    {256, 512, 1024}^2, 4-16 channels."""
+    from diffrp_gb300 import synthetic as S
+    rng = np.random.default_rng(seed)
+    meshes, items = [], []
+    for m in range(48):
+        F = float(np.exp(rng.uniform(np.log(1e3), np.log(5e5))))
+        if rng.uniform() < 0.5:
+            sub = int(np.clip(round(np.log(F / 20.0) / np.log(4.0)), 3, 7))
+            v, f = S.icosphere(sub, 1.0)
+        else:
+            n = int(round(np.sqrt(F / 2.0))) + 1
+            v, f = S.random_displaced_grid(n, seed=seed * 1000 + m, sigma=0.03)
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        v = (v.astype(np.float64) @ q.T) * rng.uniform(0.5, 1.2)
+        c = int(rng.integers(4, 17))
+        meshes.append((v.astype(np.float32), f, c))
+        for _ in range(int(rng.integers(1, 5))):
+            res = int(rng.choice([256, 512, 1024]))
+            eye = S.sphere_eyes(1, 3.2, seed=int(rng.integers(1 << 30)))[0]
+            mvp = S.perspective(30.0, res, res, 0.1, 100.0).astype(np.float64) @ \
+                S.view_matrix(S.lookat_pose(eye)).astype(np.float64)
+            items.append((m, (res, res), mvp))
+    return meshes, items
+
+
+def large16_workload(dev, seed=0):
+    """1024x1024-vertex heightfield (2,093,058 tris) on [-1, 1]^2 with 6-octave
+    value noise of amplitude 0.3, 16 oblique views at 2048x2048, 12 channels."""
+    from diffrp_gb300 import synthetic as S
+    v, f = S.heightfield(1024, 0.3, 6, seed)
+    items = []
+    for k in range(16):
+        az = 2 * np.pi * k / 16
+        el = np.radians(35.0 + 10.0 * np.sin(3 * az))
+        eye = 2.6 * np.array([np.cos(az) * np.cos(el), np.sin(az) * np.cos(el), np.sin(el)])
+        mvp = S.perspective(40.0, 2048, 2048, 0.1, 20.0).astype(np.float64) @ \
+            S.view_matrix(S.lookat_pose(eye, up=(0.0, 0.0, 1.0))).astype(np.float64)
+        items.append((0, (2048, 2048), mvp))
+    return [(v, f, 12)], items
+
+
+def run_batched(dev, name, steps, warmup, plain=True, recompute=False, tune=True):
+    """Mpix/s of the batched form (graph-captured) and of the plain per-item
+    drop-in calls (eager, and graph-captured when it fits) on one workload."""
+    import torch
+    from diffrp_gb300 import autotune
+    meshes, items = {"views64": views64_workload, "uneven48": uneven48_workload,
+                     "large16": large16_workload}[name](dev)
+    tile = None
+    if tune:
+        # tune the tile shape on the largest item's geometry
+        m, (H, W), mvp = max(items, key=lambda it: len(meshes[it[0]][1]) * it[1][0] * it[1][1])
+        v, f, _ = meshes[m]
+        clip = torch.from_numpy(np.concatenate([v, np.ones((len(v), 1), np.float32)], 1) @
+                                mvp.astype(np.float32).T).to(dev).contiguous()
+        tri = torch.from_numpy(f).to(dev)
+        ch = autotune.tune_rasterizer(autotune.nvdr.RasterizeCudaContext(dev), clip, tri, (H, W), reps=3,
+                                      use_cache=False)
+        tile = (ch["tile_log2"], ch["threads_per_tri"])
+    torch.cuda.reset_peak_memory_stats(dev)
+    wl = MultiViewWorkload(dev, meshes, items, recompute=recompute, tile=tile)
+    res = {"items": len(items), "meshes": len(meshes), "pixels_per_step": wl.pixels,
+           "triangles_per_step": int(sum(len(meshes[m][1]) for m, _, _ in items)),
+           "tile": 1 << (tile or (4, 0))[0], "threads_per_tri": (tile or (4, 0))[1]}
+    g = _graph(wl.batched_step, dev, warm=max(2, warmup))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    s = torch.cuda.current_stream(dev)
+
+    def timed(fn, n):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        torch.cuda.synchronize(dev)
+        for i in range(n):
+            flush.fill_(i & 0xff)
+            evs[i][0].record(s)
+            fn()
+            evs[i][1].record(s)
+        torch.cuda.synchronize(dev)
+        return sum(a.elapsed_time(b) for a, b in evs) / n
+
+    ms = timed(g.replay, steps)
+    res["batched"] = {"value": wl.pixels / ms / 1e3, "unit": UNIT, "ms_per_step": ms,
+                      "launches_per_step": 13, "path": "batched, one CUDA graph"}
+    res["peak_memory_gb"] = torch.cuda.max_memory_allocated(dev) / 1e9
+    if recompute:
+        res["batched"]["recompute"] = True
+    if plain:
+        for _ in range(max(2, warmup)):
+            wl.plain_step()
+        ms_p = timed(wl.plain_step, max(3, steps // 4))
+        res["plain_eager"] = {"value": wl.pixels / ms_p / 1e3, "unit": UNIT, "ms_per_step": ms_p,
+                              "launches_per_step": LAUNCHES_PER_STEP * len(items)}
+        try:
+            gp = _graph(wl.plain_step, dev, warm=2)
+            ms_g = timed(gp.replay, steps)
+            res["plain_graphed"] = {"value": wl.pixels / ms_g / 1e3, "unit": UNIT, "ms_per_step": ms_g}
+        except RuntimeError as e:  # pragma: no cover
+            res["plain_graphed"] = {"unavailable": str(e)[:200]}
+    return res
 
 
 def _clock_sampler():
@@ -178,7 +403,7 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None):
+def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None, batch=None):
     """CUDA-event time of each C-ABI entry point of the step on the same
     inputs: each entry point is captured alone in a CUDA graph and replayed
     between events on the launching stream, L2 flushed before every replay."""
@@ -186,7 +411,16 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None):
     from diffrp_gb300 import _ffi
     from diffrp_gb300 import nvdr as dr
     s = torch.cuda.current_stream(dev)
-    sp = s.cuda_stream
+
+    class _CurStream:
+        """ctypes argument: the stream current at call time (graph capture
+        switches streams)."""
+
+        @property
+        def _as_parameter_(self):
+            return ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+    sp = _CurStream()
     ctx = dr.RasterizeCudaContext(dev)
     if tuned is not None:
         from diffrp_gb300 import autotune
@@ -225,6 +459,14 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None):
         "rasterize_bwd": lambda: _ffi.call("drp_rasterize_bwd", clip.data_ptr(), 0, V, tri.data_ptr(), F, 1, H, W,
                                            rast.data_ptr(), grast.data_ptr(), None, gpos.data_ptr(), sp),
     }
+    if batch is not None:
+        b_rast, b_color, b_out = batch.forward_buffers(clip, a_t)
+        b_g = g.reshape(-1).contiguous()
+        b_gp = torch.zeros_like(clip)
+        b_ga = torch.zeros_like(a_t).reshape(-1)
+        flat_attr = a_t.reshape(-1)
+        ops["batch_forward"] = lambda: batch._forward_raw(clip, flat_attr, b_rast, b_color, b_out)
+        ops["batch_backward"] = lambda: batch._backward_raw(clip, flat_attr, b_rast, b_color, b_g, b_gp, b_ga)
     P = H * W
     # Algorithmic bytes per launch ("Roofline accounting").
     algo = {
@@ -234,6 +476,12 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None):
         "antialias_bwd": P * (4 * C + 4 * C + 16 + 4 * C) + V * 16,
         "interpolate_bwd": P * (4 * C + 16 + 16) + V * 4 * C * 2,
         "rasterize_bwd": P * (16 + 16) + V * 16 * 2,
+        # fused raster + interpolation (rast and colour written), antialias
+        # (colour read, output written)
+        "batch_forward": P * (16 + 4 * C + 4 * C + 4 * C) + V * (16 + 4 * C) + F * 12,
+        # rast, colour and output gradient read once; vertex / attribute
+        # gradients written once
+        "batch_backward": P * (16 + 4 * C + 4 * C) + V * (16 + 4 * C) * 2 + F * 12,
     }
     times = {}
     for name, fn in ops.items():
@@ -316,6 +564,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="full", choices=["full", "steps"],
                     help="steps: only the warm-up and timed device-resident steps (for profilers)")
+    ap.add_argument("--workload", default="single", choices=["single", "views64", "uneven48", "large16"],
+                    help="single: the headline single-mesh line (with the 64-view batched comparison "
+                         "attached); others: one line for that batched workload")
+    ap.add_argument("--no-batched", action="store_true", help="skip the attached 64-view comparison")
+    ap.add_argument("--tile", default=None,
+                    help="fixed raster shape 'tile_log2,threads_per_tri' instead of autotuning (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -331,13 +585,46 @@ def main():
     torch.cuda.set_device(dev)
     import __graft_entry__
     __graft_entry__.build()
+    if args.workload != "single":
+        W_ = max(3, args.warmup)
+        res = run_batched(dev, args.workload, steps=args.steps, warmup=W_, plain=args.workload != "large16",
+                          recompute=args.workload == "large16")
+        if world > 1:
+            t = torch.tensor([res["batched"]["ms_per_step"]], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            res["batched"]["ms_per_step"] = float(t[0])
+            res["batched"]["value"] = res["pixels_per_step"] * world / float(t[0]) / 1e3
+        if rank == 0:
+            desc = {"views64": "64 views of icosphere-3 (1280 tris), 512x512, 8 ch",
+                    "uneven48": "48 meshes, 1e3-5e5 tris (log-uniform), 1-4 views at 256/512/1024, 4-16 ch",
+                    "large16": "2.09M-tri heightfield, 16 views at 2048x2048, 12 ch, recompute in backward"}
+            print(json.dumps({
+                "metric": METRIC, "value": res["batched"]["value"], "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": W_, "ms_per_step": res["batched"]["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded meshes, cameras, attributes and targets)",
+                "config": {"workload": desc[args.workload], "global_batch": res["items"] * world,
+                           "parallelism": "replicas" if world > 1 else "single GPU",
+                           "l2": "flushed between steps (256 MiB write outside the timed events)"},
+                "detail": res}))
+        if world > 1:
+            dist.destroy_process_group()
+        return 0
 
     verts_np, f, attr_np, mvp, target = make_workload()
     step = Step(dev, f, mvp, target)
     from diffrp_gb300 import autotune
     with torch.no_grad():
         clip0 = (torch.nn.functional.pad(torch.from_numpy(verts_np).to(dev), (0, 1), value=1.0) @ step.mvp.T)
-    tuned = autotune.tune_rasterizer(step.ctx, clip0.contiguous(), step.tri, (H, W), use_cache=False)
+    if args.tile:
+        tl, tpt = [int(x) for x in args.tile.split(",")]
+        tuned = {"tile_log2": tl, "threads_per_tri": tpt}
+        autotune.apply(step.ctx, tuned)
+        step.ctx.ensure_capacity(0)
+        step.ctx._sized = False
+        tuned["list_capacity"] = None
+    else:
+        tuned = autotune.tune_rasterizer(step.ctx, clip0.contiguous(), step.tri, (H, W), use_cache=False)
     verts = torch.from_numpy(verts_np).to(dev).requires_grad_(True)
     attr = torch.from_numpy(attr_np).to(dev).requires_grad_(True)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -348,6 +635,10 @@ def main():
     graphed = GraphedStep(step, verts_np, attr_np, dev)
     for _ in range(W_):
         graphed()
+    bstep = BatchStep(dev, f, mvp, target, len(verts_np), C, tile=(tuned["tile_log2"], tuned["threads_per_tri"]))
+    batched = GraphedStep(bstep, verts_np, attr_np, dev)
+    for _ in range(W_):
+        batched()
     torch.cuda.synchronize()
 
     def barrier():
@@ -368,10 +659,11 @@ def main():
         barrier()
         return sum(a.elapsed_time(b) for a, b in evs)
 
-    # -- device-resident timing: the graph-captured step is the headline; the
-    # eager (plain per-op launch) step is reported beside it ----------------
+    # -- device-resident timing: the batching form captured as one CUDA graph
+    # is the headline; the drop-in (plain per-op) path is reported beside it,
+    # graph-captured and eager ---------------------------------------------
     clk, clk_path = _clock_sampler()
-    total_ms = timed(graphed, args.steps)
+    total_ms = timed(batched, args.steps)
     if args.mode == "steps":
         if clk is not None:
             clk.terminate()
@@ -380,6 +672,7 @@ def main():
         if world > 1:
             dist.destroy_process_group()
         return 0
+    plain_ms = timed(graphed, args.steps)
     eager_ms = timed(lambda: step(verts, attr), args.steps)
 
     # -- end-to-end through the public API with host buffers -----------------
@@ -389,19 +682,22 @@ def main():
     h_gv = torch.empty_like(h_verts).pin_memory()
     h_ga = torch.empty_like(h_attr).pin_memory()
 
-    def e2e_step():
-        graphed.load(h_verts, h_attr)
-        loss = graphed()
-        h_loss.copy_(loss.detach(), non_blocking=True)
-        h_gv.copy_(graphed.verts.grad, non_blocking=True)
-        h_ga.copy_(graphed.attr.grad, non_blocking=True)
+    def e2e_of(gs):
+        def e2e_step():
+            gs.load(h_verts, h_attr)
+            loss = gs()
+            h_loss.copy_(loss.detach(), non_blocking=True)
+            h_gv.copy_(gs.verts.grad, non_blocking=True)
+            h_ga.copy_(gs.attr.grad, non_blocking=True)
+        return e2e_step
 
-    e2e_ms = timed(e2e_step, args.steps)
+    e2e_ms = timed(e2e_of(batched), args.steps)
+    e2e_plain_ms = timed(e2e_of(graphed), args.steps)
     clocks = _clock_summary(clk, clk_path, dev.index if dev.index is not None else 0)
     if world > 1:
-        t = torch.tensor([total_ms, e2e_ms, eager_ms], device=dev)
+        t = torch.tensor([total_ms, e2e_ms, eager_ms, plain_ms, e2e_plain_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, e2e_ms, eager_ms = float(t[0]), float(t[1]), float(t[2])
+        total_ms, e2e_ms, eager_ms, plain_ms, e2e_plain_ms = [float(x) for x in t]
 
     pix = H * W * args.steps * world
     value = pix / (total_ms / 1e3) / 1e6
@@ -410,8 +706,8 @@ def main():
     d2h = 4 + h_gv.numel() * 4 + h_ga.numel() * 4
 
     if rank == 0:
-        times, algo = kernel_breakdown(dev, verts_np, f, attr_np, mvp, target, tuned=tuned)
-        dom = max(times, key=times.get)
+        times, algo = kernel_breakdown(dev, verts_np, f, attr_np, mvp, target, tuned=tuned, batch=bstep.renderer)
+        dom = max(["batch_forward", "batch_backward"], key=times.get)
         peak, peak_kind = _peaks()
         achieved = algo[dom] / (times[dom] / 1e3) / 1e9
         traffic = None
@@ -428,7 +724,7 @@ def main():
                        "global_batch": world, "resolution": [H, W], "channels": C,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "flushed between steps (256 MiB write outside the timed events)",
-                       "path": "drop-in nvdr API ops, whole fwd+bwd step captured as one CUDA graph",
+                       "path": "batching form (diffrp_gb300.batch, one item), whole fwd+bwd step as one CUDA graph",
                        "raster_tuning": {"tile": 1 << tuned["tile_log2"], "threads_per_tri": tuned["threads_per_tri"],
                                          "list_capacity": tuned["list_capacity"]}},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -436,11 +732,17 @@ def main():
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                          "algorithmic_bytes": algo[dom], "kernel_ms": times[dom]},
             "kernel_ms": times,
+            "plain": {"value": pix / (plain_ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": plain_ms / args.steps,
+                      "note": "same step through the drop-in nvdr ops, captured as one CUDA graph"},
             "eager": {"value": pix / (eager_ms / 1e3) / 1e6, "unit": UNIT,
-                      "note": "same step, eager per-op launches (host-launch bound)"},
+                      "note": "same step, drop-in nvdr ops, eager per-op launches (host-launch bound)"},
+            "e2e_dropin": {"value": pix / (e2e_plain_ms / 1e3) / 1e6, "unit": UNIT,
+                           "note": "end to end through the drop-in nvdr ops (graph), host buffers"},
             "clocks": clocks,
-            "gpu_launches": LAUNCHES_PER_STEP * args.steps * 3,
+            "gpu_launches": (BATCH_LAUNCHES_PER_STEP * 2 + LAUNCHES_PER_STEP * 3) * args.steps,
         }
+        if not args.no_batched:
+            line["batched_views64"] = run_batched(dev, "views64", steps=max(5, args.steps // 3), warmup=W_)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(verts_np, f, attr_np, mvp, target)
         print(json.dumps(line))
