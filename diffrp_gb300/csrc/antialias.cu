@@ -191,3 +191,93 @@ int launch_aa_bwd(const AAArgs& a, cudaStream_t s) {
 }
 
 }  // namespace drp
+
+// ---------------------------------------------------------------------------
+// drp_antialias_fwd_noalloc: the antialias forward for callers that cannot
+// allocate device memory.  Its per-triangle scratch (the 32-byte screen-space
+// records that drp_antialias_fwd keeps in a caller workspace) lives in the
+// fixed array below, which every GPU that loads this library keeps for the
+// life of the process.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+#include "../../include/diffrp_gb300.h"
+
+static __device__ __align__(256) float4 g_aa_noalloc_scratch[2 * DRP_NOALLOC_AA_MAX_TRIANGLE_VIEWS];
+
+namespace {
+std::mutex g_noalloc_mutex;
+constexpr int kMaxDevices = 64;
+void* g_noalloc_scratch_addr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (host code may not use the array's name as a device address).
+int noalloc_scratch(void** out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        drp_set_last_error("drp_antialias_fwd_noalloc: cudaGetDevice failed");
+        return DRP_STATUS_CUDA_ERROR;
+    }
+    if (dev < 0 || dev >= kMaxDevices) {
+        drp_set_last_error("drp_antialias_fwd_noalloc: device ordinal out of range");
+        return DRP_STATUS_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_scratch_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_aa_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            drp_set_last_error("drp_antialias_fwd_noalloc: cudaGetSymbolAddress of the scratch array failed");
+            return DRP_STATUS_CUDA_ERROR;
+        }
+        g_noalloc_scratch_addr[dev] = p;
+    }
+    *out = g_noalloc_scratch_addr[dev];
+    return DRP_STATUS_OK;
+}
+}  // namespace
+
+extern "C" __attribute__((visibility("default"))) int drp_antialias_fwd_noalloc(
+    const float* color, int channels, const float* rast, const float* pos, long long pos_view_stride,
+    long long num_vertices, const int* tri, long long num_triangles, const int* nbr, int num_views, int height,
+    int width, float* out, void* stream) {
+    if (num_views <= 0 || height <= 0 || width <= 0 || height > DRP_MAX_RESOLUTION || width > DRP_MAX_RESOLUTION) {
+        drp_set_last_error("drp_antialias_fwd_noalloc: bad views / resolution");
+        return DRP_STATUS_INVALID_ARGUMENT;
+    }
+    if (channels <= 0 || num_triangles < 0 || num_vertices < 0 || pos_view_stride < 0 || (pos_view_stride % 4)) {
+        drp_set_last_error("drp_antialias_fwd_noalloc: bad channels, sizes or stride");
+        return DRP_STATUS_INVALID_ARGUMENT;
+    }
+    if ((long long)num_views * num_triangles > DRP_NOALLOC_AA_MAX_TRIANGLE_VIEWS) {
+        drp_set_last_error("drp_antialias_fwd_noalloc: num_views * num_triangles exceeds "
+                           "DRP_NOALLOC_AA_MAX_TRIANGLE_VIEWS (262144); use drp_antialias_fwd with a workspace");
+        return DRP_STATUS_INVALID_ARGUMENT;
+    }
+    if (!color || !rast || !pos || !tri || !out || (reinterpret_cast<uintptr_t>(rast) & 15) ||
+        (reinterpret_cast<uintptr_t>(pos) & 15)) {
+        drp_set_last_error("drp_antialias_fwd_noalloc: null or misaligned pointer");
+        return DRP_STATUS_INVALID_ARGUMENT;
+    }
+    void* scratch = nullptr;
+    const int st = noalloc_scratch(&scratch);
+    if (st != DRP_STATUS_OK) return st;
+    drp::AAArgs a{};
+    a.color = color;
+    a.C = channels;
+    a.rast = rast;
+    a.pos = pos;
+    a.pos_view_stride = pos_view_stride;
+    a.num_vertices = num_vertices;
+    a.num_triangles = num_triangles;
+    a.tri = tri;
+    a.nbr = nbr;
+    a.tri_rec = scratch;  // every record read by the pixel pass is written by the setup pass first
+    a.B = num_views;
+    a.H = height;
+    a.W = width;
+    a.out = out;
+    drp::launch_aa_fwd(a, static_cast<cudaStream_t>(stream));
+    return drp_check_launch("drp_antialias_fwd_noalloc");
+}

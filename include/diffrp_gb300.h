@@ -170,6 +170,31 @@ int drp_antialias_fwd(void* workspace, size_t workspace_bytes, const float* colo
                       long long num_triangles, const int* nbr, int num_views, int height, int width, float* out,
                       void* stream);
 
+/* Most num_views * num_triangles that drp_antialias_fwd_noalloc accepts
+ * (its fixed scratch holds 32 bytes per triangle and view: 8 MiB). */
+#define DRP_NOALLOC_AA_MAX_TRIANGLE_VIEWS 262144
+
+/*
+ * drp_antialias_fwd without a workspace argument, for callers that cannot
+ * allocate device memory: a host whose GPU memory is handed out by someone
+ * else's allocator or reserved up front (an engine or plugin host with a
+ * fixed budget), or code that must not allocate at the call site.  It
+ * allocates nothing: the per-triangle scratch is a fixed array inside this
+ * library (8 MiB per GPU, held until the process exits), so the call rejects
+ * num_views * num_triangles above DRP_NOALLOC_AA_MAX_TRIANGLE_VIEWS with
+ * DRP_STATUS_INVALID_ARGUMENT.  Same arguments and output as
+ * drp_antialias_fwd.  The first call on each device looks up the array's
+ * device address (cudaGetSymbolAddress) -- make that first call before any
+ * stream capture.  All calls share the one array: calls whose GPU work
+ * overlaps (different streams, or threads without ordering) race on it.
+ * No counterpart in the reference: dr.antialias always allocates its own
+ * buffers.
+ */
+int drp_antialias_fwd_noalloc(const float* color, int channels, const float* rast, const float* pos,
+                              long long pos_view_stride, long long num_vertices, const int* tri,
+                              long long num_triangles, const int* nbr, int num_views, int height, int width,
+                              float* out, void* stream);
+
 /* Backward: grad_color overwritten, grad_pos accumulated (times
  * pos_gradient_boost); grad_pos may be NULL. */
 int drp_antialias_bwd(void* workspace, size_t workspace_bytes, const float* color, int channels, const float* rast,
