@@ -324,10 +324,15 @@ class SurfaceDeferredRenderSession(RenderSessionMixin):
 
     def edge_gradient(self, rgb: torch.Tensor):
         """Edge-gradient visibility operator (Rasterized Edge Gradients): the
-        image is returned unchanged; its backward adds screen-space gradients
-        to the clip-space positions of the triangles on either side of every
-        pixel boundary where the triangle id changes."""
-        from .edge_gradient import edge_gradient
-        rast = self.rasterize()[0]
-        vao = self.vertex_array_object()
-        return torch.flipud(edge_gradient(torch.flipud(rgb), rast, self.clip_space(), vao.tris.contiguous()))
+        (H, W, C) image is returned unchanged; its backward adds gradients to
+        the fragment positions across every pixel boundary where the triangle
+        id changes, and from there to the geometry."""
+        from .edge_gradient import EdgeGradientFn
+        from .interpolator import polyfill_interpolate
+        rast = self.rasterize()[0].squeeze(0)
+        clip = self.clip_space()
+        tris = self.vertex_array_object().tris
+        frag = polyfill_interpolate(clip, rast, tris[float_to_triidx(rast[..., 3]) - 1], 1.0)
+        frag_xy = frag[..., :2] / frag[..., 3:4]
+        flat_tris_xy = (clip[..., :2] / clip[..., 3:4])[tris.long()]
+        return torch.flipud(EdgeGradientFn.apply(frag_xy, flat_tris_xy, rast, torch.flipud(rgb)))

@@ -204,6 +204,22 @@ int drp_antialias_bwd(void* workspace, size_t workspace_bytes, const float* colo
                       void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Edge-gradient visibility operator                                         */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * Backward of _EdgeGradient (diffrp/rendering/surface_deferred.py:126-169),
+ * the operator behind SurfaceDeferredRenderSession.edge_gradient
+ * (:777-804).  All buffers are in the bottom-up rast frame: frag_xy (H, W, 2)
+ * fragment NDC positions, tris_xy (F, 3, 2) triangle NDC vertices, rast
+ * (H, W, 4), rgb and grad_out (H, W, C).  grad_frag_xy (H, W, 2) is
+ * overwritten.
+ */
+int drp_edge_gradient_bwd(const float* frag_xy, const float* tris_xy, long long num_triangles, const float* rast,
+                          const float* rgb, int channels, const float* grad_out, int height, int width,
+                          float* grad_frag_xy, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Batching form: many (mesh, view, resolution) items per launch             */
 /* ------------------------------------------------------------------------ */
 

@@ -98,6 +98,17 @@ def _install_stubs():
 
     calibur.projection_gl_persp = projection_gl_persp
     calibur.normalized = lambda x: np.asarray(x) / np.linalg.norm(x)
+    import torch_redstone
+
+    def supercat(tensors, dim=0):
+        """Concatenate along ``dim``, broadcasting every other dimension."""
+        nd = max(t.dim() for t in tensors)
+        ts = [t.reshape((1,) * (nd - t.dim()) + tuple(t.shape)) for t in tensors]
+        d = dim % nd
+        shape = [max(t.shape[i] for t in ts) for i in range(nd)]
+        return torch.cat([t.expand(*[t.shape[i] if i == d else shape[i] for i in range(nd)]) for t in ts], dim=d)
+
+    torch_redstone.supercat = supercat
     import nvdiffrast
     nvdiffrast.torch = oracle_dr
     sys.modules["nvdiffrast.torch"] = oracle_dr
@@ -260,6 +271,30 @@ def render(api, d, name, session_cls, options_cls, ctx=None):
     return {k: v.detach().cpu().numpy() for k, v in out.items()}
 
 
+def edge_gradient_golden(mods, normals_out, seed=7):
+    """The reference's own _EdgeGradient backward on the inputs its session
+    forms for the face-soup normals scenario (surface_deferred.py:795-804)."""
+    sd = mods["diffrp.rendering.surface_deferred"]
+    interp = mods["diffrp.rendering.interpolator"]
+    rast = torch.from_numpy(normals_out["rast"])[0]
+    clip = torch.from_numpy(normals_out["clip"])
+    F = clip.shape[0] // 3
+    tris = torch.arange(3 * F, dtype=torch.int32).reshape(F, 3)
+    frag = interp.polyfill_interpolate(clip, rast, tris[interp.float_to_triidx(rast[..., 3]) - 1], 1.0)
+    frag_xy = (frag[..., :2] / frag[..., 3:4]).detach()
+    flat_tris_xy = (clip[..., :2] / clip[..., 3:4])[tris.long()]
+    rng = np.random.default_rng(seed)
+    rgb = torch.from_numpy(np.flipud(normals_out["normals"][..., :3]).copy())
+    grad = torch.from_numpy(rng.normal(size=tuple(rgb.shape)).astype(np.float32))
+    leaf = frag_xy.clone().requires_grad_(True)
+    rgb_leaf = rgb.clone().requires_grad_(True)
+    out = sd._EdgeGradient.apply(leaf, flat_tris_xy, rast, rgb_leaf)
+    out.backward(grad)
+    return {"frag_xy": frag_xy.numpy(), "flat_tris_xy": flat_tris_xy.numpy(), "rast": rast.numpy(),
+            "rgb": rgb.numpy(), "grad_out": grad.numpy(), "grad_frag_xy": leaf.grad.numpy(),
+            "grad_rgb": rgb_leaf.grad.numpy()}
+
+
 def main():
     mods = _load_reference()
     sc = mods["diffrp.scene"]
@@ -277,6 +312,11 @@ def main():
         path = os.path.join(HERE, "session_%s.npz" % name)
         np.savez_compressed(path, **payload)
         print("wrote", path, sorted(res))
+        if name == "normals":
+            eg = edge_gradient_golden(mods, res)
+            path = os.path.join(HERE, "edge_gradient.npz")
+            np.savez_compressed(path, **eg)
+            print("wrote", path, sorted(eg))
 
 
 if __name__ == "__main__":
