@@ -629,12 +629,13 @@ def main():
     attr = torch.from_numpy(attr_np).to(dev).requires_grad_(True)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     W_ = max(3, args.warmup)
-    for _ in range(W_):
-        step(verts, attr)
-    torch.cuda.synchronize()
-    graphed = GraphedStep(step, verts_np, attr_np, dev)
-    for _ in range(W_):
-        graphed()
+    if args.mode != "steps":
+        for _ in range(W_):
+            step(verts, attr)
+        torch.cuda.synchronize()
+        graphed = GraphedStep(step, verts_np, attr_np, dev)
+        for _ in range(W_):
+            graphed()
     bstep = BatchStep(dev, f, mvp, target, len(verts_np), C, tile=(tuned["tile_log2"], tuned["threads_per_tri"]))
     batched = GraphedStep(bstep, verts_np, attr_np, dev)
     for _ in range(W_):

@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(256) batch_aa_fwd_kernel(BatchArgs a) {
 // Fused backward of one pixel: antialias colour gradient -> interpolation
 // backward (attribute gradients, d/du, d/dv) -> rasterisation backward
 // (vertex gradients).  Warps never straddle items (256-pixel blocks).
-__global__ void __launch_bounds__(256) batch_bwd_kernel(BatchArgs a) {
+__global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
     const int2 blk = a.pix_blocks[blockIdx.x];
     const drp_batch_item& it = a.items[blk.x];
     const int pix = blk.y * 256 + threadIdx.x;
@@ -257,11 +257,10 @@ __global__ void __launch_bounds__(256) batch_bwd_kernel(BatchArgs a) {
     for (int k = 0; k < 12; ++k) pv[k] = 0.f;
     if (t >= 0) {
         const int py = pix / W, px = pix - py * W;
-        const float4 p0 = P[i0], p1 = P[i1], p2 = P[i2];
-        Shade S;
-        shade_eval(p0, p1, p2, px, py, W, H, S);
+        const float X = fmaf((float)(2 * px + 1), __frcp_rn((float)W), -1.0f);
+        const float Y = fmaf((float)(2 * py + 1), __frcp_rn((float)H), -1.0f);
         float4 g3[3];
-        shade_grad(p0, p1, p2, S, gu, gv, 0.f, nullptr, g3);
+        uv_grad_fast(P[i0], P[i1], P[i2], X, Y, gu, gv, g3);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             pv[4 * k] = g3[k].x;

@@ -310,6 +310,31 @@ __device__ __forceinline__ void shade_grad(const float4& p0, const float4& p1, c
     }
 }
 
+// Gradient of (u, v) alone w.r.t. the three clip vertices at NDC (X, Y),
+// for backward passes (no bit-exactness needed: reciprocals replace IEEE
+// divisions).  out[i] receives dL/d p_i.
+__device__ __forceinline__ void uv_grad_fast(const float4& p0, const float4& p1, const float4& p2, float X, float Y,
+                                             float gu, float gv, float4 out[3]) {
+    const float a[3] = {p0.x - X * p0.w, p1.x - X * p1.w, p2.x - X * p2.w};
+    const float c[3] = {p0.y - Y * p0.w, p1.y - Y * p1.w, p2.y - Y * p2.w};
+    const float n0 = fmaf(a[1], c[2], -a[2] * c[1]);
+    const float n1 = fmaf(a[2], c[0], -a[0] * c[2]);
+    const float n2 = fmaf(a[0], c[1], -a[1] * c[0]);
+    const float inv_s = __frcp_rn((n0 + n1) + n2);
+    const float beta = fmaf(gu, n0, gv * n1) * inv_s;  // sum gb_i b_i
+    const float gn[3] = {(gu - beta) * inv_s, (gv - beta) * inv_s, -beta * inv_s};
+    float ga[3], gc[3];
+    cross3(c, gn, ga);
+    cross3(gn, a, gc);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        out[i].x = ga[i];
+        out[i].y = gc[i];
+        out[i].z = 0.0f;
+        out[i].w = -X * ga[i] - Y * gc[i];
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Warp-level helpers.
 // ---------------------------------------------------------------------------
@@ -322,6 +347,7 @@ __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 struct Seg {
     int run_end;
     bool head;
+    int steps;  // shuffle steps needed by the longest run of the warp
 };
 
 __device__ __forceinline__ Seg seg_setup(long long key) {
@@ -333,6 +359,9 @@ __device__ __forceinline__ Seg seg_setup(long long key) {
     const unsigned heads = __ballot_sync(FULL, s.head);
     const unsigned after = (lane == 31) ? 0u : (heads & ~((2u << lane) - 1u));
     s.run_end = after ? (__ffs(after) - 2) : 31;
+    const unsigned len = s.head ? (unsigned)(s.run_end - lane + 1) : 1u;
+    const unsigned longest = __reduce_max_sync(FULL, len);
+    s.steps = longest <= 1 ? 0 : 32 - __clz(longest - 1);  // ceil(log2(longest))
     return s;
 }
 
@@ -340,8 +369,8 @@ template <int N>
 __device__ __forceinline__ void seg_reduce(const Seg& s, float (&v)[N]) {
     const unsigned FULL = 0xffffffffu;
     const int lane = lane_id();
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
+    for (int k = 0; k < s.steps; ++k) {  // warp-uniform trip count
+        const int off = 1 << k;
 #pragma unroll
         for (int i = 0; i < N; ++i) {
             const float o = __shfl_down_sync(FULL, v[i], off);
