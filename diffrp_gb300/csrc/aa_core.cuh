@@ -78,10 +78,11 @@ struct AAPair {
     float2 cF, cO;
 };
 
-// Pair (A, B) with A the left / lower pixel; rA, rB their rast rows; rec the
-// view's triangle records (F triangles); W the view width.
-__device__ __forceinline__ void aa_pair(const float4* rec, long long F, int W, int A, int Bp, const float4& rA,
-                                        const float4& rB, AAPair& R) {
+// Pair (A, B) with A the left / lower pixel at column ax, row ay and B its
+// right (vertical = false) or upper (vertical = true) neighbour; rA, rB their
+// rast rows; rec the view's triangle records (F triangles).
+__device__ __forceinline__ void aa_pair(const float4* rec, long long F, int A, int Bp, int ax, int ay, bool vertical,
+                                        const float4& rA, const float4& rB, AAPair& R) {
     R.valid = false;
     const int tA = rast_tri(rA.w), tB = rast_tri(rB.w);
     const int cA = (tA >= 0 && tA < F) ? tA : -1;
@@ -102,8 +103,11 @@ __device__ __forceinline__ void aa_pair(const float4* rec, long long F, int W, i
     R.s[0] = make_float2(q0.x, q0.y);
     R.s[1] = make_float2(q0.z, q0.w);
     R.s[2] = make_float2(q1.x, q1.y);
-    R.cF = make_float2((float)(Fp % W) + 0.5f, (float)(Fp / W) + 0.5f);
-    R.cO = make_float2((float)(Op % W) + 0.5f, (float)(Op / W) + 0.5f);
+    const float2 ctrA = make_float2((float)ax + 0.5f, (float)ay + 0.5f);
+    const float2 ctrB = vertical ? make_float2(ctrA.x, (float)(ay + 1) + 0.5f)
+                                 : make_float2((float)(ax + 1) + 0.5f, ctrA.y);
+    R.cF = Fp == A ? ctrA : ctrB;
+    R.cO = Fp == A ? ctrB : ctrA;
     int best = -1;
     float bt = 0.f, beF = 0.f, beO = 0.f;
 #pragma unroll
@@ -144,13 +148,15 @@ __device__ __forceinline__ void aa_pair(const float4* rec, long long F, int W, i
 }
 
 // Pair slot q of a pixel, in the fixed order left, right, below, above:
-// (first pixel, second pixel) with the first being the left / lower one.
-__device__ __forceinline__ bool pair_slot(int q, int pix, int px, int py, int W, int H, int& A, int& B) {
+// (first pixel, second pixel) with the first being the left / lower one, at
+// column ax, row ay; vertical for the below / above pairs.
+__device__ __forceinline__ bool pair_slot(int q, int pix, int px, int py, int W, int H, int& A, int& B, int& ax,
+                                          int& ay, bool& vertical) {
     switch (q) {
-    case 0: A = pix - 1; B = pix; return px > 0;
-    case 1: A = pix; B = pix + 1; return px < W - 1;
-    case 2: A = pix - W; B = pix; return py > 0;
-    default: A = pix; B = pix + W; return py < H - 1;
+    case 0: A = pix - 1; B = pix; ax = px - 1; ay = py; vertical = false; return px > 0;
+    case 1: A = pix; B = pix + 1; ax = px; ay = py; vertical = false; return px < W - 1;
+    case 2: A = pix - W; B = pix; ax = px; ay = py - 1; vertical = true; return py > 0;
+    default: A = pix; B = pix + W; ax = px; ay = py; vertical = true; return py < H - 1;
     }
 }
 
@@ -168,13 +174,14 @@ __device__ __forceinline__ void aa_fwd_pixel(const float4* R, const float* Cc, c
     for (int q = 0; q < 4; ++q) {
         src[q] = -1;
         wt[q] = 0.f;
-        int A, B;
-        if (!pair_slot(q, pix, px, py, W, H, A, B)) continue;
+        int A, B, ax, ay;
+        bool vert;
+        if (!pair_slot(q, pix, px, py, W, H, A, B, ax, ay, vert)) continue;
         const int other = A == pix ? B : A;
         const float4 ro = R[other];
         if (ro.w == rs.w) continue;
         AAPair pr;
-        aa_pair(rec, F, W, A, B, A == pix ? rs : ro, A == pix ? ro : rs, pr);
+        aa_pair(rec, F, A, B, ax, ay, vert, A == pix ? rs : ro, A == pix ? ro : rs, pr);
         if (pr.valid && pr.target == pix) {
             src[q] = pr.src;
             wt[q] = pr.w;
@@ -220,13 +227,14 @@ __device__ __forceinline__ void aa_bwd_terms(const float4* R, const float* Cc, c
         at.role[q] = 0;
         at.tgt[q] = 0;
         at.wt[q] = 0.f;
-        int A, B;
-        if (!pair_slot(q, pix, px, py, W, H, A, B)) continue;
+        int A, B, ax, ay;
+        bool vert;
+        if (!pair_slot(q, pix, px, py, W, H, A, B, ax, ay, vert)) continue;
         const int other = A == pix ? B : A;
         const float4 ro = R[other];
         if (ro.w == rs.w) continue;
         AAPair p;
-        aa_pair(rec, F, W, A, B, A == pix ? rs : ro, A == pix ? ro : rs, p);
+        aa_pair(rec, F, A, B, ax, ay, vert, A == pix ? rs : ro, A == pix ? ro : rs, p);
         if (!p.valid) continue;
         at.role[q] = p.target == pix ? 1 : 2;
         at.tgt[q] = p.target;

@@ -379,11 +379,14 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
                 if (!(e2.y & TP_ACTIVE)) continue;
                 const int4 e0 = tp.e0, e1 = tp.e1, v2b = tp.v2b;
                 const int x0 = v2b.z & 0xffff, x1 = v2b.z >> 16, y0 = v2b.w & 0xffff, y1 = v2b.w >> 16;
+                // 8x4 blocks overlapped by the primitive's bbox: columns c0..c1, rows r0..r1
+                const int c0 = x0 >> 3, c1 = x1 >> 3, r0 = y0 >> 2, r1 = y1 >> 2;
 #pragma unroll
                 for (int q = 0; q < PPT; ++q) {
                     int dx, dy, bx, by;
                     tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
-                    if (x1 < bx || x0 > bx + 7 || y1 < by || y0 > by + 3) continue;  // warp-uniform
+                    const int bc = bx >> 3, br = by >> 2;
+                    if (bc < c0 || bc > c1 || br < r0 || br > r1) continue;  // warp-uniform
                     const int sx = (tx0 + dx) * DRP_SUBPIX + DRP_HALF_SUBPIX;
                     const int sy = (ty0 + dy) * DRP_SUBPIX + DRP_HALF_SUBPIX;
                     if (!tile_prim_covers(tp, e0, e1, e2, dx, dy, sx, sy)) continue;
