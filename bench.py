@@ -712,10 +712,13 @@ def main():
         peak, peak_kind = _peaks()
         achieved = algo[dom] / (times[dom] / 1e3) / 1e9
         traffic = None
-        tpath = os.path.join(ROOT, "profiles", "traffic.json")
+        tpath = os.path.join(ROOT, "profiles", "traffic.txt")
         if os.path.exists(tpath):
             with open(tpath) as fh:
-                traffic = json.load(fh).get(dom)
+                for ln in fh:
+                    parts = ln.split()
+                    if len(parts) == 2 and parts[0] == dom and not ln.startswith("#"):
+                        traffic = int(parts[1])
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": W_, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
