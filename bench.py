@@ -468,7 +468,7 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None, batc
         ops["batch_forward"] = lambda: batch._forward_raw(clip, flat_attr, b_rast, b_color, b_out)
         ops["batch_backward"] = lambda: batch._backward_raw(clip, flat_attr, b_rast, b_color, b_g, b_gp, b_ga)
     P = H * W
-    # Algorithmic bytes per launch ("Roofline accounting").
+    # Algorithmic bytes per launch: every input read once, every output written once.
     algo = {
         "rasterize_fwd": P * 16 + V * 16 + F * 12,
         "interpolate_fwd": P * (16 + 4 * C) + V * 4 * C,
