@@ -302,18 +302,14 @@ def run_batched(dev, name, steps, warmup, plain=True, recompute=False, tune=True
     meshes, items = {"views64": views64_workload, "uneven48": uneven48_workload,
                      "large16": large16_workload}[name](dev)
     tile = None
-    if tune:
-        # tune the tile shape on the largest item's geometry
-        m, (H, W), mvp = max(items, key=lambda it: len(meshes[it[0]][1]) * it[1][0] * it[1][1])
-        v, f, _ = meshes[m]
-        clip = torch.from_numpy(np.concatenate([v, np.ones((len(v), 1), np.float32)], 1) @
-                                mvp.astype(np.float32).T).to(dev).contiguous()
-        tri = torch.from_numpy(f).to(dev)
-        ch = autotune.tune_rasterizer(autotune.nvdr.RasterizeCudaContext(dev), clip, tri, (H, W), reps=3,
-                                      use_cache=False)
-        tile = (ch["tile_log2"], ch["threads_per_tri"])
     torch.cuda.reset_peak_memory_stats(dev)
     wl = MultiViewWorkload(dev, meshes, items, recompute=recompute, tile=tile)
+    if tune:
+        with torch.no_grad():
+            pos0 = torch.cat([wl._clip(m, k) for k, (m, _) in enumerate(wl.items)])
+            attr0 = torch.cat([a.reshape(-1) for a in wl.attrs])
+            ch = autotune.tune_batch(wl.renderer, pos0, attr0, reps=3)
+        tile = (ch["tile_log2"], ch["threads_per_tri"])
     res = {"items": len(items), "meshes": len(meshes), "pixels_per_step": wl.pixels,
            "triangles_per_step": int(sum(len(meshes[m][1]) for m, _, _ in items)),
            "tile": 1 << (tile or (4, 0))[0], "threads_per_tri": (tile or (4, 0))[1]}
@@ -637,6 +633,12 @@ def main():
         for _ in range(W_):
             graphed()
     bstep = BatchStep(dev, f, mvp, target, len(verts_np), C, tile=(tuned["tile_log2"], tuned["threads_per_tri"]))
+    if not args.tile:
+        with torch.no_grad():
+            btuned = autotune.tune_batch(bstep.renderer, clip0.contiguous(),
+                                         torch.from_numpy(attr_np).to(dev).reshape(-1))
+    else:
+        btuned = {"tile_log2": tuned["tile_log2"], "threads_per_tri": tuned["threads_per_tri"]}
     batched = GraphedStep(bstep, verts_np, attr_np, dev)
     for _ in range(W_):
         batched()
@@ -729,8 +731,10 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "flushed between steps (256 MiB write outside the timed events)",
                        "path": "batching form (diffrp_gb300.batch, one item), whole fwd+bwd step as one CUDA graph",
-                       "raster_tuning": {"tile": 1 << tuned["tile_log2"], "threads_per_tri": tuned["threads_per_tri"],
-                                         "list_capacity": tuned["list_capacity"]}},
+                       "raster_tuning": {"tile": 1 << btuned["tile_log2"],
+                                         "threads_per_tri": btuned["threads_per_tri"],
+                                         "plain_path": {"tile": 1 << tuned["tile_log2"],
+                                                        "threads_per_tri": tuned["threads_per_tri"]}}},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,

@@ -18,7 +18,7 @@ import torch
 
 from . import nvdr
 
-__all__ = ["TILE_CHOICES", "TPT_CHOICES", "tune_rasterizer", "apply", "cache_path", "workload_key"]
+__all__ = ["TILE_CHOICES", "TPT_CHOICES", "tune_rasterizer", "tune_batch", "apply", "cache_path", "workload_key"]
 
 TILE_CHOICES = (3, 4, 5)
 TPT_CHOICES = (0, 1, 4, 8, 32)
@@ -106,3 +106,32 @@ def tune_rasterizer(ctx, pos, tri, resolution, ranges=None, reps=5, candidates=N
             table[key] = choice
             _store(table)
     return choice
+
+
+def tune_batch(renderer, pos, attr, reps=5, candidates=None):
+    """Time the batched forward (``drp_batch_forward``) of ``renderer`` on
+    its own items for every (tile size, threads per primitive) candidate and
+    keep the fastest; returns the choice with the measured times."""
+    if candidates is None:
+        candidates = [(t, p) for t in TILE_CHOICES for p in (0, 4)]
+    stream = torch.cuda.current_stream(pos.device)
+    times = {}
+    best = None
+    for tl, tpt in candidates:
+        renderer.set_raster_shape(tl, tpt)
+        rast, color, out = renderer.forward_buffers(pos, attr)  # sizes the tile lists
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            renderer._forward_raw(pos.contiguous(), attr.contiguous().reshape(-1), rast, color, out)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        ts.sort()
+        times["%d/%d" % (tl, tpt)] = ts[len(ts) // 2]
+        if best is None or ts[len(ts) // 2] < best[0]:
+            best = (ts[len(ts) // 2], tl, tpt)
+    renderer.set_raster_shape(best[1], best[2])
+    renderer.forward_buffers(pos, attr)
+    return {"tile_log2": best[1], "threads_per_tri": best[2], "ms": best[0], "times_ms": times}

@@ -86,31 +86,39 @@ class BatchRenderer:
         self.nbr = torch.cat(nbr_parts).contiguous()
         self.attr_floats = a0
         self.attr_offsets = attr_off
-        arr = (_Item * len(items))()
+        self._item_specs = []
         p0 = 0
         self.pos_offsets = []
-        for i, (m, (H, W)) in enumerate(items):
+        for m, (H, W) in items:
             tri, V, C = meshes[m]
-            arr[i].pos_offset = p0
-            arr[i].attr_offset = attr_off[m]
-            arr[i].tri_first = tri_first[m]
-            arr[i].tri_count = int(tri.shape[0])
-            arr[i].num_vertices = int(V)
-            arr[i].height = int(H)
-            arr[i].width = int(W)
-            arr[i].channels = int(C)
+            self._item_specs.append((p0, attr_off[m], tri_first[m], int(tri.shape[0]), int(V), int(H), int(W),
+                                     int(C)))
             self.pos_offsets.append(p0)
             p0 += int(V)
         self.pos_rows = p0
+        self.items = items
+        self._plan()
+
+    def _plan(self):
+        """(Re)build the item table and block maps for the current tile size."""
+        arr = (_Item * len(self.items))()
+        for i, (po, ao, tf, tc, V, H, W, C) in enumerate(self._item_specs):
+            arr[i].pos_offset = po
+            arr[i].attr_offset = ao
+            arr[i].tri_first = tf
+            arr[i].tri_count = tc
+            arr[i].num_vertices = V
+            arr[i].height = H
+            arr[i].width = W
+            arr[i].channels = C
         totals = (ctypes.c_longlong * 6)()
-        _ffi.call("drp_batch_plan", ctypes.addressof(arr), len(items), self.tile_log2, ctypes.addressof(totals))
+        _ffi.call("drp_batch_plan", ctypes.addressof(arr), len(self.items), self.tile_log2, ctypes.addressof(totals))
         (self.total_prims, self.total_tiles, self.total_pixels, self.image_floats, self.prim_blocks,
          self.pixel_blocks) = [int(x) for x in totals]
         pmap = (ctypes.c_int * max(2, 2 * self.prim_blocks))()
         xmap = (ctypes.c_int * max(2, 2 * self.pixel_blocks))()
-        _ffi.call("drp_batch_block_maps", ctypes.addressof(arr), len(items), ctypes.addressof(pmap),
+        _ffi.call("drp_batch_block_maps", ctypes.addressof(arr), len(self.items), ctypes.addressof(pmap),
                   ctypes.addressof(xmap))
-        self.items = items
         self.item_table = arr
         self._items_dev = torch.from_numpy(np.frombuffer(bytes(arr), dtype=np.uint8).copy()).to(self.device)
         self._pmap = torch.from_numpy(np.frombuffer(bytes(pmap), dtype=np.int32).copy()).to(self.device)
@@ -118,6 +126,14 @@ class BatchRenderer:
         self._capacity = 0
         self._ws = None
         self.last_list_entries = 0
+
+    def set_raster_shape(self, tile_log2, threads_per_tri):
+        """Change the fine-raster tile size / threads per primitive (re-plans;
+        call before capturing a CUDA graph)."""
+        self.threads_per_tri = int(threads_per_tri)
+        if int(tile_log2) != self.tile_log2:
+            self.tile_log2 = int(tile_log2)
+            self._plan()
 
     # -- layout helpers ---------------------------------------------------------
     def pack_positions(self, per_item):

@@ -95,6 +95,7 @@ struct BatchEmit {
     const int* tri;  // the item's mesh triangles (local vertex indices)
     const float* A;  // the item's mesh attributes
     int W, H, C;
+    bool vec;  // 128-bit attribute / colour access: C % 4 == 0 and both bases 16-byte aligned
     float4* rast;
     float* color;
     __device__ __forceinline__ void operator()(int px, int py, unsigned long long k, float X, float Y) const {
@@ -102,7 +103,11 @@ struct BatchEmit {
         float* col = color + o * C;
         if (k == ~0ull) {
             rast[o] = make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int c = 0; c < C; ++c) col[c] = 0.f;
+            if (vec) {
+                for (int c = 0; c < C; c += 4) *reinterpret_cast<float4*>(col + c) = make_float4(0.f, 0.f, 0.f, 0.f);
+            } else {
+                for (int c = 0; c < C; ++c) col[c] = 0.f;
+            }
             return;
         }
         const int t = (int)(uint32_t)(k & 0xffffffffu);
@@ -113,7 +118,21 @@ struct BatchEmit {
         const float* a0 = A + (long long)i0 * C;
         const float* a1 = A + (long long)i1 * C;
         const float* a2 = A + (long long)i2 * C;
-        for (int c = 0; c < C; ++c) col[c] = fmaf(a0[c] - a2[c], S.u, fmaf(a1[c] - a2[c], S.v, a2[c]));
+        if (vec) {
+            for (int c = 0; c < C; c += 4) {
+                const float4 x0 = __ldg(reinterpret_cast<const float4*>(a0 + c));
+                const float4 x1 = __ldg(reinterpret_cast<const float4*>(a1 + c));
+                const float4 x2 = __ldg(reinterpret_cast<const float4*>(a2 + c));
+                float4 o;
+                o.x = fmaf(x0.x - x2.x, S.u, fmaf(x1.x - x2.x, S.v, x2.x));
+                o.y = fmaf(x0.y - x2.y, S.u, fmaf(x1.y - x2.y, S.v, x2.y));
+                o.z = fmaf(x0.z - x2.z, S.u, fmaf(x1.z - x2.z, S.v, x2.z));
+                o.w = fmaf(x0.w - x2.w, S.u, fmaf(x1.w - x2.w, S.v, x2.w));
+                *reinterpret_cast<float4*>(col + c) = o;
+            }
+        } else {
+            for (int c = 0; c < C; ++c) col[c] = fmaf(a0[c] - a2[c], S.u, fmaf(a1[c] - a2[c], S.v, a2[c]));
+        }
     }
 };
 
@@ -170,6 +189,7 @@ batch_fine_kernel(BatchArgs a) {
         e.C = it.channels;
         e.rast = reinterpret_cast<float4*>(a.rast) + it.pixel_offset;
         e.color = a.color + it.image_offset;
+        e.vec = (it.channels & 3) == 0 && ((reinterpret_cast<uintptr_t>(e.A) | reinterpret_cast<uintptr_t>(e.color)) & 15) == 0;
         fine_tile<TILE_LOG2, TPT>(ft, e);
     }
 }
@@ -225,30 +245,62 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
     const Seg seg = seg_setup(t >= 0 ? (long long)t : (long long)(-1 - lane_id()));
     const float u = r.x, v = r.y, w = 1.0f - u - v;
     float gu = 0.f, gv = 0.f;
+    const bool vec = (C & 3) == 0 && ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(GA) |
+                                       reinterpret_cast<uintptr_t>(Gd)) & 15) == 0;
     for (int c0 = 0; c0 < C; c0 += 4) {
         float val[12];
 #pragma unroll
         for (int k = 0; k < 12; ++k) val[k] = 0.f;
         if (t >= 0) {
+            float g[4], x0[4], x1[4], x2[4];
+            if (vec) {
+                const float4 gq = *reinterpret_cast<const float4*>(Gd + (long long)pix * C + c0);
+                const float4 q0 = __ldg(reinterpret_cast<const float4*>(A + (long long)i0 * C + c0));
+                const float4 q1 = __ldg(reinterpret_cast<const float4*>(A + (long long)i1 * C + c0));
+                const float4 q2 = __ldg(reinterpret_cast<const float4*>(A + (long long)i2 * C + c0));
+                g[0] = gq.x; g[1] = gq.y; g[2] = gq.z; g[3] = gq.w;
+                x0[0] = q0.x; x0[1] = q0.y; x0[2] = q0.z; x0[3] = q0.w;
+                x1[0] = q1.x; x1[1] = q1.y; x1[2] = q1.z; x1[3] = q1.w;
+                x2[0] = q2.x; x2[1] = q2.y; x2[2] = q2.z; x2[3] = q2.w;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int c = c0 + k < C ? c0 + k : C - 1;
+                    g[k] = c0 + k < C ? Gd[(long long)pix * C + c] : 0.f;
+                    x0[k] = A[(long long)i0 * C + c];
+                    x1[k] = A[(long long)i1 * C + c];
+                    x2[k] = A[(long long)i2 * C + c];
+                }
+            }
+            if (at.any) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (c0 + k < C) g[k] = aa_bwd_channel(at, Gd, C, pix, c0 + k);
+            }
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const int c = c0 + k;
-                if (c >= C) break;
-                const float g = at.any ? aa_bwd_channel(at, Gd, C, pix, c) : Gd[(long long)pix * C + c];
-                const float x0 = A[(long long)i0 * C + c], x1 = A[(long long)i1 * C + c], x2 = A[(long long)i2 * C + c];
-                val[k] = g * u;
-                val[4 + k] = g * v;
-                val[8 + k] = g * w;
-                gu = fmaf(g, x0 - x2, gu);
-                gv = fmaf(g, x1 - x2, gv);
+                val[k] = g[k] * u;
+                val[4 + k] = g[k] * v;
+                val[8 + k] = g[k] * w;
+                gu = fmaf(g[k], x0[k] - x2[k], gu);
+                gv = fmaf(g[k], x1[k] - x2[k], gv);
             }
         }
         seg_reduce<12>(seg, val);
         if (t >= 0 && seg.head) {
-            for (int k = 0; k < 4 && c0 + k < C; ++k) {
-                atomicAdd(GA + (long long)i0 * C + c0 + k, val[k]);
-                atomicAdd(GA + (long long)i1 * C + c0 + k, val[4 + k]);
-                atomicAdd(GA + (long long)i2 * C + c0 + k, val[8 + k]);
+            if (vec) {
+                atomic_add4(reinterpret_cast<float4*>(GA + (long long)i0 * C + c0),
+                            make_float4(val[0], val[1], val[2], val[3]));
+                atomic_add4(reinterpret_cast<float4*>(GA + (long long)i1 * C + c0),
+                            make_float4(val[4], val[5], val[6], val[7]));
+                atomic_add4(reinterpret_cast<float4*>(GA + (long long)i2 * C + c0),
+                            make_float4(val[8], val[9], val[10], val[11]));
+            } else {
+                for (int k = 0; k < 4 && c0 + k < C; ++k) {
+                    atomicAdd(GA + (long long)i0 * C + c0 + k, val[k]);
+                    atomicAdd(GA + (long long)i1 * C + c0 + k, val[4 + k]);
+                    atomicAdd(GA + (long long)i2 * C + c0 + k, val[8 + k]);
+                }
             }
         }
     }
