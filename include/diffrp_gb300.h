@@ -220,6 +220,22 @@ int drp_edge_gradient_bwd(const float* frag_xy, const float* tris_xy, long long 
                           float* grad_frag_xy, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Fused image loss                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* Workspace bytes for drp_l1_loss_fwd over n elements. */
+int drp_l1_loss_workspace_size(long long n, size_t* bytes);
+
+/*
+ * loss = scale * sum |pred - target| and grad = scale * sign(pred - target)
+ * (0 at ties) in one pass over n elements; loss is one device float.  The
+ * mean-absolute-error image loss the benchmark fits renders with (no
+ * counterpart in the reference, which leaves losses to the user).
+ */
+int drp_l1_loss_fwd(void* workspace, size_t workspace_bytes, const float* pred, const float* target, long long n,
+                    float scale, float* loss, float* grad, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Batching form: many (mesh, view, resolution) items per launch             */
 /* ------------------------------------------------------------------------ */
 
