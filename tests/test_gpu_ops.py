@@ -225,3 +225,23 @@ def test_autotuner_choice_is_exact(cuda_lib, tmp_path, monkeypatch):
     np.testing.assert_array_equal(rast.cpu().numpy(), ref)
     again = autotune.tune_rasterizer(_ctx(), _t(pos), _t(tri), (96, 96))
     assert again["tile_log2"] == choice["tile_log2"] and again["threads_per_tri"] == choice["threads_per_tri"]
+
+
+def test_triangle_ids_above_2_pow_24(cuda_lib):
+    """Triangle ids past 2^24 use the float-bit encoding of the rast w channel
+    (diffrp/rendering/interpolator.py:24-29); the last triangles of a
+    2^24 + 64 triangle buffer (all earlier ones degenerate) must come back
+    with exactly the oracle's encoded ids, and decode to their indices."""
+    from diffrp_gb300.rendering.interpolator import float_to_triidx
+    n_deg = 1 << 24
+    soup, st = scenes.random_soup(64, seed=21)
+    pos = np.concatenate([np.array([[0.0, 0.0, 0.0, 1.0]], np.float32), soup])
+    tri = np.zeros((n_deg + 64, 3), np.int32)
+    tri[n_deg:] = st + 1
+    rast, _ = _dr().rasterize(_ctx(), _t(pos), _t(tri), (24, 24), grad_db=False)
+    ref, _, _ = O.rasterize(pos, tri, (24, 24), grad_db=False, nthreads=8)
+    r = rast.cpu().numpy()
+    np.testing.assert_array_equal(r, ref)
+    ids = float_to_triidx(rast[..., 3]).cpu().numpy()
+    covered = ids > 0
+    assert covered.sum() > 0 and (ids[covered] > n_deg).all()
