@@ -14,7 +14,8 @@ Packed layouts (see ``drp_batch_item`` in include/diffrp_gb300.h):
   attributes  (sum over meshes of V * C,) floats, mesh order;
   images      (sum over items of H * W * C,) floats, item order.
 ``recompute=True`` keeps no per-pixel buffer between forward and backward:
-the backward re-runs the rasteriser (and the fused interpolation) instead.
+the backward re-runs the rasteriser (and the fused interpolation, but not the
+antialias pass) instead.
 """
 import ctypes
 
@@ -167,14 +168,16 @@ class BatchRenderer:
         return self._ws
 
     def _forward_raw(self, pos, attr, rast, color, out):
+        """out=None writes rast and colour only (no antialias pass)."""
         cap = self._capacity if self._capacity else 4 * self.total_prims + 4096
+        optr = None if out is None else out.data_ptr()
         ws = self._workspace(cap)
         stream = torch.cuda.current_stream(self.device).cuda_stream
         args = (self._items_dev.data_ptr(), len(self.items), self._pmap.data_ptr(), self.prim_blocks,
                 self._xmap.data_ptr(), self.pixel_blocks, self.total_prims, self.total_tiles, pos.data_ptr(),
                 self.tri.data_ptr(), attr.data_ptr(), self.nbr.data_ptr(), self.tile_log2, self.threads_per_tri)
         _ffi.call("drp_batch_forward", ws.data_ptr(), ws.numel(), *args, cap, rast.data_ptr(), color.data_ptr(),
-                  out.data_ptr(), stream)
+                  optr, stream)
         if not self._capacity:
             torch.cuda.current_stream(self.device).synchronize()
             stats = ws[:16].view(torch.int64).cpu()
@@ -186,7 +189,7 @@ class BatchRenderer:
             if needed > cap:
                 ws = self._workspace(self._capacity)
                 _ffi.call("drp_batch_forward", ws.data_ptr(), ws.numel(), *args, self._capacity, rast.data_ptr(),
-                          color.data_ptr(), out.data_ptr(), stream)
+                          color.data_ptr(), optr, stream)
 
     def _backward_raw(self, pos, attr, rast, color, grad_out, grad_pos, grad_attr):
         ws = self._workspace(self._capacity)
@@ -238,9 +241,7 @@ class _BatchFn(torch.autograd.Function):
         if r.recompute:
             pos, attr = ctx.saved_tensors
             rast, color = r._buffers()
-            scratch = torch.empty_like(color)
-            r._forward_raw(pos, attr, rast, color, scratch)
-            del scratch
+            r._forward_raw(pos, attr, rast, color, None)
         else:
             pos, attr, rast, color = ctx.saved_tensors
         grad_pos = torch.zeros_like(pos)

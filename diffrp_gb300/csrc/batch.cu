@@ -49,6 +49,7 @@ struct BatchArgs {
     uint32_t* queue;
     int4* prims;
     uint32_t *tile_count, *tile_offset, *tile_cursor, *tile_list;
+    unsigned long long* chunk_sums;  // tile-scan chunk sums
     float4* aa_rec;
 };
 
@@ -333,7 +334,7 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
 // Host side.
 // ---------------------------------------------------------------------------
 struct BatchLayout {
-    size_t stats, queue, prims, count, offset, cursor, list, aa, total;
+    size_t stats, queue, prims, count, offset, cursor, chunks, list, aa, total;
 };
 
 BatchLayout batch_layout(long long total_prims, long long total_tiles, unsigned long long cap) {
@@ -345,7 +346,8 @@ BatchLayout batch_layout(long long total_prims, long long total_tiles, unsigned 
     L.count = up(L.prims + (size_t)total_prims * 48);
     L.offset = up(L.count + (size_t)total_tiles * 4);
     L.cursor = up(L.offset + (size_t)total_tiles * 4);
-    L.list = up(L.cursor + (size_t)total_tiles * 4);
+    L.chunks = up(L.cursor + (size_t)total_tiles * 4);
+    L.list = up(L.chunks + (size_t)scan_chunks(total_tiles) * 8);
     L.aa = up(L.list + (size_t)cap * 4);
     L.total = up(L.aa + (size_t)total_prims * 32);
     return L;
@@ -360,6 +362,7 @@ static void carve(BatchArgs& a, void* ws, const BatchLayout& L) {
     a.tile_offset = reinterpret_cast<uint32_t*>(w + L.offset);
     a.tile_cursor = reinterpret_cast<uint32_t*>(w + L.cursor);
     a.tile_list = reinterpret_cast<uint32_t*>(w + L.list);
+    a.chunk_sums = reinterpret_cast<unsigned long long*>(w + L.chunks);
     a.aa_rec = reinterpret_cast<float4*>(w + L.aa);
 }
 
@@ -382,8 +385,8 @@ template <int TL>
 static void launch_batch_raster(const BatchArgs& a, cudaStream_t s) {
     if (a.n_prim_blocks > 0) {
         batch_setup_bin_kernel<TL, false><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
-        scan_tiles_kernel<<<1, 1024, 0, s>>>(a.tile_count, a.tile_offset, a.tile_cursor, a.total_tiles,
-                                             reinterpret_cast<unsigned long long*>(a.stats));
+        launch_tile_scan(a.tile_count, a.tile_offset, a.tile_cursor, a.total_tiles, a.chunk_sums,
+                         reinterpret_cast<unsigned long long*>(a.stats), s);
         batch_setup_bin_kernel<TL, true><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
     } else {
         cudaMemsetAsync(a.tile_offset, 0, sizeof(uint32_t) * a.total_tiles, s);
@@ -408,6 +411,7 @@ int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream
     case 5: launch_batch_raster<5>(a, s); break;
     default: launch_batch_raster<4>(a, s); break;
     }
+    if (!a.out) return 0;  // raster + interpolation only (recomputing them for the backward)
     if (a.n_prim_blocks > 0) batch_aa_setup_kernel<<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
     if (a.n_pix_blocks > 0) batch_aa_fwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
     return 0;
@@ -540,7 +544,7 @@ DRP_API int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp
     if (tile_log2 < 3 || tile_log2 > 5) return bfail("batch: tile_log2 must be 3, 4 or 5");
     if (threads_per_tri < 0 || threads_per_tri > 32 || (threads_per_tri & (threads_per_tri - 1)))
         return bfail("batch: threads_per_tri must be 0 or a power of two <= 32");
-    if (!rast || !color || !out || (reinterpret_cast<uintptr_t>(rast) & 15)) return bfail("batch: bad outputs");
+    if (!rast || !color || (reinterpret_cast<uintptr_t>(rast) & 15)) return bfail("batch: bad outputs");
     a.nbr = nbr;
     a.tile_log2 = tile_log2;
     a.tpt = threads_per_tri;

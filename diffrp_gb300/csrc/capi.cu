@@ -37,7 +37,7 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 bool res_ok(int h, int w) { return h > 0 && w > 0 && h <= DRP_MAX_RESOLUTION && w <= DRP_MAX_RESOLUTION; }
 
 struct RasterLayout {
-    size_t stats, prims, count, offset, cursor, list, total;
+    size_t stats, prims, count, offset, cursor, chunks, list, total;
 };
 
 RasterLayout raster_layout(int B, long long maxT, int H, int W, int tile_log2, unsigned long long cap) {
@@ -50,7 +50,8 @@ RasterLayout raster_layout(int B, long long maxT, int H, int W, int tile_log2, u
     L.count = align_up(L.prims + (size_t)B * (size_t)maxT * 48, 256);
     L.offset = align_up(L.count + ntiles * 4, 256);
     L.cursor = align_up(L.offset + ntiles * 4, 256);
-    L.list = align_up(L.cursor + ntiles * 4, 256);
+    L.chunks = align_up(L.cursor + ntiles * 4, 256);
+    L.list = align_up(L.chunks + (size_t)drp::scan_chunks((long long)ntiles) * 8, 256);
     L.total = align_up(L.list + (size_t)cap * 4, 256);
     return L;
 }
@@ -145,6 +146,7 @@ DRP_API int drp_rasterize_fwd(void* workspace, size_t workspace_bytes, const flo
     a.ws.tile_offset = reinterpret_cast<uint32_t*>(w + L.offset);
     a.ws.tile_cursor = reinterpret_cast<uint32_t*>(w + L.cursor);
     a.ws.tile_list = reinterpret_cast<uint32_t*>(w + L.list);
+    a.ws.chunk_sums = reinterpret_cast<unsigned long long*>(w + L.chunks);
     drp::launch_rasterize(a, static_cast<cudaStream_t>(stream));
     return check_launch("drp_rasterize_fwd");
 }

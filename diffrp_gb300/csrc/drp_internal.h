@@ -7,6 +7,12 @@
 
 namespace drp {
 
+// Tile-count scan: chunks of kScanChunk tiles, one block of kScanThreads each.
+constexpr int kScanThreads = 256;
+constexpr int kScanPerThread = 16;
+constexpr int kScanChunk = kScanThreads * kScanPerThread;
+__host__ __device__ inline long long scan_chunks(long long n) { return (n + kScanChunk - 1) / kScanChunk; }
+
 // Device scratch carved out of the caller-provided rasterisation workspace.
 struct RasterWs {
     void* prims;            // B * max_view_tris * 48 bytes
@@ -14,6 +20,7 @@ struct RasterWs {
     uint32_t* tile_offset;  // B * tiles
     uint32_t* tile_cursor;  // B * tiles
     uint32_t* tile_list;    // list_capacity entries
+    unsigned long long* chunk_sums;  // tile-scan chunk sums, ceil(B * tiles / 4096)
     uint32_t* stats;        // [0..1] total list entries (u64), [2] device error bits, [3] spare
 };
 

@@ -1,28 +1,55 @@
 // loss.cu -- fused mean-absolute-error loss for image fitting: one pass reads
 // prediction and target, writes the per-element gradient sign(p - t) * scale
-// and per-block partial sums; a second single-block pass adds the partials in
-// a fixed order (deterministic loss).
+// and per-block partial sums (compensated float sums over a grid of a few
+// blocks per SM); a second single-block pass adds the partials in a fixed
+// order (reproducible loss).
 #include "drp_common.cuh"
 #include "drp_internal.h"
 
 namespace drp {
 
 constexpr int kLossThreads = 256;
-constexpr int kLossItems = 8;  // elements per thread per block pass
+constexpr int kLossBlocksPerSM = 8;
 
+// Kahan step: s + x with the lost low part carried in c.
+__device__ inline void kahan_add(float& s, float& c, float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+__device__ inline float l1_grad(float d, float scale) { return d > 0.0f ? scale : (d < 0.0f ? -scale : 0.0f); }
+
+// Grid-stride pass over float4 groups (scalar head/tail when the three
+// pointers are not 16-byte aligned alike); one partial per block.  The grid is
+// fixed per device, so the summation order -- and the loss -- is reproducible.
 __global__ void __launch_bounds__(kLossThreads) l1_partial_kernel(const float* p, const float* t, long long n,
                                                                   float scale, float* grad, float* partial) {
     __shared__ float warp_sum[kLossThreads / 32];
-    const long long base = (long long)blockIdx.x * kLossThreads * kLossItems;
-    float s = 0.0f;
-#pragma unroll
-    for (int k = 0; k < kLossItems; ++k) {
-        const long long i = base + (long long)k * kLossThreads + threadIdx.x;
-        if (i < n) {
-            const float d = p[i] - t[i];
-            s += fabsf(d);
-            grad[i] = d > 0.0f ? scale : (d < 0.0f ? -scale : 0.0f);
+    const long long stride = (long long)gridDim.x * kLossThreads;
+    const long long tid = (long long)blockIdx.x * kLossThreads + threadIdx.x;
+    float s = 0.0f, c = 0.0f;
+    const bool vec = ((reinterpret_cast<uintptr_t>(p) | reinterpret_cast<uintptr_t>(t) |
+                       reinterpret_cast<uintptr_t>(grad)) & 15) == 0;
+    long long done = 0;
+    if (vec) {
+        const long long n4 = n >> 2;
+        const float4* p4 = reinterpret_cast<const float4*>(p);
+        const float4* t4 = reinterpret_cast<const float4*>(t);
+        float4* g4 = reinterpret_cast<float4*>(grad);
+        for (long long i = tid; i < n4; i += stride) {
+            const float4 a = p4[i], b = t4[i];
+            const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z, dw = a.w - b.w;
+            kahan_add(s, c, (fabsf(dx) + fabsf(dy)) + (fabsf(dz) + fabsf(dw)));
+            g4[i] = make_float4(l1_grad(dx, scale), l1_grad(dy, scale), l1_grad(dz, scale), l1_grad(dw, scale));
         }
+        done = n4 << 2;
+    }
+    for (long long i = done + tid; i < n; i += stride) {
+        const float d = p[i] - t[i];
+        kahan_add(s, c, fabsf(d));
+        grad[i] = l1_grad(d, scale);
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
@@ -53,6 +80,21 @@ __global__ void __launch_bounds__(1024) l1_final_kernel(const float* partial, lo
     }
 }
 
+// Blocks for n elements: enough to fill every SM, never more than one
+// float4 group per thread.
+static long long l1_blocks(long long n) {
+    static int max_blocks = 0;
+    if (max_blocks == 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) return 1;  // no device: callers fail at launch
+        max_blocks = sms * kLossBlocksPerSM;
+    }
+    const long long need = ((n + 3) / 4 + kLossThreads - 1) / kLossThreads;
+    return need < max_blocks ? (need > 0 ? need : 1) : max_blocks;
+}
+
 }  // namespace drp
 
 extern "C" __attribute__((visibility("default"))) int drp_l1_loss_workspace_size(long long n, size_t* bytes) {
@@ -60,8 +102,7 @@ extern "C" __attribute__((visibility("default"))) int drp_l1_loss_workspace_size
         drp_set_last_error("drp_l1_loss_workspace_size: bad arguments");
         return 1;
     }
-    const long long per = (long long)drp::kLossThreads * drp::kLossItems;
-    *bytes = (size_t)((n + per - 1) / per) * sizeof(float) + 256;
+    *bytes = (size_t)drp::l1_blocks(n) * sizeof(float) + 256;
     return 0;
 }
 
@@ -69,8 +110,7 @@ extern "C" __attribute__((visibility("default"))) int drp_l1_loss_fwd(void* work
                                                                       const float* pred, const float* target,
                                                                       long long n, float scale, float* loss,
                                                                       float* grad, void* stream) {
-    const long long per = (long long)drp::kLossThreads * drp::kLossItems;
-    const long long nblocks = (n + per - 1) / per;
+    const long long nblocks = drp::l1_blocks(n);
     if (n <= 0 || !pred || !target || !loss || !grad || !workspace ||
         workspace_bytes < (size_t)nblocks * sizeof(float) || nblocks > 0x7fffffffll) {
         drp_set_last_error("drp_l1_loss_fwd: bad arguments or workspace too small");

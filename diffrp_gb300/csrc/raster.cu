@@ -220,8 +220,8 @@ static void launch_bin(const RasterArgs& a, cudaStream_t s) {
     dim3 grid((unsigned)((a.max_view_tris + 255) / 256), (unsigned)a.B);
     setup_bin_kernel<TL, false><<<grid, 256, 0, s>>>(a);
     const long long n = (long long)a.B * a.tiles_x * a.tiles_y;
-    scan_tiles_kernel<<<1, 1024, 0, s>>>(a.ws.tile_count, a.ws.tile_offset, a.ws.tile_cursor, n,
-                                         reinterpret_cast<unsigned long long*>(a.ws.stats));
+    launch_tile_scan(a.ws.tile_count, a.ws.tile_offset, a.ws.tile_cursor, n, a.ws.chunk_sums,
+                     reinterpret_cast<unsigned long long*>(a.ws.stats), s);
     setup_bin_kernel<TL, true><<<grid, 256, 0, s>>>(a);
 }
 

@@ -5,6 +5,7 @@
 // the fine raster of one tile by one CTA.
 #pragma once
 #include "drp_common.cuh"
+#include "drp_internal.h"
 
 namespace drp {
 
@@ -467,44 +468,141 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
     }
 }
 
-// Exclusive scan of tile counts -> offsets (and cursors); total entries -> stats.
-static __global__ void __launch_bounds__(1024) scan_tiles_kernel(const uint32_t* counts, uint32_t* offsets,
-                                                          uint32_t* cursors, long long n,
-                                                          unsigned long long* total) {
-    __shared__ unsigned long long warp_sums[32];
-    const int tid = threadIdx.x;
-    const long long per = (n + blockDim.x - 1) / blockDim.x;
-    const long long lo = min(n, per * tid), hi = min(n, lo + per);
-    unsigned long long s = 0;
-    for (long long i = lo; i < hi; ++i) s += counts[i];
-    // block exclusive scan of s
-    unsigned long long x = s;
-    const int lane = tid & 31, warp = tid >> 5;
+// ---------------------------------------------------------------------------
+// Exclusive scan of per-tile list counts -> offsets (and cursors), total
+// entries -> stats (u64).  Chunks of kScanChunk tiles: one block per chunk,
+// 16 contiguous tiles per thread.  More than one chunk takes two launches:
+// chunk sums, then each block adds the sums of the chunks before it (at most
+// a few hundred values) and scans its own chunk.  No inter-block waiting.
+// ---------------------------------------------------------------------------
+
+// Block-wide inclusive scan of one u64 per thread (kScanThreads threads).
+__device__ inline unsigned long long scan_block_u64(unsigned long long x, unsigned long long* warp_sums,
+                                                    unsigned long long& block_total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
-        unsigned long long y = __shfl_up_sync(0xffffffffu, x, off);
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, off);
         if (lane >= off) x += y;
     }
     if (lane == 31) warp_sums[warp] = x;
     __syncthreads();
     if (warp == 0) {
-        unsigned long long v = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+        unsigned long long v = lane < kScanThreads / 32 ? warp_sums[lane] : 0;
 #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            unsigned long long y = __shfl_up_sync(0xffffffffu, v, off);
+        for (int off = 1; off < kScanThreads / 32; off <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, v, off);
             if (lane >= off) v += y;
         }
-        warp_sums[lane] = v;
+        if (lane < kScanThreads / 32) warp_sums[lane] = v;
     }
     __syncthreads();
-    unsigned long long base = (warp ? warp_sums[warp - 1] : 0) + x - s;
-    for (long long i = lo; i < hi; ++i) {
-        uint32_t o = (uint32_t)min(base, (unsigned long long)0xffffffffu);
-        offsets[i] = o;
-        cursors[i] = o;
-        base += counts[i];
+    block_total = warp_sums[kScanThreads / 32 - 1];
+    return (warp ? warp_sums[warp - 1] : 0) + x;
+}
+
+static __global__ void __launch_bounds__(kScanThreads) scan_chunk_sums_kernel(const uint32_t* counts, long long n,
+                                                                              unsigned long long* sums) {
+    __shared__ unsigned long long red[kScanThreads / 32];
+    const long long base = (long long)blockIdx.x * kScanChunk;
+    unsigned long long s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPerThread; ++k) {
+        const long long i = base + (long long)k * kScanThreads + threadIdx.x;
+        if (i < n) s += counts[i];
     }
-    if (tid == blockDim.x - 1) *total = base;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+#pragma unroll
+        for (int w = 0; w < kScanThreads / 32; ++w) t += red[w];
+        sums[blockIdx.x] = t;
+    }
+}
+
+// counts / offsets / cursors must be 16-byte aligned (workspace carve).
+static __global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(const uint32_t* counts, uint32_t* offsets,
+                                                                         uint32_t* cursors, long long n,
+                                                                         const unsigned long long* chunk_sums,
+                                                                         unsigned long long* total) {
+    __shared__ unsigned long long warp_sums[kScanThreads / 32];
+    __shared__ unsigned long long prefix_sh;
+    const long long b = blockIdx.x;
+    // Sum of the chunks before this one (fixed order per thread, then a tree).
+    unsigned long long p = 0;
+    for (long long j = threadIdx.x; j < b; j += kScanThreads) p += chunk_sums[j];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) p += __shfl_xor_sync(0xffffffffu, p, off);
+    if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = p;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+#pragma unroll
+        for (int w = 0; w < kScanThreads / 32; ++w) t += warp_sums[w];
+        prefix_sh = t;
+    }
+    __syncthreads();
+    const unsigned long long prefix = prefix_sh;
+
+    const long long lo = b * kScanChunk + (long long)threadIdx.x * kScanPerThread;
+    const bool full = lo + kScanPerThread <= n;
+    uint32_t c[kScanPerThread];
+    if (full) {
+        const uint4* src = reinterpret_cast<const uint4*>(counts + lo);
+#pragma unroll
+        for (int k = 0; k < kScanPerThread / 4; ++k) {
+            const uint4 v = src[k];
+            c[4 * k] = v.x;
+            c[4 * k + 1] = v.y;
+            c[4 * k + 2] = v.z;
+            c[4 * k + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanPerThread; ++k) c[k] = lo + k < n ? counts[lo + k] : 0u;
+    }
+    unsigned long long s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPerThread; ++k) s += c[k];
+    unsigned long long chunk_total;
+    __syncthreads();  // warp_sums reuse
+    unsigned long long run = prefix + scan_block_u64(s, warp_sums, chunk_total) - s;
+    uint32_t o[kScanPerThread];
+#pragma unroll
+    for (int k = 0; k < kScanPerThread; ++k) {
+        o[k] = (uint32_t)min(run, (unsigned long long)0xffffffffu);
+        run += c[k];
+    }
+    if (full) {
+        uint4* d0 = reinterpret_cast<uint4*>(offsets + lo);
+        uint4* d1 = reinterpret_cast<uint4*>(cursors + lo);
+#pragma unroll
+        for (int k = 0; k < kScanPerThread / 4; ++k) {
+            const uint4 v = make_uint4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+            d0[k] = v;
+            d1[k] = v;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanPerThread; ++k)
+            if (lo + k < n) {
+                offsets[lo + k] = o[k];
+                cursors[lo + k] = o[k];
+            }
+    }
+    if (b == gridDim.x - 1 && threadIdx.x == 0) *total = prefix + chunk_total;
+}
+
+// chunk_sums: scan_chunks(n) u64 of scratch (unused when n <= kScanChunk).
+static inline void launch_tile_scan(const uint32_t* counts, uint32_t* offsets, uint32_t* cursors, long long n,
+                                    unsigned long long* chunk_sums, unsigned long long* total, cudaStream_t s) {
+    const long long chunks = scan_chunks(n);
+    if (chunks <= 0) return;
+    if (chunks > 1) scan_chunk_sums_kernel<<<(unsigned)chunks, kScanThreads, 0, s>>>(counts, n, chunk_sums);
+    scan_tiles_kernel<<<(unsigned)chunks, kScanThreads, 0, s>>>(counts, offsets, cursors, n, chunk_sums, total);
 }
 
 }  // namespace drp

@@ -277,7 +277,10 @@ int drp_batch_workspace_size(long long total_prims, long long total_tiles, unsig
  * Forward of every item: rasterise (persistent CTAs over an (item, tile)
  * work queue), interpolate attr into colour (fused), antialias into out.
  * items / block maps are device copies.  nbr: per-mesh topology from
- * drp_antialias_topology at the mesh's triangle offset, or NULL.
+ * drp_antialias_topology at the mesh's triangle offset, or NULL.  out may be
+ * NULL: then only rast and colour are written (the antialias pass is
+ * skipped), which is how a backward without stored per-pixel buffers
+ * regenerates them.
  */
 int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
                       const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,

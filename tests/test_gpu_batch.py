@@ -16,12 +16,16 @@ from diffrp_gb300 import synthetic as S
 pytestmark = pytest.mark.gpu
 
 
-def _scene():
+SMALL_ITEMS = [(0, (48, 64)), (1, (32, 32)), (0, (40, 40)), (2, (24, 56)), (1, (64, 48))]
+# 8x8 tiles: 4875 + 1536 + 2764 tiles, more than two 4096-tile scan chunks
+LARGE_ITEMS = [(0, (520, 600)), (1, (384, 256)), (2, (700, 252))]
+
+
+def _scene(items=SMALL_ITEMS):
     rng = np.random.default_rng(0)
     meshes_np = [S.icosphere(2, 0.8), S.random_displaced_grid(9, seed=1, sigma=0.1), S.icosphere(1, 0.6)]
     chans = [8, 5, 3]
     attrs = [rng.uniform(0, 1, (len(v), c)).astype(np.float32) for (v, _), c in zip(meshes_np, chans)]
-    items = [(0, (48, 64)), (1, (32, 32)), (0, (40, 40)), (2, (24, 56)), (1, (64, 48))]
     views = []
     for k, (m, (H, W)) in enumerate(items):
         v, _ = meshes_np[m]
@@ -32,9 +36,9 @@ def _scene():
     return meshes_np, chans, attrs, items, views
 
 
-def _renderer(recompute=False, tile_log2=4, tpt=0):
+def _renderer(recompute=False, tile_log2=4, tpt=0, items=SMALL_ITEMS):
     from diffrp_gb300.batch import BatchRenderer
-    meshes_np, chans, attrs, items, views = _scene()
+    meshes_np, chans, attrs, items, views = _scene(items)
     meshes = [(torch.from_numpy(f).cuda(), len(v), c) for (v, f), c in zip(meshes_np, chans)]
     r = BatchRenderer(meshes, items, tile_log2=tile_log2, threads_per_tri=tpt, recompute=recompute)
     pos = r.pack_positions([torch.from_numpy(p).cuda() for p in views])
@@ -42,10 +46,11 @@ def _renderer(recompute=False, tile_log2=4, tpt=0):
     return r, pos, attr, (meshes_np, chans, attrs, items, views)
 
 
-@pytest.mark.parametrize("tile_log2,tpt", [(4, 0), (5, 0), (3, 4)])
-def test_batch_forward_matches_per_item_calls(cuda_lib, tile_log2, tpt):
+@pytest.mark.parametrize("tile_log2,tpt,items", [(4, 0, SMALL_ITEMS), (5, 0, SMALL_ITEMS), (3, 4, SMALL_ITEMS),
+                                                 (3, 0, LARGE_ITEMS)], ids=["t4", "t5", "t3p4", "t3_many_tiles"])
+def test_batch_forward_matches_per_item_calls(cuda_lib, tile_log2, tpt, items):
     from diffrp_gb300 import nvdr as dr
-    r, pos, attr, (meshes_np, chans, attrs, items, views) = _renderer(tile_log2=tile_log2, tpt=tpt)
+    r, pos, attr, (meshes_np, chans, attrs, items, views) = _renderer(tile_log2=tile_log2, tpt=tpt, items=items)
     rast, color, out = r.forward_buffers(pos, attr)
     rv = r.rast_views(rast)
     cv = r.images(color)
@@ -90,6 +95,16 @@ def test_batch_gradients_match_per_item_autograd(cuda_lib, recompute):
     for got, ref in [(pos_b.grad.cpu().numpy(), gp_ref), (attr_b.grad.cpu().numpy(), ga_ref)]:
         scale = max(np.abs(ref).max(), 1e-12)
         assert np.abs(got - ref).max() / scale <= 1e-4
+
+
+def test_batch_raster_only_forward(cuda_lib):
+    """A forward without an output buffer writes the same rast and colour as
+    the full forward (the antialias pass is skipped)."""
+    r, pos, attr, _ = _renderer()
+    rast, color, out = r.forward_buffers(pos, attr)
+    rast2, color2 = r._buffers()
+    r._forward_raw(pos, attr, rast2, color2, None)
+    assert torch.equal(rast, rast2) and torch.equal(color, color2)
 
 
 def test_batch_cuda_graph_replay(cuda_lib):

@@ -89,6 +89,28 @@ def test_list_overflow_fallback_exact(cuda_lib):
     np.testing.assert_array_equal(rast.cpu().numpy(), ref)
 
 
+def test_tile_scan_across_chunks(cuda_lib):
+    """More tiles than one scan chunk of 4096: 14 views of 300x260 with 8x8
+    tiles is 17556 tiles (five chunks, the last one ragged).  The image is
+    exact, no tile overflows its list, and the list total equals the sum of
+    the per-view totals (each view alone fits in one chunk)."""
+    res = (300, 260)
+    pos, tri = scenes.multi_view(2, n_views=14, res=res)
+    dr = _dr()
+    ctx = _ctx(tile_log2=3, validate=True)
+    rast, _ = dr.rasterize(ctx, _t(pos), _t(tri), res, grad_db=False)
+    total, err = ctx._read_stats_sync()
+    assert err & 2 == 0, "a tile list overflowed"
+    ref, _, _ = O.rasterize(pos, tri, res, grad_db=False)
+    np.testing.assert_array_equal(rast.cpu().numpy(), ref)
+    per_view = 0
+    for v in range(pos.shape[0]):
+        c = _ctx(tile_log2=3, validate=True)
+        dr.rasterize(c, _t(pos[v:v + 1]), _t(tri), res, grad_db=False)
+        per_view += c._read_stats_sync()[0]
+    assert total == per_view > 0
+
+
 def test_depth_peeling(cuda_lib):
     pos, tri = scenes.random_soup(120, seed=2)
     dr = _dr()
