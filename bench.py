@@ -115,8 +115,11 @@ class GraphedStep:
         torch.cuda.current_stream(dev).wait_stream(side)
         torch.cuda.synchronize(dev)
         self.graph = torch.cuda.CUDAGraph()
+        n0 = kernel_launches()
         with torch.cuda.graph(self.graph):
             self.loss = step(self.verts, self.attr)
+        # our kernels in one step, counted by the library as they are captured
+        self.launches_per_step = kernel_launches() - n0
         torch.cuda.synchronize(dev)
 
     def load(self, h_verts, h_attr):
@@ -154,13 +157,10 @@ class BatchStep:
         return loss
 
 
-# Kernel launches of ours per step: rasterize (setup, scan, fill, fine) = 4,
-# interpolate fwd/bwd = 2, antialias fwd/bwd = 2 + 2 triangle setups,
-# rasterize bwd = 1.
-LAUNCHES_PER_STEP = 11
-# Batching form per step: setup/count, scan, setup/fill, fine, AA setup, AA
-# forward; backward: AA setup, fused backward.
-BATCH_LAUNCHES_PER_STEP = 8
+def kernel_launches():
+    """Kernel launches libdiffrp_gb300 has enqueued (captures included)."""
+    from diffrp_gb300 import _ffi
+    return _ffi.kernel_launches()
 
 
 # ---------------------------------------------------------------------------
@@ -177,8 +177,10 @@ def _graph(fn, dev, warm=3):
     torch.cuda.current_stream(dev).wait_stream(side)
     torch.cuda.synchronize(dev)
     g = torch.cuda.CUDAGraph()
+    n0 = kernel_launches()
     with torch.cuda.graph(g):
         fn()
+    g.launches_per_step = kernel_launches() - n0
     torch.cuda.synchronize(dev)
     return g
 
@@ -336,16 +338,18 @@ def run_batched(dev, name, steps, warmup, plain=True, recompute=False, tune=True
 
     ms = timed(g.replay, steps)
     res["batched"] = {"value": wl.pixels / ms / 1e3, "unit": UNIT, "ms_per_step": ms,
-                      "launches_per_step": 13, "path": "batched, one CUDA graph"}
+                      "launches_per_step": g.launches_per_step, "path": "batched, one CUDA graph"}
     res["peak_memory_gb"] = torch.cuda.max_memory_allocated(dev) / 1e9
     if recompute:
         res["batched"]["recompute"] = True
     if plain:
         for _ in range(max(2, warmup)):
+            n0 = kernel_launches()
             wl.plain_step()
+            plain_launches = kernel_launches() - n0
         ms_p = timed(wl.plain_step, max(3, steps // 4))
         res["plain_eager"] = {"value": wl.pixels / ms_p / 1e3, "unit": UNIT, "ms_per_step": ms_p,
-                              "launches_per_step": LAUNCHES_PER_STEP * len(items)}
+                              "launches_per_step": plain_launches}
         try:
             gp = _graph(wl.plain_step, dev, warm=2)
             ms_g = timed(gp.replay, steps)
@@ -468,7 +472,9 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None, batc
         b_ga = torch.zeros_like(a_t).reshape(-1)
         flat_attr = a_t.reshape(-1)
         ops["batch_forward"] = lambda: batch._forward_raw(clip, flat_attr, b_rast, b_color, b_out)
-        ops["batch_backward"] = lambda: batch._backward_raw(clip, flat_attr, b_rast, b_color, b_g, b_gp, b_ga)
+        # the step's backward reuses the antialias records of its forward
+        ops["batch_backward"] = lambda: batch._backward_raw(clip, flat_attr, b_rast, b_color, b_g, b_gp, b_ga,
+                                                            batch._fwd_gen)
     P = H * W
     # Algorithmic bytes per launch: every input read once, every output written once.
     algo = {
@@ -478,9 +484,9 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None, batc
         "antialias_bwd": P * (4 * C + 4 * C + 16 + 4 * C) + V * 16,
         "interpolate_bwd": P * (4 * C + 16 + 16) + V * 4 * C * 2,
         "rasterize_bwd": P * (16 + 16) + V * 16 * 2,
-        # fused raster + interpolation (rast and colour written), antialias
-        # (colour read, output written)
-        "batch_forward": P * (16 + 4 * C + 4 * C + 4 * C) + V * (16 + 4 * C) + F * 12,
+        # outputs written once (rast, colour, antialiased output), vertex
+        # positions / attributes / triangles read once
+        "batch_forward": P * (16 + 4 * C + 4 * C) + V * (16 + 4 * C) + F * 12,
         # rast, colour and output gradient read once; vertex / attribute
         # gradients written once
         "batch_backward": P * (16 + 4 * C + 4 * C) + V * (16 + 4 * C) * 2 + F * 12,
@@ -608,6 +614,7 @@ def main():
                 "config": {"workload": desc[args.workload], "global_batch": res["items"] * world,
                            "parallelism": "replicas" if world > 1 else "single GPU",
                            "l2": "flushed between steps (256 MiB write outside the timed events)"},
+                "gpu_launches": res["batched"]["launches_per_step"] * args.steps,
                 "detail": res}))
         if world > 1:
             dist.destroy_process_group()
@@ -753,7 +760,9 @@ def main():
             "e2e_dropin": {"value": pix / (e2e_plain_ms / 1e3) / 1e6, "unit": UNIT,
                            "note": "end to end through the drop-in nvdr ops (graph), host buffers"},
             "clocks": clocks,
-            "gpu_launches": (BATCH_LAUNCHES_PER_STEP * 2 + LAUNCHES_PER_STEP * 3) * args.steps,
+            # timed regions: batched graph and its e2e (2x), drop-in graph, its e2e and eager (3x)
+            "gpu_launches": (batched.launches_per_step * 2 + graphed.launches_per_step * 3) * args.steps,
+            "launches_per_step": {"batched": batched.launches_per_step, "dropin": graphed.launches_per_step},
         }
         if not args.no_batched:
             line["batched_views64"] = run_batched(dev, "views64", steps=max(5, args.steps // 3), warmup=W_)

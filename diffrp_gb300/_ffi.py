@@ -67,6 +67,8 @@ def load():
             lib.drp_status_string.argtypes = [ctypes.c_int]
             lib.drp_last_error.restype = ctypes.c_char_p
             lib.drp_last_error.argtypes = []
+            lib.drp_kernel_launches.restype = ctypes.c_ulonglong
+            lib.drp_kernel_launches.argtypes = []
             if lib.drp_abi_version() != ABI_VERSION:
                 raise RuntimeError("libdiffrp_gb300 ABI %d != expected %d" % (lib.drp_abi_version(), ABI_VERSION))
             _lib = lib
@@ -87,3 +89,9 @@ def size_out(name, *args):
     out = ctypes.c_size_t(0)
     call(name, *args, ctypes.byref(out))
     return out.value
+
+
+def kernel_launches():
+    """Kernel launches the library has enqueued so far (graph captures count
+    each captured launch once)."""
+    return int(load().drp_kernel_launches())

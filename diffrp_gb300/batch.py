@@ -27,6 +27,8 @@ from . import nvdr
 
 __all__ = ["BatchRenderer"]
 
+REUSE_AA_RECORDS = 1  # DRP_BATCH_REUSE_AA_RECORDS
+
 
 class _Item(ctypes.Structure):
     _fields_ = [("pos_offset", ctypes.c_longlong), ("attr_offset", ctypes.c_longlong),
@@ -48,7 +50,7 @@ def _register():
         "drp_batch_block_maps": [P, I, P, P],
         "drp_batch_workspace_size": [LL, LL, ULL, ctypes.POINTER(ctypes.c_size_t)],
         "drp_batch_forward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, I, I, ULL, P, P, P, P],
-        "drp_batch_backward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, P, P, P, P, P, P],
+        "drp_batch_backward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, P, P, P, P, P, I, P],
     }
     for name, args in sigs.items():
         fn = getattr(lib, name)
@@ -127,6 +129,8 @@ class BatchRenderer:
         self._capacity = 0
         self._ws = None
         self.last_list_entries = 0
+        self._fwd_gen = 0  # bumped by every forward; the workspace's AA records belong to the latest
+        self._rec_ws = None  # the workspace buffer holding those records
 
     def set_raster_shape(self, tile_log2, threads_per_tri):
         """Change the fine-raster tile size / threads per primitive (re-plans;
@@ -171,6 +175,7 @@ class BatchRenderer:
         """out=None writes rast and colour only (no antialias pass)."""
         cap = self._capacity if self._capacity else 4 * self.total_prims + 4096
         optr = None if out is None else out.data_ptr()
+        self._fwd_gen += 1
         ws = self._workspace(cap)
         stream = torch.cuda.current_stream(self.device).cuda_stream
         args = (self._items_dev.data_ptr(), len(self.items), self._pmap.data_ptr(), self.prim_blocks,
@@ -190,15 +195,19 @@ class BatchRenderer:
                 ws = self._workspace(self._capacity)
                 _ffi.call("drp_batch_forward", ws.data_ptr(), ws.numel(), *args, self._capacity, rast.data_ptr(),
                           color.data_ptr(), optr, stream)
+        self._rec_ws = ws
 
-    def _backward_raw(self, pos, attr, rast, color, grad_out, grad_pos, grad_attr):
-        ws = self._workspace(self._capacity)
+    def _backward_raw(self, pos, attr, rast, color, grad_out, grad_pos, grad_attr, gen=None):
+        """gen: the forward generation that produced rast / colour from pos;
+        when it is still the latest, its antialias records are reused."""
+        ws = self._workspace(0)  # the backward reads no tile list
         stream = torch.cuda.current_stream(self.device).cuda_stream
+        flags = REUSE_AA_RECORDS if gen is not None and gen == self._fwd_gen and ws is self._rec_ws else 0
         _ffi.call("drp_batch_backward", ws.data_ptr(), ws.numel(), self._items_dev.data_ptr(), len(self.items),
                   self._pmap.data_ptr(), self.prim_blocks, self._xmap.data_ptr(), self.pixel_blocks,
                   self.total_prims, self.total_tiles, pos.data_ptr(), self.tri.data_ptr(), attr.data_ptr(),
                   self.nbr.data_ptr(), rast.data_ptr(), color.data_ptr(), grad_out.data_ptr(), grad_pos.data_ptr(),
-                  grad_attr.data_ptr(), stream)
+                  grad_attr.data_ptr(), flags, stream)
 
     def _buffers(self):
         rast = torch.empty((self.total_pixels, 4), dtype=torch.float32, device=self.device)
@@ -229,6 +238,7 @@ class _BatchFn(torch.autograd.Function):
         out = torch.empty_like(color)
         renderer._forward_raw(pos, attr, rast, color, out)
         ctx.renderer = renderer
+        ctx.gen = renderer._fwd_gen
         if renderer.recompute:
             ctx.save_for_backward(pos, attr)
         else:
@@ -242,9 +252,11 @@ class _BatchFn(torch.autograd.Function):
             pos, attr = ctx.saved_tensors
             rast, color = r._buffers()
             r._forward_raw(pos, attr, rast, color, None)
+            gen = r._fwd_gen
         else:
             pos, attr, rast, color = ctx.saved_tensors
+            gen = ctx.gen
         grad_pos = torch.zeros_like(pos)
         grad_attr = torch.zeros_like(attr)
-        r._backward_raw(pos, attr, rast, color, grad_out.contiguous(), grad_pos, grad_attr)
+        r._backward_raw(pos, attr, rast, color, grad_out.contiguous(), grad_pos, grad_attr, gen)
         return grad_pos, grad_attr, None

@@ -96,10 +96,14 @@ __device__ __forceinline__ void aa_pair(const float4* rec, long long F, int A, i
     else Fp = cA < cB ? A : Bp;
     const int Op = (Fp == A) ? Bp : A;
     const int T = (Fp == A) ? cA : cB;
-    const float4 q0 = rec[2 * (long long)T], q1 = rec[2 * (long long)T + 1];
+    const float4 q1 = rec[2 * (long long)T + 1];
     const float sgn = q1.z;
-    if (sgn == 0.0f) return;
     const unsigned mask = __float_as_uint(q1.w);
+    // A triangle without a silhouette edge never blends: its exit edge, if
+    // any, fails the mask test below.  Inside a closed mesh that is almost
+    // every pair, so stop before the edge functions.
+    if (sgn == 0.0f || mask == 0u) return;
+    const float4 q0 = rec[2 * (long long)T];
     R.s[0] = make_float2(q0.x, q0.y);
     R.s[1] = make_float2(q0.z, q0.w);
     R.s[2] = make_float2(q1.x, q1.y);
@@ -160,13 +164,46 @@ __device__ __forceinline__ bool pair_slot(int q, int pix, int px, int py, int W,
     }
 }
 
+// Copy C floats (128-bit groups when C % 4 == 0 and both ends are 16-byte
+// aligned); up to four groups are loaded before the first store.
+__device__ __forceinline__ void copy_channels(const float* src, float* dst, int C) {
+    if ((C & 3) == 0 && (((uintptr_t)src | (uintptr_t)dst) & 15) == 0) {
+        const float4* s4 = reinterpret_cast<const float4*>(src);
+        float4* d4 = reinterpret_cast<float4*>(dst);
+        const int G = C >> 2;
+        for (int g0 = 0; g0 < G; g0 += 4) {
+            float4 v[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (g0 + k < G) v[k] = s4[g0 + k];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (g0 + k < G) d4[g0 + k] = v[k];
+        }
+    } else {
+        for (int c = 0; c < C; ++c) dst[c] = src[c];
+    }
+}
+
 // Forward of one pixel: out = c + sum over pair slots targeting this pixel of
 // w (c[src] - c), in slot order (fmaf).  R, Cc: the view's rast and colour.
+// COPY = false: o already holds c (the caller wrote it), so pixels without a
+// blend are left untouched.  The pixel's and its four neighbours' rast rows
+// are loaded together, before any of them is used.
+template <bool COPY>
 __device__ __forceinline__ void aa_fwd_pixel(const float4* R, const float* Cc, const float4* rec, long long F, int W,
                                              int H, int C, int pix, float* o) {
     const int py = pix / W, px = pix - py * W;
     const float* cs = Cc + (long long)pix * C;
+    int A[4], B[4], ax[4], ay[4];
+    bool vert[4], has[4];
+    float4 rn[4];
     const float4 rs = R[pix];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        has[q] = pair_slot(q, pix, px, py, W, H, A[q], B[q], ax[q], ay[q], vert[q]);
+        if (has[q]) rn[q] = R[A[q] == pix ? B[q] : A[q]];
+    }
     int src[4];
     float wt[4];
     bool any = false;
@@ -174,14 +211,10 @@ __device__ __forceinline__ void aa_fwd_pixel(const float4* R, const float* Cc, c
     for (int q = 0; q < 4; ++q) {
         src[q] = -1;
         wt[q] = 0.f;
-        int A, B, ax, ay;
-        bool vert;
-        if (!pair_slot(q, pix, px, py, W, H, A, B, ax, ay, vert)) continue;
-        const int other = A == pix ? B : A;
-        const float4 ro = R[other];
-        if (ro.w == rs.w) continue;
+        if (!has[q] || rn[q].w == rs.w) continue;
         AAPair pr;
-        aa_pair(rec, F, A, B, ax, ay, vert, A == pix ? rs : ro, A == pix ? ro : rs, pr);
+        const bool first = A[q] == pix;
+        aa_pair(rec, F, A[q], B[q], ax[q], ay[q], vert[q], first ? rs : rn[q], first ? rn[q] : rs, pr);
         if (pr.valid && pr.target == pix) {
             src[q] = pr.src;
             wt[q] = pr.w;
@@ -189,19 +222,15 @@ __device__ __forceinline__ void aa_fwd_pixel(const float4* R, const float* Cc, c
         }
     }
     if (!any) {
-        if ((C & 3) == 0 && (((uintptr_t)cs | (uintptr_t)o) & 15) == 0) {
-            for (int c = 0; c < C; c += 4)
-                *reinterpret_cast<float4*>(o + c) = *reinterpret_cast<const float4*>(cs + c);
-        } else {
-            for (int c = 0; c < C; ++c) o[c] = cs[c];
-        }
+        if (COPY) copy_channels(cs, o, C);
         return;
     }
     for (int c = 0; c < C; ++c) {
-        float v = cs[c];
+        const float base = cs[c];
+        float v = base;
 #pragma unroll
         for (int q = 0; q < 4; ++q)
-            if (src[q] >= 0) v = fmaf(wt[q], Cc[(long long)src[q] * C + c] - cs[c], v);
+            if (src[q] >= 0) v = fmaf(wt[q], Cc[(long long)src[q] * C + c] - base, v);
         o[c] = v;
     }
 }
@@ -220,21 +249,27 @@ __device__ __forceinline__ void aa_bwd_terms(const float4* R, const float* Cc, c
                                              long long F, int W, int H, int C, const float4* P, const int* tri,
                                              float4* GP, float boost, int pix, AATerms& at) {
     const int py = pix / W, px = pix - py * W;
+    int As[4], Bs[4], axs[4], ays[4];
+    bool verts[4], has[4];
+    float4 rn[4];
     const float4 rs = R[pix];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        has[q] = pair_slot(q, pix, px, py, W, H, As[q], Bs[q], axs[q], ays[q], verts[q]);
+        if (has[q]) rn[q] = R[As[q] == pix ? Bs[q] : As[q]];
+    }
     at.any = false;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         at.role[q] = 0;
         at.tgt[q] = 0;
         at.wt[q] = 0.f;
-        int A, B, ax, ay;
-        bool vert;
-        if (!pair_slot(q, pix, px, py, W, H, A, B, ax, ay, vert)) continue;
-        const int other = A == pix ? B : A;
-        const float4 ro = R[other];
+        if (!has[q]) continue;
+        const int A = As[q], B = Bs[q];
+        const float4 ro = rn[q];
         if (ro.w == rs.w) continue;
         AAPair p;
-        aa_pair(rec, F, A, B, ax, ay, vert, A == pix ? rs : ro, A == pix ? ro : rs, p);
+        aa_pair(rec, F, A, B, axs[q], ays[q], verts[q], A == pix ? rs : ro, A == pix ? ro : rs, p);
         if (!p.valid) continue;
         at.role[q] = p.target == pix ? 1 : 2;
         at.tgt[q] = p.target;

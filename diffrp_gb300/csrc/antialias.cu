@@ -112,7 +112,9 @@ int launch_topology(const int* tri, long long F, void* ws, size_t ws_bytes, int*
     cudaMemsetAsync(cnt, 0, cap * sizeof(unsigned), s);
     const long long n = 3 * F;
     topo_insert_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(tri, F, keys, cnt, slots, cap - 1);
+    drp_note_launch();
     topo_resolve_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(tri, F, keys, cnt, slots, cap - 1, nbr);
+    drp_note_launch();
     return 0;
 }
 
@@ -133,7 +135,7 @@ __global__ void __launch_bounds__(256) aa_fwd_kernel(AAArgs a) {
     const float4* R = reinterpret_cast<const float4*>(a.rast) + (long long)b * npix;
     const float* Cc = a.color + (long long)b * npix * a.C;
     const float4* rec = reinterpret_cast<const float4*>(a.tri_rec) + (long long)b * a.num_triangles * 2;
-    aa_fwd_pixel(R, Cc, rec, a.num_triangles, a.W, a.H, a.C, pix, a.out + ((long long)b * npix + pix) * a.C);
+    aa_fwd_pixel<true>(R, Cc, rec, a.num_triangles, a.W, a.H, a.C, pix, a.out + ((long long)b * npix + pix) * a.C);
 }
 
 __global__ void __launch_bounds__(256) aa_bwd_kernel(AAArgs a) {
@@ -170,6 +172,7 @@ static void launch_aa_setup(const AAArgs& a, cudaStream_t s) {
     if (a.num_triangles <= 0) return;
     dim3 grid((unsigned)((a.num_triangles + 255) / 256), (unsigned)a.B);
     aa_setup_kernel<<<grid, 256, 0, s>>>(a);
+    drp_note_launch();
 }
 
 int launch_aa_fwd(const AAArgs& a, cudaStream_t s) {
@@ -178,6 +181,7 @@ int launch_aa_fwd(const AAArgs& a, cudaStream_t s) {
     launch_aa_setup(a, s);
     dim3 grid((unsigned)((npix + 255) / 256), (unsigned)a.B);
     aa_fwd_kernel<<<grid, 256, 0, s>>>(a);
+    drp_note_launch();
     return 0;
 }
 
@@ -187,6 +191,7 @@ int launch_aa_bwd(const AAArgs& a, cudaStream_t s) {
     launch_aa_setup(a, s);
     dim3 grid((unsigned)((npix + 255) / 256), (unsigned)a.B);
     aa_bwd_kernel<<<grid, 256, 0, s>>>(a);
+    drp_note_launch();
     return 0;
 }
 

@@ -83,31 +83,47 @@ __global__ void __launch_bounds__(256) batch_setup_bin_kernel(BatchArgs a) {
             rec[2] = make_int4(0, 0, 0, 0);
         }
     }
-    if (FILL)
+    if (FILL) {
         bin_box<TILE_LOG2>(bx, live, it.tiles_x, a.tile_cursor + it.tile_offset, a.tile_list, a.list_capacity,
                            (uint32_t)pidx);
-    else
+    } else {
+        // The antialias triangle record rides along with the count pass (same
+        // triangle, same vertices).
+        aa_tri_record(reinterpret_cast<const float4*>(a.pos) + it.pos_offset, a.tri + 3 * (long long)it.tri_first,
+                      a.nbr ? a.nbr + 3 * (long long)it.tri_first : nullptr, j, it.tri_count, it.num_vertices,
+                      it.width, it.height, a.aa_rec + pidx * 2);
         bin_box<TILE_LOG2>(bx, live, it.tiles_x, a.tile_count + it.tile_offset, nullptr, 0, 0);
+    }
 }
 
 // rast + interpolated attributes of one pixel (interpolator.py:45 order).
+// The colour also goes to out (when not null): the antialias pass then only
+// rewrites the pixels it blends.
 struct BatchEmit {
     const float4* P;
     const int* tri;  // the item's mesh triangles (local vertex indices)
     const float* A;  // the item's mesh attributes
     int W, H, C;
-    bool vec;  // 128-bit attribute / colour access: C % 4 == 0 and both bases 16-byte aligned
+    bool vec;  // 128-bit attribute / colour / output access: C % 4 == 0 and all bases 16-byte aligned
     float4* rast;
     float* color;
+    float* out;
     __device__ __forceinline__ void operator()(int px, int py, unsigned long long k, float X, float Y) const {
         const long long o = (long long)py * W + px;
         float* col = color + o * C;
+        float* oc = out ? out + o * C : nullptr;
         if (k == ~0ull) {
             rast[o] = make_float4(0.f, 0.f, 0.f, 0.f);
             if (vec) {
-                for (int c = 0; c < C; c += 4) *reinterpret_cast<float4*>(col + c) = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int c = 0; c < C; c += 4) {
+                    *reinterpret_cast<float4*>(col + c) = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (oc) *reinterpret_cast<float4*>(oc + c) = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
             } else {
-                for (int c = 0; c < C; ++c) col[c] = 0.f;
+                for (int c = 0; c < C; ++c) {
+                    col[c] = 0.f;
+                    if (oc) oc[c] = 0.f;
+                }
             }
             return;
         }
@@ -130,9 +146,14 @@ struct BatchEmit {
                 o.z = fmaf(x0.z - x2.z, S.u, fmaf(x1.z - x2.z, S.v, x2.z));
                 o.w = fmaf(x0.w - x2.w, S.u, fmaf(x1.w - x2.w, S.v, x2.w));
                 *reinterpret_cast<float4*>(col + c) = o;
+                if (oc) *reinterpret_cast<float4*>(oc + c) = o;
             }
         } else {
-            for (int c = 0; c < C; ++c) col[c] = fmaf(a0[c] - a2[c], S.u, fmaf(a1[c] - a2[c], S.v, a2[c]));
+            for (int c = 0; c < C; ++c) {
+                const float v = fmaf(a0[c] - a2[c], S.u, fmaf(a1[c] - a2[c], S.v, a2[c]));
+                col[c] = v;
+                if (oc) oc[c] = v;
+            }
         }
     }
 };
@@ -190,7 +211,9 @@ batch_fine_kernel(BatchArgs a) {
         e.C = it.channels;
         e.rast = reinterpret_cast<float4*>(a.rast) + it.pixel_offset;
         e.color = a.color + it.image_offset;
-        e.vec = (it.channels & 3) == 0 && ((reinterpret_cast<uintptr_t>(e.A) | reinterpret_cast<uintptr_t>(e.color)) & 15) == 0;
+        e.out = a.out ? a.out + it.image_offset : nullptr;
+        e.vec = (it.channels & 3) == 0 && ((reinterpret_cast<uintptr_t>(e.A) | reinterpret_cast<uintptr_t>(e.color) |
+                                            reinterpret_cast<uintptr_t>(e.out)) & 15) == 0;
         fine_tile<TILE_LOG2, TPT>(ft, e);
     }
 }
@@ -211,8 +234,9 @@ __global__ void __launch_bounds__(256) batch_aa_fwd_kernel(BatchArgs a) {
     const int pix = blk.y * 256 + threadIdx.x;
     if (pix >= it.width * it.height) return;
     const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
-    aa_fwd_pixel(R, a.color + it.image_offset, a.aa_rec + it.prim_offset * 2, it.tri_count, it.width, it.height,
-                 it.channels, pix, a.out + it.image_offset + (long long)pix * it.channels);
+    // out already holds the colour (written by the fine raster): only blended pixels change
+    aa_fwd_pixel<false>(R, a.color + it.image_offset, a.aa_rec + it.prim_offset * 2, it.tri_count, it.width,
+                        it.height, it.channels, pix, a.out + it.image_offset + (long long)pix * it.channels);
 }
 
 // Fused backward of one pixel: antialias colour gradient -> interpolation
@@ -248,31 +272,36 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
     float gu = 0.f, gv = 0.f;
     const bool vec = (C & 3) == 0 && ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(GA) |
                                        reinterpret_cast<uintptr_t>(Gd)) & 15) == 0;
+    // Channel groups of 4: the next group's loads are issued before this
+    // group's reduction and atomics, which would otherwise hold them back.
+    float g[4], x0[4], x1[4], x2[4];
+    auto load_group = [&](int c0) {
+        if (vec) {
+            const float4 gq = __ldg(reinterpret_cast<const float4*>(Gd + (long long)pix * C + c0));
+            const float4 q0 = __ldg(reinterpret_cast<const float4*>(A + (long long)i0 * C + c0));
+            const float4 q1 = __ldg(reinterpret_cast<const float4*>(A + (long long)i1 * C + c0));
+            const float4 q2 = __ldg(reinterpret_cast<const float4*>(A + (long long)i2 * C + c0));
+            g[0] = gq.x; g[1] = gq.y; g[2] = gq.z; g[3] = gq.w;
+            x0[0] = q0.x; x0[1] = q0.y; x0[2] = q0.z; x0[3] = q0.w;
+            x1[0] = q1.x; x1[1] = q1.y; x1[2] = q1.z; x1[3] = q1.w;
+            x2[0] = q2.x; x2[1] = q2.y; x2[2] = q2.z; x2[3] = q2.w;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int c = c0 + k < C ? c0 + k : C - 1;
+                g[k] = c0 + k < C ? Gd[(long long)pix * C + c] : 0.f;
+                x0[k] = A[(long long)i0 * C + c];
+                x1[k] = A[(long long)i1 * C + c];
+                x2[k] = A[(long long)i2 * C + c];
+            }
+        }
+    };
+    if (t >= 0) load_group(0);
     for (int c0 = 0; c0 < C; c0 += 4) {
         float val[12];
 #pragma unroll
         for (int k = 0; k < 12; ++k) val[k] = 0.f;
         if (t >= 0) {
-            float g[4], x0[4], x1[4], x2[4];
-            if (vec) {
-                const float4 gq = *reinterpret_cast<const float4*>(Gd + (long long)pix * C + c0);
-                const float4 q0 = __ldg(reinterpret_cast<const float4*>(A + (long long)i0 * C + c0));
-                const float4 q1 = __ldg(reinterpret_cast<const float4*>(A + (long long)i1 * C + c0));
-                const float4 q2 = __ldg(reinterpret_cast<const float4*>(A + (long long)i2 * C + c0));
-                g[0] = gq.x; g[1] = gq.y; g[2] = gq.z; g[3] = gq.w;
-                x0[0] = q0.x; x0[1] = q0.y; x0[2] = q0.z; x0[3] = q0.w;
-                x1[0] = q1.x; x1[1] = q1.y; x1[2] = q1.z; x1[3] = q1.w;
-                x2[0] = q2.x; x2[1] = q2.y; x2[2] = q2.z; x2[3] = q2.w;
-            } else {
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const int c = c0 + k < C ? c0 + k : C - 1;
-                    g[k] = c0 + k < C ? Gd[(long long)pix * C + c] : 0.f;
-                    x0[k] = A[(long long)i0 * C + c];
-                    x1[k] = A[(long long)i1 * C + c];
-                    x2[k] = A[(long long)i2 * C + c];
-                }
-            }
             if (at.any) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
@@ -286,6 +315,7 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
                 gu = fmaf(g[k], x0[k] - x2[k], gu);
                 gv = fmaf(g[k], x1[k] - x2[k], gv);
             }
+            if (c0 + 4 < C) load_group(c0 + 4);
         }
         seg_reduce<12>(seg, val);
         if (t >= 0 && seg.head) {
@@ -347,9 +377,11 @@ BatchLayout batch_layout(long long total_prims, long long total_tiles, unsigned 
     L.offset = up(L.count + (size_t)total_tiles * 4);
     L.cursor = up(L.offset + (size_t)total_tiles * 4);
     L.chunks = up(L.cursor + (size_t)total_tiles * 4);
-    L.list = up(L.chunks + (size_t)scan_chunks(total_tiles) * 8);
-    L.aa = up(L.list + (size_t)cap * 4);
-    L.total = up(L.aa + (size_t)total_prims * 32);
+    // the antialias records sit before the list: their offset must not depend
+    // on the list capacity (the backward may reuse the forward's records)
+    L.aa = up(L.chunks + (size_t)scan_chunks(total_tiles) * 8);
+    L.list = up(L.aa + (size_t)total_prims * 32);
+    L.total = up(L.list + (size_t)cap * 4);
     return L;
 }
 
@@ -378,16 +410,21 @@ static void launch_batch_fine(const BatchArgs& a, cudaStream_t s) {
         grid = sms * (per > 0 ? per : 1);
     }
     const long long g = a.total_tiles < grid ? a.total_tiles : grid;
-    if (g > 0) batch_fine_kernel<TL, TPT><<<(unsigned)g, NT, 0, s>>>(a);
+    if (g > 0) {
+        batch_fine_kernel<TL, TPT><<<(unsigned)g, NT, 0, s>>>(a);
+        drp_note_launch();
+    }
 }
 
 template <int TL>
 static void launch_batch_raster(const BatchArgs& a, cudaStream_t s) {
     if (a.n_prim_blocks > 0) {
         batch_setup_bin_kernel<TL, false><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+        drp_note_launch();
         launch_tile_scan(a.tile_count, a.tile_offset, a.tile_cursor, a.total_tiles, a.chunk_sums,
                          reinterpret_cast<unsigned long long*>(a.stats), s);
         batch_setup_bin_kernel<TL, true><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+        drp_note_launch();
     } else {
         cudaMemsetAsync(a.tile_offset, 0, sizeof(uint32_t) * a.total_tiles, s);
     }
@@ -412,15 +449,24 @@ int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream
     default: launch_batch_raster<4>(a, s); break;
     }
     if (!a.out) return 0;  // raster + interpolation only (recomputing them for the backward)
-    if (a.n_prim_blocks > 0) batch_aa_setup_kernel<<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
-    if (a.n_pix_blocks > 0) batch_aa_fwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+    // (the antialias triangle records were written by the setup / count pass)
+    if (a.n_pix_blocks > 0) {
+        batch_aa_fwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+        drp_note_launch();
+    }
     return 0;
 }
 
-int launch_batch_backward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream_t s) {
+int launch_batch_backward(BatchArgs a, void* ws, const BatchLayout& L, bool reuse_records, cudaStream_t s) {
     carve(a, ws, L);
-    if (a.n_prim_blocks > 0) batch_aa_setup_kernel<<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
-    if (a.n_pix_blocks > 0) batch_bwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+    if (a.n_prim_blocks > 0 && !reuse_records) {
+        batch_aa_setup_kernel<<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+        drp_note_launch();
+    }
+    if (a.n_pix_blocks > 0) {
+        batch_bwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+        drp_note_launch();
+    }
     return 0;
 }
 
@@ -560,7 +606,7 @@ DRP_API int drp_batch_backward(void* workspace, size_t workspace_bytes, const dr
                                long long pixel_blocks, long long total_prims, long long total_tiles,
                                const float* pos, const int* tri, const float* attr, const int* nbr,
                                const float* rast, const float* color, const float* grad_out, float* grad_pos,
-                               float* grad_attr, void* stream) {
+                               float* grad_attr, int flags, void* stream) {
     drp::BatchArgs a;
     drp::BatchLayout L;
     int st = batch_common(workspace, workspace_bytes, items, num_items, prim_block_map, prim_blocks, pixel_block_map,
@@ -574,6 +620,8 @@ DRP_API int drp_batch_backward(void* workspace, size_t workspace_bytes, const dr
     a.grad_out = grad_out;
     a.grad_pos = grad_pos;
     a.grad_attr = grad_attr;
-    drp::launch_batch_backward(a, workspace, L, static_cast<cudaStream_t>(stream));
+    if (flags & ~DRP_BATCH_REUSE_AA_RECORDS) return bfail("batch: unknown flags");
+    drp::launch_batch_backward(a, workspace, L, (flags & DRP_BATCH_REUSE_AA_RECORDS) != 0,
+                               static_cast<cudaStream_t>(stream));
     return drp_check_launch("drp_batch_backward");
 }

@@ -1,6 +1,7 @@
 // capi.cu -- extern "C" entry points declared in include/diffrp_gb300.h.
 // Host-side validation (sizes, null pointers, alignment, workspace size) and
 // the launch of the kernels in raster.cu / interp.cu / antialias.cu.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -61,6 +62,14 @@ RasterLayout raster_layout(int B, long long maxT, int H, int W, int tile_log2, u
 void drp_set_last_error(const char* msg) { snprintf(g_last_error, sizeof(g_last_error), "%s", msg); }
 
 int drp_check_launch(const char* what) { return check_launch(what); }
+
+namespace {
+std::atomic<unsigned long long> g_kernel_launches{0};
+}
+
+void drp_note_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
+
+DRP_API unsigned long long drp_kernel_launches(void) { return g_kernel_launches.load(std::memory_order_relaxed); }
 
 DRP_API int drp_abi_version(void) { return DRP_ABI_VERSION; }
 

@@ -128,3 +128,5 @@ int launch_aa_bwd(const AAArgs& a, cudaStream_t s);
 void drp_set_last_error(const char* msg);
 // DRP_STATUS_OK, or DRP_STATUS_CUDA_ERROR with the message set, after a launch.
 int drp_check_launch(const char* what);
+// Count one kernel launch enqueued by this library (drp_kernel_launches).
+void drp_note_launch();

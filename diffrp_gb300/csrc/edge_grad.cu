@@ -118,5 +118,6 @@ extern "C" __attribute__((visibility("default"))) int drp_edge_gradient_bwd(
     a.out = reinterpret_cast<float2*>(grad_frag_xy);
     const int n = height * width;
     drp::edge_grad_bwd_kernel<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(a);
+    drp_note_launch();
     return drp_check_launch("drp_edge_gradient_bwd");
 }

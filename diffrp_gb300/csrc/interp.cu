@@ -241,6 +241,7 @@ int launch_interp_fwd(const InterpArgs& a, cudaStream_t s) {
     const long long n = (long long)a.B * a.H * a.W;
     if (n == 0) return 0;
     interp_fwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    drp_note_launch();
     return 0;
 }
 
@@ -248,18 +249,21 @@ int launch_interp_bwd(const InterpArgs& a, cudaStream_t s) {
     const long long n = (long long)a.B * a.H * a.W;
     if (n == 0) return 0;
     interp_bwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    drp_note_launch();
     return 0;
 }
 
 int launch_interp_sparse_fwd(const SparseInterpArgs& a, cudaStream_t s) {
     if (a.N == 0) return 0;
     interp_sparse_fwd_kernel<<<(unsigned)((a.N + 255) / 256), 256, 0, s>>>(a);
+    drp_note_launch();
     return 0;
 }
 
 int launch_interp_sparse_bwd(const SparseInterpArgs& a, cudaStream_t s) {
     if (a.N == 0) return 0;
     interp_sparse_bwd_kernel<<<(unsigned)((a.N + 255) / 256), 256, 0, s>>>(a);
+    drp_note_launch();
     return 0;
 }
 

@@ -119,6 +119,8 @@ extern "C" __attribute__((visibility("default"))) int drp_l1_loss_fwd(void* work
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     float* partial = static_cast<float*>(workspace);
     drp::l1_partial_kernel<<<(unsigned)nblocks, drp::kLossThreads, 0, s>>>(pred, target, n, scale, grad, partial);
+    drp_note_launch();
     drp::l1_final_kernel<<<1, 1024, 0, s>>>(partial, nblocks, scale, loss);
+    drp_note_launch();
     return drp_check_launch("drp_l1_loss_fwd");
 }

@@ -205,13 +205,13 @@ static void launch_fine(const RasterArgs& a, int tpt, cudaStream_t s) {
     constexpr int NT = (1 << (2 * TL)) < 256 ? (1 << (2 * TL)) : 256;
     dim3 grid((unsigned)(a.tiles_x * a.tiles_y), (unsigned)a.B);
     switch (tpt) {
-    case 0: fine_raster_kernel<TL, 0><<<grid, NT, 0, s>>>(a); break;
-    case 1: fine_raster_kernel<TL, 1><<<grid, NT, 0, s>>>(a); break;
-    case 2: fine_raster_kernel<TL, 2><<<grid, NT, 0, s>>>(a); break;
-    case 4: fine_raster_kernel<TL, 4><<<grid, NT, 0, s>>>(a); break;
-    case 8: fine_raster_kernel<TL, 8><<<grid, NT, 0, s>>>(a); break;
-    case 16: fine_raster_kernel<TL, 16><<<grid, NT, 0, s>>>(a); break;
-    default: fine_raster_kernel<TL, 32><<<grid, NT, 0, s>>>(a); break;
+    case 0: fine_raster_kernel<TL, 0><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
+    case 1: fine_raster_kernel<TL, 1><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
+    case 2: fine_raster_kernel<TL, 2><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
+    case 4: fine_raster_kernel<TL, 4><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
+    case 8: fine_raster_kernel<TL, 8><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
+    case 16: fine_raster_kernel<TL, 16><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
+    default: fine_raster_kernel<TL, 32><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
     }
 }
 
@@ -219,10 +219,12 @@ template <int TL>
 static void launch_bin(const RasterArgs& a, cudaStream_t s) {
     dim3 grid((unsigned)((a.max_view_tris + 255) / 256), (unsigned)a.B);
     setup_bin_kernel<TL, false><<<grid, 256, 0, s>>>(a);
+    drp_note_launch();
     const long long n = (long long)a.B * a.tiles_x * a.tiles_y;
     launch_tile_scan(a.ws.tile_count, a.ws.tile_offset, a.ws.tile_cursor, n, a.ws.chunk_sums,
                      reinterpret_cast<unsigned long long*>(a.ws.stats), s);
     setup_bin_kernel<TL, true><<<grid, 256, 0, s>>>(a);
+    drp_note_launch();
 }
 
 int launch_rasterize(const RasterArgs& a, cudaStream_t s) {
@@ -250,6 +252,7 @@ int launch_raster_bwd(const RasterBwdArgs& a, cudaStream_t s) {
     const long long n = (long long)a.B * a.H * a.W;
     if (n == 0) return 0;
     raster_bwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    drp_note_launch();
     return 0;
 }
 

@@ -291,18 +291,68 @@ __device__ __forceinline__ unsigned long long tile_prim_key(const float4& z4, in
     return ((unsigned long long)depth_order(z) << 32) | (unsigned long long)__float_as_uint(z4.w);
 }
 
-// Pixel q of thread tid inside a tile: warps own 8x4 pixel blocks (blocks
-// are numbered across the tile, then down), lanes are row-major inside the
-// block.  A warp can then skip a primitive whose bbox misses its block with
-// one uniform test.
+// Pixel q of thread tid inside a tile.  The tile is cut into 8x4 pixel
+// blocks, numbered row-major (T/8 per row); lanes are row-major inside a
+// block.  With one pixel per thread warp w owns block w; with four (32-pixel
+// tiles, 256 threads) warp w owns the 2x2 blocks of the 16x8 region at
+// ((w & 1) * 16, (w >> 1) * 8), q walking them row-major.  A warp can then
+// skip a primitive whose block mask misses its blocks with one uniform test.
+template <int TILE_LOG2, int NTHREADS>
+__device__ __forceinline__ int tile_block(int tid, int q) {
+    constexpr int T = 1 << TILE_LOG2;
+    constexpr int PPT = T * T / NTHREADS;
+    static_assert(PPT == 1 || (PPT == 4 && T == 32), "tile_pixel: unsupported tile shape");
+    const int w = tid >> 5;
+    if (PPT == 4) return ((((w >> 1) << 1) | (q >> 1)) * (T / 8)) + (((w & 1) << 1) | (q & 1));
+    return w + q * (NTHREADS >> 5);
+}
+
 template <int TILE_LOG2, int NTHREADS>
 __device__ __forceinline__ void tile_pixel(int tid, int q, int& dx, int& dy, int& bx, int& by) {
     constexpr int T = 1 << TILE_LOG2;
-    const int blk = (tid >> 5) + q * (NTHREADS >> 5);
+    const int blk = tile_block<TILE_LOG2, NTHREADS>(tid, q);
     bx = (blk % (T / 8)) * 8;
     by = (blk / (T / 8)) * 4;
     dx = bx + (tid & 7);
     dy = by + ((tid >> 3) & 3);
+}
+
+// Bit b set when the local bbox [x0, x1] x [y0, y1] overlaps 8x4 block b
+// (row-major, T/8 blocks per row; at most 32 blocks per tile).
+template <int T>
+__device__ __forceinline__ uint32_t block_mask(int x0, int x1, int y0, int y1) {
+    constexpr int CW = T / 8;
+    constexpr unsigned long long REP = CW == 4 ? 0x11111111ull : (CW == 2 ? 0x55ull : 0x3ull);
+    const unsigned long long cols = (2ull << (x1 >> 3)) - (1ull << (x0 >> 3));
+    const unsigned long long rows = (1ull << (((y1 >> 2) + 1) * CW)) - (1ull << ((y0 >> 2) * CW));
+    return (uint32_t)(cols * REP & rows);
+}
+
+// Clear the blocks of mask m (block_mask numbering) that lie wholly outside
+// one of the primitive's edges: the edge function is linear, so its largest
+// value over a block's pixels sits at a block corner.  BIG primitives keep
+// their bbox mask.  All terms stay below 2^30 in magnitude (prepare_tile_prim
+// only keeps 32-bit edges under that bound over the tile).
+template <int T>
+__device__ __forceinline__ uint32_t refine_block_mask(const TilePrim& tp, uint32_t m) {
+    if (tp.e2.y & TP_BIG) return m;
+    constexpr int CW = T / 8;
+    const int4 e0 = tp.e0, e1 = tp.e1, e2 = tp.e2;
+    const int A[3] = {e0.x, e0.w, e1.z}, B[3] = {e0.y, e1.x, e1.w}, C[3] = {e0.z, e1.y, e2.x};
+    uint32_t out = m;
+    for (uint32_t r = m; r; r &= r - 1u) {
+        const int b = __ffs(r) - 1;
+        const int bx = (b % CW) * 8, by = (b / CW) * 4;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int mx = C[k] + max(A[k] * bx, A[k] * (bx + 7)) + max(B[k] * by, B[k] * (by + 3));
+            if (mx < 0) {
+                out &= ~(1u << b);
+                break;
+            }
+        }
+    }
+    return out;
 }
 
 // One tile's work for the fine raster.
@@ -336,6 +386,7 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
     constexpr int GROUPS = TPT > 0 ? NTHREADS / TPT : 1;
     __shared__ unsigned long long keys[NPIX];
     __shared__ TilePrim prims[CHUNK];
+    __shared__ uint32_t pmask[CHUNK];  // 8x4 blocks each prepared primitive's bbox overlaps
     __shared__ int n_complex;
     __shared__ float col_ndc[T], row_ndc[T];
 
@@ -369,31 +420,46 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
         const int n = (int)min((long long)CHUNK, total - base);
         if (tid < n && tid < CHUNK) {
             const long long pidx = overflow ? pbase + base + tid : (long long)ft.list[base + tid];
-            prepare_tile_prim<T>(recs + pidx * 3, tx0, ty0, W, H, prims[tid]);
-            if (prims[tid].e2.y & TP_COMPLEX) atomicAdd(&n_complex, 1);
+            TilePrim& tp = prims[tid];
+            prepare_tile_prim<T>(recs + pidx * 3, tx0, ty0, W, H, tp);
+            const int fl = tp.e2.y;
+            if (fl & TP_COMPLEX) atomicAdd(&n_complex, 1);
+            uint32_t bm = 0u;
+            if (fl & TP_ACTIVE) {
+                bm = block_mask<T>(tp.v2b.z & 0xffff, tp.v2b.z >> 16, tp.v2b.w & 0xffff, tp.v2b.w >> 16);
+                if (TPT == 0) bm = refine_block_mask<T>(tp, bm);
+            }
+            pmask[tid] = bm;
         }
         __syncthreads();
         if (TPT == 0) {
-            for (int j = 0; j < n; ++j) {
-                const TilePrim& tp = prims[j];
-                const int4 e2 = tp.e2;
-                if (!(e2.y & TP_ACTIVE)) continue;
-                const int4 e0 = tp.e0, e1 = tp.e1, v2b = tp.v2b;
-                const int x0 = v2b.z & 0xffff, x1 = v2b.z >> 16, y0 = v2b.w & 0xffff, y1 = v2b.w >> 16;
-                // 8x4 blocks overlapped by the primitive's bbox: columns c0..c1, rows r0..r1
-                const int c0 = x0 >> 3, c1 = x1 >> 3, r0 = y0 >> 2, r1 = y1 >> 2;
+            // Each warp ballots the primitives whose block mask meets its own
+            // blocks, then walks only those (warp-uniform loop).
+            const int lane = tid & 31;
+            uint32_t wbits = 0;
 #pragma unroll
-                for (int q = 0; q < PPT; ++q) {
-                    int dx, dy, bx, by;
-                    tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
-                    const int bc = bx >> 3, br = by >> 2;
-                    if (bc < c0 || bc > c1 || br < r0 || br > r1) continue;  // warp-uniform
-                    const int sx = (tx0 + dx) * DRP_SUBPIX + DRP_HALF_SUBPIX;
-                    const int sy = (ty0 + dy) * DRP_SUBPIX + DRP_HALF_SUBPIX;
-                    if (!tile_prim_covers(tp, e0, e1, e2, dx, dy, sx, sy)) continue;
-                    bool ok;
-                    const unsigned long long k = tile_prim_key(tp.z, e2.z, e2.w, sx, sy, ok);
-                    if (ok && k < best[q] && (!prev_g || k > prevk[q])) best[q] = k;
+            for (int q = 0; q < PPT; ++q) wbits |= 1u << tile_block<TILE_LOG2, NTHREADS>(tid, q);
+            for (int j0 = 0; j0 < n; j0 += 32) {
+                const uint32_t pm = j0 + lane < n ? pmask[j0 + lane] : 0u;
+                uint32_t hits = __ballot_sync(0xffffffffu, (pm & wbits) != 0u);
+                while (hits) {
+                    const int b = __ffs(hits) - 1;
+                    hits &= hits - 1;
+                    const uint32_t mj = __shfl_sync(0xffffffffu, pm, b);
+                    const TilePrim& tp = prims[j0 + b];
+                    const int4 e0 = tp.e0, e1 = tp.e1, e2 = tp.e2;
+#pragma unroll
+                    for (int q = 0; q < PPT; ++q) {
+                        if (!((mj >> tile_block<TILE_LOG2, NTHREADS>(tid, q)) & 1u)) continue;  // warp-uniform
+                        int dx, dy, bx, by;
+                        tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+                        const int sx = (tx0 + dx) * DRP_SUBPIX + DRP_HALF_SUBPIX;
+                        const int sy = (ty0 + dy) * DRP_SUBPIX + DRP_HALF_SUBPIX;
+                        if (!tile_prim_covers(tp, e0, e1, e2, dx, dy, sx, sy)) continue;
+                        bool ok;
+                        const unsigned long long k = tile_prim_key(tp.z, e2.z, e2.w, sx, sy, ok);
+                        if (ok && k < best[q] && (!prev_g || k > prevk[q])) best[q] = k;
+                    }
                 }
             }
         } else {
@@ -423,6 +489,18 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
         __syncthreads();
     }
     if (TPT == 0) {
+        if (n_complex == 0) {
+            // Every key is final and in this thread's registers: emit at once.
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) {
+                int dx, dy, bx, by;
+                tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+                const int px = tx0 + dx, py = ty0 + dy;
+                if (px >= W || py >= H) continue;
+                emit(px, py, best[q], col_ndc[dx], row_ndc[dy]);
+            }
+            return;
+        }
 #pragma unroll
         for (int q = 0; q < PPT; ++q) {
             int dx, dy, bx, by;
@@ -601,8 +679,12 @@ static inline void launch_tile_scan(const uint32_t* counts, uint32_t* offsets, u
                                     unsigned long long* chunk_sums, unsigned long long* total, cudaStream_t s) {
     const long long chunks = scan_chunks(n);
     if (chunks <= 0) return;
-    if (chunks > 1) scan_chunk_sums_kernel<<<(unsigned)chunks, kScanThreads, 0, s>>>(counts, n, chunk_sums);
+    if (chunks > 1) {
+        scan_chunk_sums_kernel<<<(unsigned)chunks, kScanThreads, 0, s>>>(counts, n, chunk_sums);
+        drp_note_launch();
+    }
     scan_tiles_kernel<<<(unsigned)chunks, kScanThreads, 0, s>>>(counts, offsets, cursors, n, chunk_sums, total);
+    drp_note_launch();
 }
 
 }  // namespace drp

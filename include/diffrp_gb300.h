@@ -53,6 +53,12 @@ int drp_abi_version(void);
 const char* drp_status_string(int status);
 const char* drp_last_error(void);
 
+/* Kernel launches this library has enqueued since it was loaded, all threads
+ * and streams (launches recorded into a CUDA graph count once, at capture).
+ * No counterpart in the reference: a diagnostic for counting the kernels of a
+ * step. */
+unsigned long long drp_kernel_launches(void);
+
 /* ------------------------------------------------------------------------ */
 /* Rasterisation                                                             */
 /* ------------------------------------------------------------------------ */
@@ -288,13 +294,19 @@ int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp_batch_i
                       const int* tri, const float* attr, const int* nbr, int tile_log2, int threads_per_tri,
                       unsigned long long list_capacity, float* rast, float* color, float* out, void* stream);
 
+/* drp_batch_backward flag: the workspace still holds the antialias triangle
+ * records of the last drp_batch_forward, which ran on the same positions
+ * (nothing else used the workspace since): they are not recomputed. */
+#define DRP_BATCH_REUSE_AA_RECORDS 1
+
 /* Fused backward: grad_out (image floats) -> grad_pos (accumulated, pos
- * layout) and grad_attr (accumulated, attr layout). */
+ * layout) and grad_attr (accumulated, attr layout).  flags: 0 or
+ * DRP_BATCH_REUSE_AA_RECORDS. */
 int drp_batch_backward(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
                        const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
                        long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
                        const int* tri, const float* attr, const int* nbr, const float* rast, const float* color,
-                       const float* grad_out, float* grad_pos, float* grad_attr, void* stream);
+                       const float* grad_out, float* grad_pos, float* grad_attr, int flags, void* stream);
 
 #ifdef __cplusplus
 }

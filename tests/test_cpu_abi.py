@@ -41,6 +41,15 @@ def test_abi_version_and_status_strings(lib):
     assert lib.drp_status_string(1) == b"invalid argument"
 
 
+def test_kernel_launch_counter_ignores_rejected_calls(lib):
+    """Calls the host-side validation rejects launch nothing."""
+    from diffrp_gb300 import _ffi
+    before = _ffi.kernel_launches()
+    with pytest.raises(RuntimeError):
+        _ffi.call("drp_l1_loss_fwd", None, 0, None, None, 0, ctypes.c_float(1.0), None, None, None)
+    assert _ffi.kernel_launches() == before
+
+
 def test_workspace_queries_and_validation(lib):
     from diffrp_gb300 import _ffi
     n = _ffi.size_out("drp_raster_workspace_size", 2, 1000, 512, 512, 4, 10000)

@@ -97,6 +97,25 @@ def test_batch_gradients_match_per_item_autograd(cuda_lib, recompute):
         assert np.abs(got - ref).max() / scale <= 1e-4
 
 
+def test_batch_backward_after_interleaved_forward(cuda_lib):
+    """A second forward on other positions before the first backward replaces
+    the workspace's antialias records: the first backward must rebuild its
+    own and give the same gradients as an uninterrupted forward / backward."""
+    r, pos, attr, _ = _renderer()
+    w = torch.linspace(-1, 1, r.image_floats, device="cuda")
+    pa = pos.clone().requires_grad_(True)
+    (r(pa, attr) * w).sum().backward()
+    ref = pa.grad.clone()
+    pb = pos.clone().requires_grad_(True)
+    out1 = r(pb, attr)
+    other = pos.clone()
+    other[:, :2] *= 1.1
+    r(other, attr)  # overwrites the records
+    (out1 * w).sum().backward()
+    scale = ref.abs().max()
+    assert float((pb.grad - ref).abs().max() / scale) <= 1e-5
+
+
 def test_batch_raster_only_forward(cuda_lib):
     """A forward without an output buffer writes the same rast and colour as
     the full forward (the antialias pass is skipped)."""
