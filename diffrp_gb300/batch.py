@@ -49,7 +49,8 @@ def _register():
         "drp_batch_plan": [P, I, I, P],
         "drp_batch_block_maps": [P, I, P, P],
         "drp_batch_workspace_size": [LL, LL, ULL, ctypes.POINTER(ctypes.c_size_t)],
-        "drp_batch_forward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, I, I, ULL, P, P, P, P],
+        "drp_batch_forward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, I, I, ULL, ctypes.c_uint,
+                              P, P, P, P],
         "drp_batch_backward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, P, P, P, P, P, I, P],
     }
     for name, args in sigs.items():
@@ -65,10 +66,14 @@ class BatchRenderer:
     meshes: list of (tri (F, 3) int32 CUDA tensor, num_vertices, channels).
     items:  list of (mesh index, (height, width)).
     tile_log2 / threads_per_tri: fine-raster shape (see nvdr.RasterizeCudaContext).
+    bin_depth: None sizes fixed-depth tile bins from the first forward's
+    largest tile (one setup pass per forward afterwards); 0 keeps exact tile
+    lists (count, scan and fill passes); n > 0 fixes the depth.
     """
 
-    def __init__(self, meshes, items, device=None, tile_log2=4, threads_per_tri=0, recompute=False):
+    def __init__(self, meshes, items, device=None, tile_log2=4, threads_per_tri=0, recompute=False, bin_depth=None):
         _register()
+        self.bin_depth_mode = bin_depth
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.tile_log2 = int(tile_log2)
         self.threads_per_tri = int(threads_per_tri)
@@ -100,6 +105,7 @@ class BatchRenderer:
             p0 += int(V)
         self.pos_rows = p0
         self.items = items
+        self._fwd_gen = 0  # bumped by every forward; the workspace's AA records belong to the latest
         self._plan()
 
     def _plan(self):
@@ -127,10 +133,13 @@ class BatchRenderer:
         self._pmap = torch.from_numpy(np.frombuffer(bytes(pmap), dtype=np.int32).copy()).to(self.device)
         self._xmap = torch.from_numpy(np.frombuffer(bytes(xmap), dtype=np.int32).copy()).to(self.device)
         self._capacity = 0
+        self._depth = 0
         self._ws = None
+        self._pending = None
+        self._pinned = None
         self.last_list_entries = 0
-        self._fwd_gen = 0  # bumped by every forward; the workspace's AA records belong to the latest
-        self._rec_ws = None  # the workspace buffer holding those records
+        self.last_max_tile = 0
+        self._rec_ws = None  # the workspace buffer holding the latest forward's AA records
 
     def set_raster_shape(self, tile_log2, threads_per_tri):
         """Change the fine-raster tile size / threads per primitive (re-plans;
@@ -171,9 +180,46 @@ class BatchRenderer:
             self._ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
         return self._ws
 
+    def _choose_depth(self, max_tile, needed):
+        if self.bin_depth_mode is not None:
+            return int(self.bin_depth_mode)
+        depth = int(max_tile * 1.25) + 8
+        # fixed-depth bins only while they stay near the exact lists' size
+        return depth if self.total_tiles * depth <= 2 * needed + (4 << 20) else 0
+
+    def _poll_stats(self):
+        """Grow the bins / list from the stats of an earlier forward whose
+        lists overflowed (the overflowing tiles were still exact, but slow)."""
+        if self._pending is None or not self._pending.query():
+            return
+        self._pending = None
+        st = self._pinned.view(torch.int32)
+        if int(st[2]) & 2:
+            if self._depth:
+                self._depth = max(int(self._depth * 1.5), int(int(st[3]) * 1.25) + 8)
+            else:
+                self._capacity = max(self._capacity, int(int(self._pinned.view(torch.int64)[0]) * 1.25) + 4096)
+
+    def _queue_stats(self, ws):
+        if torch.cuda.is_current_stream_capturing():
+            return
+        if self._pinned is None:
+            self._pinned = torch.empty(16, dtype=torch.uint8, pin_memory=True)
+        self._pinned.copy_(ws[:16], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(self.device))
+        self._pending = ev
+
     def _forward_raw(self, pos, attr, rast, color, out):
         """out=None writes rast and colour only (no antialias pass)."""
-        cap = self._capacity if self._capacity else 4 * self.total_prims + 4096
+        if not torch.cuda.is_current_stream_capturing():
+            self._poll_stats()
+        first = not self._capacity
+        depth = 0 if first else self._depth
+        if depth:
+            cap = self.total_tiles * depth
+        else:
+            cap = self._capacity if self._capacity else 4 * self.total_prims + 4096
         optr = None if out is None else out.data_ptr()
         self._fwd_gen += 1
         ws = self._workspace(cap)
@@ -181,20 +227,25 @@ class BatchRenderer:
         args = (self._items_dev.data_ptr(), len(self.items), self._pmap.data_ptr(), self.prim_blocks,
                 self._xmap.data_ptr(), self.pixel_blocks, self.total_prims, self.total_tiles, pos.data_ptr(),
                 self.tri.data_ptr(), attr.data_ptr(), self.nbr.data_ptr(), self.tile_log2, self.threads_per_tri)
-        _ffi.call("drp_batch_forward", ws.data_ptr(), ws.numel(), *args, cap, rast.data_ptr(), color.data_ptr(),
-                  optr, stream)
-        if not self._capacity:
+        _ffi.call("drp_batch_forward", ws.data_ptr(), ws.numel(), *args, cap, depth, rast.data_ptr(),
+                  color.data_ptr(), optr, stream)
+        if first:
+            # exact lists, sized synchronously; they also give the largest tile
             torch.cuda.current_stream(self.device).synchronize()
-            stats = ws[:16].view(torch.int64).cpu()
-            needed = int(stats[0])
-            if int(stats[1]) & 1:
+            needed = int(ws[:8].view(torch.int64).cpu()[0])
+            words = ws[:16].view(torch.int32).cpu()
+            if int(words[2]) & 1:
                 raise RuntimeError("BatchRenderer: triangle vertex index out of range")
             self.last_list_entries = needed
+            self.last_max_tile = int(words[3])
             self._capacity = max(cap, int(needed * 1.25) + 4096)
+            self._depth = self._choose_depth(self.last_max_tile, needed)
             if needed > cap:
                 ws = self._workspace(self._capacity)
-                _ffi.call("drp_batch_forward", ws.data_ptr(), ws.numel(), *args, self._capacity, rast.data_ptr(),
-                          color.data_ptr(), optr, stream)
+                _ffi.call("drp_batch_forward", ws.data_ptr(), ws.numel(), *args, self._capacity, 0,
+                          rast.data_ptr(), color.data_ptr(), optr, stream)
+        else:
+            self._queue_stats(ws)
         self._rec_ws = ws
 
     def _backward_raw(self, pos, attr, rast, color, grad_out, grad_pos, grad_attr, gen=None):

@@ -38,6 +38,7 @@ struct BatchArgs {
     const int* nbr;
     int tile_log2, tpt;
     unsigned long long list_capacity;
+    uint32_t bin_depth;  // 0: exact lists (count, scan, fill); > 0: fixed-depth bins (one pass)
     float* rast;
     float* color;
     float* out;
@@ -53,8 +54,14 @@ struct BatchArgs {
     float4* aa_rec;
 };
 
-template <int TILE_LOG2, bool FILL>
+// MODE kSetupCount: triangle setup, antialias record, per-tile counts;
+// kSetupFill: append to the exact lists (after the scan); kSetupBins: setup,
+// record and append to fixed-depth bins in one pass.
+constexpr int kSetupCount = 0, kSetupFill = 1, kSetupBins = 2;
+
+template <int TILE_LOG2, int MODE>
 __global__ void __launch_bounds__(256) batch_setup_bin_kernel(BatchArgs a) {
+    constexpr bool FILL = MODE == kSetupFill;
     const int2 blk = a.prim_blocks[blockIdx.x];
     const drp_batch_item& it = a.items[blk.x];
     const long long j = (long long)blk.y * 256 + threadIdx.x;
@@ -87,12 +94,17 @@ __global__ void __launch_bounds__(256) batch_setup_bin_kernel(BatchArgs a) {
         bin_box<TILE_LOG2>(bx, live, it.tiles_x, a.tile_cursor + it.tile_offset, a.tile_list, a.list_capacity,
                            (uint32_t)pidx);
     } else {
-        // The antialias triangle record rides along with the count pass (same
+        // The antialias triangle record rides along with the setup pass (same
         // triangle, same vertices).
         aa_tri_record(reinterpret_cast<const float4*>(a.pos) + it.pos_offset, a.tri + 3 * (long long)it.tri_first,
                       a.nbr ? a.nbr + 3 * (long long)it.tri_first : nullptr, j, it.tri_count, it.num_vertices,
                       it.width, it.height, a.aa_rec + pidx * 2);
-        bin_box<TILE_LOG2>(bx, live, it.tiles_x, a.tile_count + it.tile_offset, nullptr, 0, 0);
+        if (MODE == kSetupBins)
+            bin_box<TILE_LOG2>(bx, live, it.tiles_x, a.tile_count + it.tile_offset,
+                               a.tile_list + (unsigned long long)it.tile_offset * a.bin_depth, 0, (uint32_t)pidx,
+                               a.bin_depth);
+        else
+            bin_box<TILE_LOG2>(bx, live, it.tiles_x, a.tile_count + it.tile_offset, nullptr, 0, 0);
     }
 }
 
@@ -170,7 +182,7 @@ __device__ __forceinline__ int find_item_by_tile(const drp_batch_item* items, in
 
 template <int TILE_LOG2, int TPT>
 __global__ void __launch_bounds__((1 << (2 * TILE_LOG2)) < 256 ? (1 << (2 * TILE_LOG2)) : 256,
-                                  TILE_LOG2 == 3 ? 12 : 3)
+                                  TILE_LOG2 == 3 ? 12 : 4)
 batch_fine_kernel(BatchArgs a) {
     __shared__ long long job;
     __shared__ int job_item;
@@ -188,10 +200,16 @@ batch_fine_kernel(BatchArgs a) {
         const int tile = (int)(t - it.tile_offset);
         FineTile ft;
         ft.recs = a.prims;
-        const uint32_t off = a.tile_offset[t];
         ft.cnt = a.tile_count[t];
-        ft.list = a.tile_list + off;
-        ft.overflow = (unsigned long long)off + ft.cnt > a.list_capacity;
+        if (a.bin_depth) {
+            ft.list = a.tile_list + (unsigned long long)t * a.bin_depth;
+            ft.overflow = ft.cnt > a.bin_depth;
+            if (ft.overflow && threadIdx.x == 0) atomicMax(a.stats + 3, ft.cnt);  // sizes the next depth
+        } else {
+            const uint32_t off = a.tile_offset[t];
+            ft.list = a.tile_list + off;
+            ft.overflow = (unsigned long long)off + ft.cnt > a.list_capacity;
+        }
         ft.scan_base = it.prim_offset;
         ft.scan_count = it.tri_count;
         ft.tx0 = (tile % it.tiles_x) << TILE_LOG2;
@@ -418,12 +436,15 @@ static void launch_batch_fine(const BatchArgs& a, cudaStream_t s) {
 
 template <int TL>
 static void launch_batch_raster(const BatchArgs& a, cudaStream_t s) {
-    if (a.n_prim_blocks > 0) {
-        batch_setup_bin_kernel<TL, false><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+    if (a.n_prim_blocks > 0 && a.bin_depth) {
+        batch_setup_bin_kernel<TL, kSetupBins><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+        drp_note_launch();
+    } else if (a.n_prim_blocks > 0) {
+        batch_setup_bin_kernel<TL, kSetupCount><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
         drp_note_launch();
         launch_tile_scan(a.tile_count, a.tile_offset, a.tile_cursor, a.total_tiles, a.chunk_sums,
                          reinterpret_cast<unsigned long long*>(a.stats), s);
-        batch_setup_bin_kernel<TL, true><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+        batch_setup_bin_kernel<TL, kSetupFill><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
         drp_note_launch();
     } else {
         cudaMemsetAsync(a.tile_offset, 0, sizeof(uint32_t) * a.total_tiles, s);
@@ -580,8 +601,8 @@ DRP_API int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp
                               const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
                               long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
                               const int* tri, const float* attr, const int* nbr, int tile_log2, int threads_per_tri,
-                              unsigned long long list_capacity, float* rast, float* color, float* out,
-                              void* stream) {
+                              unsigned long long list_capacity, unsigned bin_depth, float* rast, float* color,
+                              float* out, void* stream) {
     drp::BatchArgs a;
     drp::BatchLayout L;
     int st = batch_common(workspace, workspace_bytes, items, num_items, prim_block_map, prim_blocks, pixel_block_map,
@@ -591,9 +612,12 @@ DRP_API int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp
     if (threads_per_tri < 0 || threads_per_tri > 32 || (threads_per_tri & (threads_per_tri - 1)))
         return bfail("batch: threads_per_tri must be 0 or a power of two <= 32");
     if (!rast || !color || (reinterpret_cast<uintptr_t>(rast) & 15)) return bfail("batch: bad outputs");
+    if (bin_depth && (unsigned long long)total_tiles * bin_depth > list_capacity)
+        return bfail("batch: list_capacity below total_tiles * bin_depth");
     a.nbr = nbr;
     a.tile_log2 = tile_log2;
     a.tpt = threads_per_tri;
+    a.bin_depth = bin_depth;
     a.rast = rast;
     a.color = color;
     a.out = out;

@@ -21,7 +21,7 @@ struct RasterWs {
     uint32_t* tile_cursor;  // B * tiles
     uint32_t* tile_list;    // list_capacity entries
     unsigned long long* chunk_sums;  // tile-scan chunk sums, ceil(B * tiles / 4096)
-    uint32_t* stats;        // [0..1] total list entries (u64), [2] device error bits, [3] spare
+    uint32_t* stats;        // [0..1] total list entries (u64), [2] device error bits, [3] largest tile count
 };
 
 struct RasterArgs {

@@ -112,7 +112,7 @@ struct RastEmit {
 
 template <int TILE_LOG2, int TPT>
 __global__ void __launch_bounds__((1 << (2 * TILE_LOG2)) < 256 ? (1 << (2 * TILE_LOG2)) : 256,
-                                  TILE_LOG2 == 3 ? 12 : 3)
+                                  TILE_LOG2 == 3 ? 12 : 4)
 fine_raster_kernel(RasterArgs a) {
     const int b = blockIdx.y;
     const int tile = blockIdx.x;

@@ -125,8 +125,12 @@ __device__ __forceinline__ bool build_prim(const float4& p0, const float4& p1, c
 // `capacity` are dropped and the tile falls back to a full scan).  Every
 // lane of the warp must call this (n = 0 for lanes with nothing to bin).
 template <int TILE_LOG2>
+// depth == 0: counters are cursors into one list of `capacity` entries
+// (slot = list index); depth > 0: counters count per tile and tile t's
+// entries go to list[t * depth + slot] while slot < depth (fixed-depth bins).
 __device__ __forceinline__ void bin_box(const PrimBox& bx, bool live, int tiles_x, uint32_t* counters,
-                                        uint32_t* list, unsigned long long capacity, uint32_t pidx) {
+                                        uint32_t* list, unsigned long long capacity, uint32_t pidx,
+                                        uint32_t depth = 0) {
     const int tx0 = bx.px0 >> TILE_LOG2, tx1 = bx.px1 >> TILE_LOG2, ty0 = bx.py0 >> TILE_LOG2,
               ty1 = bx.py1 >> TILE_LOG2;
     const int n = live ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0;
@@ -136,7 +140,11 @@ __device__ __forceinline__ void bin_box(const PrimBox& bx, bool live, int tiles_
         if (i >= n) break;
         const uint32_t tile = (uint32_t)((ty0 + i / w) * tiles_x + tx0 + i % w);
         const uint32_t slot = warp_agg_inc(counters, tile, active);
-        if (list && slot < capacity) list[slot] = pidx;
+        if (depth) {
+            if (slot < depth) list[(unsigned long long)tile * depth + slot] = pidx;
+        } else if (list && slot < capacity) {
+            list[slot] = pidx;
+        }
     }
 }
 
@@ -672,6 +680,13 @@ static __global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(const u
             }
     }
     if (b == gridDim.x - 1 && threadIdx.x == 0) *total = prefix + chunk_total;
+    // largest tile count -> stats word 3 (words 0..1 hold the total, 2 the
+    // device error bits); it sizes fixed-depth bins
+    uint32_t mx = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPerThread; ++k) mx = max(mx, c[k]);
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if ((threadIdx.x & 31) == 0 && mx) atomicMax(reinterpret_cast<uint32_t*>(total) + 3, mx);
 }
 
 // chunk_sums: scan_chunks(n) u64 of scratch (unused when n <= kScanChunk).

@@ -287,12 +287,20 @@ int drp_batch_workspace_size(long long total_prims, long long total_tiles, unsig
  * NULL: then only rast and colour are written (the antialias pass is
  * skipped), which is how a backward without stored per-pixel buffers
  * regenerates them.
+ * bin_depth 0: exact tile lists (count, scan, fill; list_capacity entries);
+ * the workspace's stats then hold the total list entries (u64 at byte 0) and
+ * the largest tile count (u32 at byte 12).  bin_depth > 0: one setup pass
+ * appends to fixed-depth bins (list_capacity >= total_tiles * bin_depth);
+ * a tile with more entries is still rasterised exactly (by scanning all of
+ * its item's triangles), sets DRP_DEVERR_LIST_OVERFLOW (u32 at byte 8) and
+ * raises the u32 at byte 12 to its count.
  */
 int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
                       const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
                       long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
                       const int* tri, const float* attr, const int* nbr, int tile_log2, int threads_per_tri,
-                      unsigned long long list_capacity, float* rast, float* color, float* out, void* stream);
+                      unsigned long long list_capacity, unsigned bin_depth, float* rast, float* color, float* out,
+                      void* stream);
 
 /* drp_batch_backward flag: the workspace still holds the antialias triangle
  * records of the last drp_batch_forward, which ran on the same positions

@@ -36,11 +36,12 @@ def _scene(items=SMALL_ITEMS):
     return meshes_np, chans, attrs, items, views
 
 
-def _renderer(recompute=False, tile_log2=4, tpt=0, items=SMALL_ITEMS):
+def _renderer(recompute=False, tile_log2=4, tpt=0, items=SMALL_ITEMS, bin_depth=None):
     from diffrp_gb300.batch import BatchRenderer
     meshes_np, chans, attrs, items, views = _scene(items)
     meshes = [(torch.from_numpy(f).cuda(), len(v), c) for (v, f), c in zip(meshes_np, chans)]
-    r = BatchRenderer(meshes, items, tile_log2=tile_log2, threads_per_tri=tpt, recompute=recompute)
+    r = BatchRenderer(meshes, items, tile_log2=tile_log2, threads_per_tri=tpt, recompute=recompute,
+                      bin_depth=bin_depth)
     pos = r.pack_positions([torch.from_numpy(p).cuda() for p in views])
     attr = r.pack_attributes([torch.from_numpy(a).cuda() for a in attrs])
     return r, pos, attr, (meshes_np, chans, attrs, items, views)
@@ -114,6 +115,25 @@ def test_batch_backward_after_interleaved_forward(cuda_lib):
     (out1 * w).sum().backward()
     scale = ref.abs().max()
     assert float((pb.grad - ref).abs().max() / scale) <= 1e-5
+
+
+@pytest.mark.parametrize("depth", [None, 2], ids=["sized", "overflowing"])
+def test_batch_fixed_depth_bins_exact(cuda_lib, depth):
+    """The first forward uses exact tile lists and sizes fixed-depth bins from
+    its largest tile; later forwards bin in one pass.  Both give the same
+    images; bins too shallow for their tiles still rasterise exactly and grow
+    for the next forward."""
+    r, pos, attr, _ = _renderer(bin_depth=depth)
+    first = r.forward_buffers(pos, attr)
+    assert r._depth > 0
+    second = r.forward_buffers(pos, attr)
+    for a, b in zip(first, second):
+        assert torch.equal(a, b)
+    if depth == 2:
+        assert r.last_max_tile > 2
+        torch.cuda.synchronize()
+        r._poll_stats()
+        assert r._depth > 2
 
 
 def test_batch_raster_only_forward(cuda_lib):
