@@ -136,13 +136,14 @@ class BatchStep:
     """The same step through the batching form (one item): fused raster +
     interpolation, antialias, fused backward (diffrp_gb300.batch)."""
 
-    def __init__(self, dev, f, mvp, target, V, C, tile=(4, 0)):
+    def __init__(self, dev, f, mvp, target, V, C, tile=(4, 0), fused_loss=True):
         import torch
         from diffrp_gb300.batch import BatchRenderer
         self.torch = torch
         self.tri = torch.from_numpy(f).to(dev)
         self.mvp = torch.from_numpy(mvp).to(dev)
         self.target = torch.from_numpy(target).to(dev).reshape(-1)
+        self.fused_loss = fused_loss
         self.renderer = BatchRenderer([(self.tri, V, C)], [(0, (H, W))], device=dev, tile_log2=tile[0],
                                       threads_per_tri=tile[1])
 
@@ -151,8 +152,10 @@ class BatchStep:
         verts.grad = None
         attr.grad = None
         clip = torch.nn.functional.pad(verts, (0, 1), value=1.0) @ self.mvp.T
-        out = self.renderer(clip, attr.reshape(-1))
-        loss = l1_loss(out, self.target)
+        if self.fused_loss:
+            loss, _ = self.renderer.render_l1(clip, attr.reshape(-1), self.target)
+        else:
+            loss = l1_loss(self.renderer(clip, attr.reshape(-1)), self.target)
         loss.backward()
         return loss
 
@@ -210,6 +213,14 @@ class MultiViewWorkload:
                                       device=dev, tile_log2=tl, threads_per_tri=tpt, recompute=recompute)
         self.target = torch.from_numpy(rng.uniform(0, 1, self.renderer.image_floats).astype(np.float32)).to(dev)
         self.targets = self.renderer.images(self.target)
+        # items grouped by mesh (every workload here): one batched transform per
+        # mesh, (n_m, 4, 4) MVPs against the mesh's (V, 4) vertices
+        order = [m for m, _ in self.items]
+        self.grouped = order == sorted(order)
+        self.mesh_mvps = []
+        for m in range(len(self.verts)):
+            ks = [k for k, (mm, _) in enumerate(self.items) if mm == m]
+            self.mesh_mvps.append(torch.stack([self.mvps[k] for k in ks]) if ks else None)
         from diffrp_gb300 import nvdr
         self.nvdr = nvdr
         self.ctx = nvdr.RasterizeCudaContext(dev)
@@ -223,12 +234,23 @@ class MultiViewWorkload:
         for t in self.verts + self.attrs:
             t.grad = None
 
+    def _packed_clip(self):
+        torch = self.torch
+        if not self.grouped:
+            return torch.cat([self._clip(m, k) for k, (m, _) in enumerate(self.items)])
+        parts = []
+        for v, mv in zip(self.verts, self.mesh_mvps):
+            if mv is not None:
+                vh = torch.nn.functional.pad(v, (0, 1), value=1.0)
+                parts.append(torch.matmul(vh, mv.transpose(1, 2)).reshape(-1, 4))
+        return torch.cat(parts) if len(parts) > 1 else parts[0]
+
     def batched_step(self):
+        """The batching form with the L1 loss fused into its antialias pass."""
         self._zero()
-        pos = self.torch.cat([self._clip(m, k) for k, (m, _) in enumerate(self.items)])
+        pos = self._packed_clip()
         attr = self.torch.cat([a.reshape(-1) for a in self.attrs])
-        out = self.renderer(pos, attr)
-        loss = l1_loss(out, self.target)
+        loss, _ = self.renderer.render_l1(pos, attr, self.target)
         loss.backward()
         return loss
 
@@ -302,17 +324,16 @@ def large16_workload(dev, seed=0):
     return [(v, f, 12)], items
 
 
-def run_batched(dev, name, steps, warmup, plain=True, recompute=False, tune=True):
+def run_batched(dev, name, steps, warmup, plain=True, recompute=False, tune=True, tile=None):
     """Mpix/s of the batched form (graph-captured) and of the plain per-item
     drop-in calls (eager, and graph-captured when it fits) on one workload."""
     import torch
     from diffrp_gb300 import autotune
     meshes, items = {"views64": views64_workload, "uneven48": uneven48_workload,
                      "large16": large16_workload}[name](dev)
-    tile = None
     torch.cuda.reset_peak_memory_stats(dev)
     wl = MultiViewWorkload(dev, meshes, items, recompute=recompute, tile=tile)
-    if tune:
+    if tune and tile is None:
         with torch.no_grad():
             pos0 = torch.cat([wl._clip(m, k) for k, (m, _) in enumerate(wl.items)])
             attr0 = torch.cat([a.reshape(-1) for a in wl.attrs])
@@ -472,6 +493,12 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None, batc
         b_ga = torch.zeros_like(a_t).reshape(-1)
         flat_attr = a_t.reshape(-1)
         ops["batch_forward"] = lambda: batch._forward_raw(clip, flat_attr, b_rast, b_color, b_out)
+        b_target = torch.from_numpy(target).to(dev).reshape(-1)
+        b_grad = torch.empty_like(b_color)
+        b_blocks = torch.empty(max(1, batch.pixel_blocks), dtype=torch.float32, device=dev)
+        b_loss = torch.empty((), dtype=torch.float32, device=dev)
+        ops["batch_forward_l1"] = lambda: batch._forward_raw(
+            clip, flat_attr, b_rast, b_color, b_out, (b_target, 1.0 / b_color.numel(), b_grad, b_blocks, b_loss))
         # the step's backward reuses the antialias records of its forward
         ops["batch_backward"] = lambda: batch._backward_raw(clip, flat_attr, b_rast, b_color, b_g, b_gp, b_ga,
                                                             batch._fwd_gen)
@@ -487,6 +514,8 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None, batc
         # outputs written once (rast, colour, antialiased output), vertex
         # positions / attributes / triangles read once
         "batch_forward": P * (16 + 4 * C + 4 * C) + V * (16 + 4 * C) + F * 12,
+        # the same plus the loss: target read, sign gradient written
+        "batch_forward_l1": P * (16 + 4 * C * 4) + V * (16 + 4 * C) + F * 12,
         # rast, colour and output gradient read once; vertex / attribute
         # gradients written once
         "batch_backward": P * (16 + 4 * C + 4 * C) + V * (16 + 4 * C) * 2 + F * 12,
@@ -595,8 +624,9 @@ def main():
     __graft_entry__.build()
     if args.workload != "single":
         W_ = max(3, args.warmup)
+        fixed = tuple(int(x) for x in args.tile.split(",")) if args.tile else None
         res = run_batched(dev, args.workload, steps=args.steps, warmup=W_, plain=args.workload != "large16",
-                          recompute=args.workload == "large16")
+                          recompute=args.workload == "large16", tile=fixed)
         if world > 1:
             t = torch.tensor([res["batched"]["ms_per_step"]], device=dev)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -655,6 +685,10 @@ def main():
     batched = GraphedStep(bstep, verts_np, attr_np, dev)
     for _ in range(W_):
         batched()
+    # the same batching form with the separate l1_loss op (reported beside)
+    bstep.fused_loss = False
+    batched_unfused = None if args.mode == "steps" else GraphedStep(bstep, verts_np, attr_np, dev)
+    bstep.fused_loss = True
     torch.cuda.synchronize()
 
     def barrier():
@@ -689,6 +723,7 @@ def main():
             dist.destroy_process_group()
         return 0
     plain_ms = timed(graphed, args.steps)
+    unfused_ms = timed(batched_unfused, args.steps)
     eager_ms = timed(lambda: step(verts, attr), args.steps)
 
     # -- end-to-end through the public API with host buffers -----------------
@@ -723,7 +758,7 @@ def main():
 
     if rank == 0:
         times, algo = kernel_breakdown(dev, verts_np, f, attr_np, mvp, target, tuned=tuned, batch=bstep.renderer)
-        dom = max(["batch_forward", "batch_backward"], key=times.get)
+        dom = max(["batch_forward_l1", "batch_backward"], key=times.get)
         peak, peak_kind = _peaks()
         achieved = algo[dom] / (times[dom] / 1e3) / 1e9
         traffic = None
@@ -743,7 +778,8 @@ def main():
                        "global_batch": world, "resolution": [H, W], "channels": C,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "flushed between steps (256 MiB write outside the timed events)",
-                       "path": "batching form (diffrp_gb300.batch, one item), whole fwd+bwd step as one CUDA graph",
+                       "path": "batching form (diffrp_gb300.batch, one item) with the L1 loss fused into its "
+                               "antialias pass (BatchRenderer.render_l1), whole fwd+bwd step as one CUDA graph",
                        "raster_tuning": {"tile": 1 << btuned["tile_log2"],
                                          "threads_per_tri": btuned["threads_per_tri"],
                                          "plain_path": {"tile": 1 << tuned["tile_log2"],
@@ -753,6 +789,10 @@ def main():
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                          "algorithmic_bytes": algo[dom], "kernel_ms": times[dom]},
             "kernel_ms": times,
+            "batched_unfused_loss": {"value": pix / (unfused_ms / 1e3) / 1e6, "unit": UNIT,
+                                     "ms_per_step": unfused_ms / args.steps,
+                                     "note": "batching form, loss by the separate l1_loss op (image written, "
+                                             "then read back by the loss)"},
             "plain": {"value": pix / (plain_ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": plain_ms / args.steps,
                       "note": "same step through the drop-in nvdr ops, captured as one CUDA graph"},
             "eager": {"value": pix / (eager_ms / 1e3) / 1e6, "unit": UNIT,
@@ -760,9 +800,13 @@ def main():
             "e2e_dropin": {"value": pix / (e2e_plain_ms / 1e3) / 1e6, "unit": UNIT,
                            "note": "end to end through the drop-in nvdr ops (graph), host buffers"},
             "clocks": clocks,
-            # timed regions: batched graph and its e2e (2x), drop-in graph, its e2e and eager (3x)
-            "gpu_launches": (batched.launches_per_step * 2 + graphed.launches_per_step * 3) * args.steps,
-            "launches_per_step": {"batched": batched.launches_per_step, "dropin": graphed.launches_per_step},
+            # timed regions: batched graph and its e2e (2x), the unfused-loss batched graph, drop-in graph,
+            # its e2e and eager (3x)
+            "gpu_launches": (batched.launches_per_step * 2 + batched_unfused.launches_per_step +
+                             graphed.launches_per_step * 3) * args.steps,
+            "launches_per_step": {"batched": batched.launches_per_step,
+                                  "batched_unfused_loss": batched_unfused.launches_per_step,
+                                  "dropin": graphed.launches_per_step},
         }
         if not args.no_batched:
             line["batched_views64"] = run_batched(dev, "views64", steps=max(5, args.steps // 3), warmup=W_)

@@ -51,7 +51,9 @@ def _register():
         "drp_batch_workspace_size": [LL, LL, ULL, ctypes.POINTER(ctypes.c_size_t)],
         "drp_batch_forward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, I, I, ULL, ctypes.c_uint,
                               P, P, P, P],
-        "drp_batch_backward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, P, P, P, P, P, I, P],
+        "drp_batch_forward_l1": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, I, I, ULL,
+                                 ctypes.c_uint, P, P, P, P, ctypes.c_float, P, P, P, P],
+        "drp_batch_backward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, P, P, P, P, P, P, I, P],
     }
     for name, args in sigs.items():
         fn = getattr(lib, name)
@@ -106,6 +108,7 @@ class BatchRenderer:
         self.pos_rows = p0
         self.items = items
         self._fwd_gen = 0  # bumped by every forward; the workspace's AA records belong to the latest
+        self._retired = []  # replaced workspaces, kept alive for graphs captured on them
         self._plan()
 
     def _plan(self):
@@ -134,6 +137,8 @@ class BatchRenderer:
         self._xmap = torch.from_numpy(np.frombuffer(bytes(xmap), dtype=np.int32).copy()).to(self.device)
         self._capacity = 0
         self._depth = 0
+        if getattr(self, "_ws", None) is not None:
+            self._retired.append(self._ws)
         self._ws = None
         self._pending = None
         self._pinned = None
@@ -177,6 +182,8 @@ class BatchRenderer:
     def _workspace(self, cap):
         nbytes = _ffi.size_out("drp_batch_workspace_size", self.total_prims, self.total_tiles, cap)
         if self._ws is None or self._ws.numel() < nbytes:
+            if self._ws is not None:
+                self._retired.append(self._ws)  # a captured CUDA graph may still use it
             self._ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
         return self._ws
 
@@ -210,8 +217,10 @@ class BatchRenderer:
         ev.record(torch.cuda.current_stream(self.device))
         self._pending = ev
 
-    def _forward_raw(self, pos, attr, rast, color, out):
-        """out=None writes rast and colour only (no antialias pass)."""
+    def _forward_raw(self, pos, attr, rast, color, out, l1=None):
+        """out=None writes rast and colour only (no antialias pass).  l1 =
+        (target, scale, grad, block_loss, loss) fuses the L1 loss into the
+        antialias pass (drp_batch_forward_l1)."""
         if not torch.cuda.is_current_stream_capturing():
             self._poll_stats()
         first = not self._capacity
@@ -227,8 +236,16 @@ class BatchRenderer:
         args = (self._items_dev.data_ptr(), len(self.items), self._pmap.data_ptr(), self.prim_blocks,
                 self._xmap.data_ptr(), self.pixel_blocks, self.total_prims, self.total_tiles, pos.data_ptr(),
                 self.tri.data_ptr(), attr.data_ptr(), self.nbr.data_ptr(), self.tile_log2, self.threads_per_tri)
-        _ffi.call("drp_batch_forward", ws.data_ptr(), ws.numel(), *args, cap, depth, rast.data_ptr(),
-                  color.data_ptr(), optr, stream)
+        if l1 is not None:
+            target, scale, grad, block_loss, loss = l1
+            tail = (target.data_ptr(), ctypes.c_float(scale), grad.data_ptr(), block_loss.data_ptr(),
+                    loss.data_ptr(), stream)
+            entry = "drp_batch_forward_l1"
+        else:
+            tail = (stream,)
+            entry = "drp_batch_forward"
+        _ffi.call(entry, ws.data_ptr(), ws.numel(), *args, cap, depth, rast.data_ptr(), color.data_ptr(), optr,
+                  *tail)
         if first:
             # exact lists, sized synchronously; they also give the largest tile
             torch.cuda.current_stream(self.device).synchronize()
@@ -242,15 +259,16 @@ class BatchRenderer:
             self._depth = self._choose_depth(self.last_max_tile, needed)
             if needed > cap:
                 ws = self._workspace(self._capacity)
-                _ffi.call("drp_batch_forward", ws.data_ptr(), ws.numel(), *args, self._capacity, 0,
-                          rast.data_ptr(), color.data_ptr(), optr, stream)
+                _ffi.call(entry, ws.data_ptr(), ws.numel(), *args, self._capacity, 0, rast.data_ptr(),
+                          color.data_ptr(), optr, *tail)
         else:
             self._queue_stats(ws)
         self._rec_ws = ws
 
-    def _backward_raw(self, pos, attr, rast, color, grad_out, grad_pos, grad_attr, gen=None):
+    def _backward_raw(self, pos, attr, rast, color, grad_out, grad_pos, grad_attr, gen=None, grad_scale=None):
         """gen: the forward generation that produced rast / colour from pos;
-        when it is still the latest, its antialias records are reused."""
+        when it is still the latest, its antialias records are reused.
+        grad_scale: a one-element device tensor multiplying grad_out."""
         ws = self._workspace(0)  # the backward reads no tile list
         stream = torch.cuda.current_stream(self.device).cuda_stream
         flags = REUSE_AA_RECORDS if gen is not None and gen == self._fwd_gen and ws is self._rec_ws else 0
@@ -258,7 +276,7 @@ class BatchRenderer:
                   self._pmap.data_ptr(), self.prim_blocks, self._xmap.data_ptr(), self.pixel_blocks,
                   self.total_prims, self.total_tiles, pos.data_ptr(), self.tri.data_ptr(), attr.data_ptr(),
                   self.nbr.data_ptr(), rast.data_ptr(), color.data_ptr(), grad_out.data_ptr(), grad_pos.data_ptr(),
-                  grad_attr.data_ptr(), flags, stream)
+                  grad_attr.data_ptr(), None if grad_scale is None else grad_scale.data_ptr(), flags, stream)
 
     def _buffers(self):
         rast = torch.empty((self.total_pixels, 4), dtype=torch.float32, device=self.device)
@@ -273,6 +291,22 @@ class BatchRenderer:
         if attr.numel() != self.attr_floats or attr.dtype != torch.float32 or not attr.is_cuda:
             raise RuntimeError("attr must hold %d float32 values on the GPU" % self.attr_floats)
         return _BatchFn.apply(pos.contiguous(), attr.contiguous().reshape(-1), self)
+
+    def render_l1(self, pos, attr, target):
+        """Render and score in one pass: returns (loss, images) with loss =
+        mean |images - target| over all image floats (target packed like
+        the images).  Differentiable w.r.t. pos and attr through both
+        outputs; the loss path never materialises a per-pixel gradient
+        product (the upstream loss gradient is applied inside the fused
+        backward)."""
+        if pos.shape != (self.pos_rows, 4) or pos.dtype != torch.float32 or not pos.is_cuda:
+            raise RuntimeError("pos must be a float32 CUDA tensor of shape (%d, 4)" % self.pos_rows)
+        if attr.numel() != self.attr_floats or attr.dtype != torch.float32 or not attr.is_cuda:
+            raise RuntimeError("attr must hold %d float32 values on the GPU" % self.attr_floats)
+        if target.numel() != self.image_floats or target.dtype != torch.float32 or not target.is_cuda:
+            raise RuntimeError("target must hold %d float32 values on the GPU" % self.image_floats)
+        return _BatchL1Fn.apply(pos.contiguous(), attr.contiguous().reshape(-1), target.contiguous().reshape(-1),
+                                self)
 
     def forward_buffers(self, pos, attr):
         """Forward without autograd; returns (rast, colour, output) packed."""
@@ -311,3 +345,49 @@ class _BatchFn(torch.autograd.Function):
         grad_attr = torch.zeros_like(attr)
         r._backward_raw(pos, attr, rast, color, grad_out.contiguous(), grad_pos, grad_attr, gen)
         return grad_pos, grad_attr, None
+
+
+class _BatchL1Fn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, pos, attr, target, renderer):
+        ctx.set_materialize_grads(False)
+        rast, color = renderer._buffers()
+        out = torch.empty_like(color)
+        grad = torch.empty_like(color)
+        block_loss = torch.empty(max(1, renderer.pixel_blocks), dtype=torch.float32, device=pos.device)
+        loss = torch.empty((), dtype=torch.float32, device=pos.device)
+        renderer._forward_raw(pos, attr, rast, color, out,
+                              (target, 1.0 / renderer.image_floats, grad, block_loss, loss))
+        ctx.renderer = renderer
+        ctx.gen = renderer._fwd_gen
+        if renderer.recompute:
+            ctx.save_for_backward(pos, attr, grad)
+        else:
+            ctx.save_for_backward(pos, attr, grad, rast, color)
+        return loss, out
+
+    @staticmethod
+    def backward(ctx, g_loss, g_out):
+        r = ctx.renderer
+        if r.recompute:
+            pos, attr, grad = ctx.saved_tensors
+            rast, color = r._buffers()
+            r._forward_raw(pos, attr, rast, color, None)
+            gen = r._fwd_gen
+        else:
+            pos, attr, grad, rast, color = ctx.saved_tensors
+            gen = ctx.gen
+        grad_pos = torch.zeros_like(pos)
+        grad_attr = torch.zeros_like(attr)
+        if g_loss is None and g_out is None:
+            return grad_pos, grad_attr, None, None
+        scale = None
+        if g_out is None:
+            gout = grad  # sign / n, scaled by the loss gradient inside the kernel
+            scale = g_loss.reshape(1).to(torch.float32).contiguous()
+        elif g_loss is None:
+            gout = g_out.contiguous()
+        else:
+            gout = (grad * g_loss + g_out).contiguous()
+        r._backward_raw(pos, attr, rast, color, gout, grad_pos, grad_attr, gen, scale)
+        return grad_pos, grad_attr, None, None

@@ -22,8 +22,9 @@ __device__ __forceinline__ float edge_fn(const float2& a, const float2& b, const
 // s2.y, sgn, mask bits); sgn = 0 marks an unusable triangle (a vertex with
 // w <= 0, zero / NaN screen area); mask bit k: edge k (vertices k+1, k+2) is
 // a silhouette (no neighbour across it, or the neighbour's opposite vertex
-// projects to the same side of the edge as this triangle's).
-__device__ __forceinline__ void aa_tri_record(const float4* P, const int* tri, const int* nbr, long long t,
+// projects to the same side of the edge as this triangle's).  opp: the
+// topology table (opposite vertex across each edge, -1 for none) or null.
+__device__ __forceinline__ void aa_tri_record(const float4* P, const int* tri, const int* opp_tab, long long t,
                                               long long F, long long V, int W, int H, float4* rec) {
     const int v[3] = {tri[3 * t], tri[3 * t + 1], tri[3 * t + 2]};
     float2 s[3];
@@ -45,17 +46,10 @@ __device__ __forceinline__ void aa_tri_record(const float4* P, const int* tri, c
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             bool sil = true;
-            const int N = nbr ? nbr[3 * t + k] : -1;
-            if (N >= 0 && N < F) {
-                const int ea = v[(k + 1) % 3], eb = v[(k + 2) % 3];
-                int opp = -1;
-#pragma unroll
-                for (int i = 0; i < 3; ++i) {
-                    const int x = tri[3 * (long long)N + i];
-                    if (x != ea && x != eb && x >= 0 && x < V) opp = x;
-                }
+            const int opp = opp_tab ? opp_tab[3 * t + k] : -1;
+            if (opp >= 0 && opp < V) {
                 float2 so;
-                if (opp >= 0 && project_vertex(P[opp], W, H, so)) {
+                if (project_vertex(P[opp], W, H, so)) {
                     const float2 qa = s[(k + 1) % 3], qb = s[(k + 2) % 3];
                     const float dT = edge_fn(qa, qb, s[k]);
                     const float dN = edge_fn(qa, qb, so);
@@ -185,16 +179,13 @@ __device__ __forceinline__ void copy_channels(const float* src, float* dst, int 
     }
 }
 
-// Forward of one pixel: out = c + sum over pair slots targeting this pixel of
-// w (c[src] - c), in slot order (fmaf).  R, Cc: the view's rast and colour.
-// COPY = false: o already holds c (the caller wrote it), so pixels without a
-// blend are left untouched.  The pixel's and its four neighbours' rast rows
-// are loaded together, before any of them is used.
-template <bool COPY>
-__device__ __forceinline__ void aa_fwd_pixel(const float4* R, const float* Cc, const float4* rec, long long F, int W,
-                                             int H, int C, int pix, float* o) {
+// Blend terms of one pixel: for each pair slot (left, right, below, above)
+// whose pair blends into this pixel, the source pixel and its weight.  The
+// pixel's and its four neighbours' rast rows are loaded together, before any
+// of them is used.  Returns whether any slot blends.
+__device__ __forceinline__ bool aa_fwd_terms(const float4* R, const float4* rec, long long F, int W, int H, int pix,
+                                             int (&src)[4], float (&wt)[4]) {
     const int py = pix / W, px = pix - py * W;
-    const float* cs = Cc + (long long)pix * C;
     int A[4], B[4], ax[4], ay[4];
     bool vert[4], has[4];
     float4 rn[4];
@@ -204,8 +195,6 @@ __device__ __forceinline__ void aa_fwd_pixel(const float4* R, const float* Cc, c
         has[q] = pair_slot(q, pix, px, py, W, H, A[q], B[q], ax[q], ay[q], vert[q]);
         if (has[q]) rn[q] = R[A[q] == pix ? B[q] : A[q]];
     }
-    int src[4];
-    float wt[4];
     bool any = false;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -221,7 +210,20 @@ __device__ __forceinline__ void aa_fwd_pixel(const float4* R, const float* Cc, c
             any = true;
         }
     }
-    if (!any) {
+    return any;
+}
+
+// Forward of one pixel: out = c + sum over pair slots targeting this pixel of
+// w (c[src] - c), in slot order (fmaf).  R, Cc: the view's rast and colour.
+// COPY = false: o already holds c (the caller wrote it), so pixels without a
+// blend are left untouched.
+template <bool COPY>
+__device__ __forceinline__ void aa_fwd_pixel(const float4* R, const float* Cc, const float4* rec, long long F, int W,
+                                             int H, int C, int pix, float* o) {
+    const float* cs = Cc + (long long)pix * C;
+    int src[4];
+    float wt[4];
+    if (!aa_fwd_terms(R, rec, F, W, H, pix, src, wt)) {
         if (COPY) copy_channels(cs, o, C);
         return;
     }
@@ -233,6 +235,70 @@ __device__ __forceinline__ void aa_fwd_pixel(const float4* R, const float* Cc, c
             if (src[q] >= 0) v = fmaf(wt[q], Cc[(long long)src[q] * C + c] - base, v);
         o[c] = v;
     }
+}
+
+__device__ __forceinline__ float l1_sign(float d, float scale) {
+    return d > 0.0f ? scale : (d < 0.0f ? -scale : 0.0f);
+}
+
+// Forward of one pixel with the mean-absolute-error loss fused: the output
+// value of every channel as aa_fwd_pixel computes it (written to o when o is
+// not null), g = sign(out - target) * scale, and the return value is the
+// pixel's sum of |out - target| in channel order.  tg, o, g: this pixel's
+// target, output and gradient rows.
+__device__ __forceinline__ float aa_fwd_pixel_l1(const float4* R, const float* Cc, const float4* rec, long long F,
+                                                 int W, int H, int C, int pix, const float* tg, float scale, float* o,
+                                                 float* g) {
+    const float* cs = Cc + (long long)pix * C;
+    int src[4];
+    float wt[4];
+    const bool any = aa_fwd_terms(R, rec, F, W, H, pix, src, wt);
+    float s = 0.0f;
+    const bool vec = (C & 3) == 0 &&
+                     (((uintptr_t)cs | (uintptr_t)tg | (uintptr_t)g | (uintptr_t)(o ? o : g)) & 15) == 0;
+    if (vec) {
+        for (int c = 0; c < C; c += 4) {
+            const float4 b4 = *reinterpret_cast<const float4*>(cs + c);
+            const float4 t4 = *reinterpret_cast<const float4*>(tg + c);
+            const float base[4] = {b4.x, b4.y, b4.z, b4.w};
+            float v[4] = {b4.x, b4.y, b4.z, b4.w};
+            if (any) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (src[q] < 0) continue;
+                    const float4 s4 = *reinterpret_cast<const float4*>(Cc + (long long)src[q] * C + c);
+                    const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) v[k] = fmaf(wt[q], sv[k] - base[k], v[k]);
+                }
+            }
+            if (o) *reinterpret_cast<float4*>(o + c) = make_float4(v[0], v[1], v[2], v[3]);
+            const float tv[4] = {t4.x, t4.y, t4.z, t4.w};
+            float gv[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float d = v[k] - tv[k];
+                s += fabsf(d);
+                gv[k] = l1_sign(d, scale);
+            }
+            *reinterpret_cast<float4*>(g + c) = make_float4(gv[0], gv[1], gv[2], gv[3]);
+        }
+    } else {
+        for (int c = 0; c < C; ++c) {
+            const float base = cs[c];
+            float v = base;
+            if (any) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (src[q] >= 0) v = fmaf(wt[q], Cc[(long long)src[q] * C + c] - base, v);
+            }
+            if (o) o[c] = v;
+            const float d = v - tg[c];
+            s += fabsf(d);
+            g[c] = l1_sign(d, scale);
+        }
+    }
+    return s;
 }
 
 // Backward pair terms of one pixel.  For every pair slot: role (0 none, 1 this
@@ -247,7 +313,7 @@ struct AATerms {
 
 __device__ __forceinline__ void aa_bwd_terms(const float4* R, const float* Cc, const float* Gd, const float4* rec,
                                              long long F, int W, int H, int C, const float4* P, const int* tri,
-                                             float4* GP, float boost, int pix, AATerms& at) {
+                                             float4* GP, float boost, int pix, AATerms& at, float gscale = 1.0f) {
     const int py = pix / W, px = pix - py * W;
     int As[4], Bs[4], axs[4], ays[4];
     bool verts[4], has[4];
@@ -278,8 +344,8 @@ __device__ __forceinline__ void aa_bwd_terms(const float4* R, const float* Cc, c
         if (!GP || A != pix || p.clamped) continue;
         float dLdw = 0.f;
         for (int c = 0; c < C; ++c)
-            dLdw = fmaf(Gd[(long long)p.target * C + c], Cc[(long long)p.src * C + c] - Cc[(long long)p.target * C + c],
-                        dLdw);
+            dLdw = fmaf(Gd[(long long)p.target * C + c] * gscale,
+                        Cc[(long long)p.src * C + c] - Cc[(long long)p.target * C + c], dLdw);
         const float dLdt = dLdw * p.sign * boost;
         const float den = p.eF - p.eO;
         const float inv2 = 1.0f / (den * den);
@@ -302,13 +368,16 @@ __device__ __forceinline__ void aa_bwd_terms(const float4* R, const float* Cc, c
 }
 
 // Colour gradient of channel c of a pixel from its terms (slot order).
-__device__ __forceinline__ float aa_bwd_channel(const AATerms& at, const float* Gd, int C, int pix, int c) {
-    const float gs = Gd[(long long)pix * C + c];
+// gscale multiplies every incoming gradient as it is read (a loss gradient
+// applied on the fly; 1 leaves them unchanged).
+__device__ __forceinline__ float aa_bwd_channel(const AATerms& at, const float* Gd, int C, int pix, int c,
+                                                float gscale = 1.0f) {
+    const float gs = Gd[(long long)pix * C + c] * gscale;
     float v = gs;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         if (at.role[q] == 1) v = fmaf(-at.wt[q], gs, v);
-        else if (at.role[q] == 2) v = fmaf(at.wt[q], Gd[(long long)at.tgt[q] * C + c], v);
+        else if (at.role[q] == 2) v = fmaf(at.wt[q], Gd[(long long)at.tgt[q] * C + c] * gscale, v);
     }
     return v;
 }

@@ -21,8 +21,12 @@ namespace drp {
 
 // ---------------------------------------------------------------------------
 // Topology: open-addressing hash of undirected edges -> the (at most two)
-// triangle edges that use it.  nbr[3t + k] = triangle across edge k (the edge
-// between vertices k+1 and k+2) when exactly two distinct triangles share it.
+// triangle edges that use it.  When exactly two distinct triangles share the
+// edge k of triangle t (between its vertices k+1 and k+2), opp[3t + k] is the
+// other triangle's vertex opposite that edge -- tri[e'] for the other
+// triangle edge e' = 3t' + k', since vertex k' is opposite edge k' -- else -1.
+// The silhouette test needs only that vertex, so the per-view triangle setup
+// reads one index per edge instead of the neighbour's three.
 // ---------------------------------------------------------------------------
 static inline unsigned long long topo_capacity(long long F) {
     unsigned long long need = (unsigned long long)max(1ll, 6 * F);
@@ -89,7 +93,7 @@ __global__ void topo_resolve_kernel(const int* tri, long long F, const unsigned 
                 if (cnt[h] == 2) {
                     const int s0 = slots[2 * h], s1 = slots[2 * h + 1];
                     const int other = (s0 == (int)e) ? s1 : s0;
-                    if (other / 3 != (int)t) out = other / 3;
+                    if (other / 3 != (int)t) out = tri[other];
                 }
                 break;
             }

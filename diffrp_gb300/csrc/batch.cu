@@ -42,6 +42,14 @@ struct BatchArgs {
     float* rast;
     float* color;
     float* out;
+    bool emit_out;          // the fine raster also writes the colour into out
+    // fused mean-absolute-error loss (null target: none)
+    const float* target;
+    float l1_scale;
+    float* l1_grad;
+    float* block_loss;      // one partial per pixel block
+    float* loss;
+    const float* grad_scale;  // backward: device scalar multiplying grad_out, or null
     const float* grad_out;
     float* grad_pos;
     float* grad_attr;
@@ -229,7 +237,7 @@ batch_fine_kernel(BatchArgs a) {
         e.C = it.channels;
         e.rast = reinterpret_cast<float4*>(a.rast) + it.pixel_offset;
         e.color = a.color + it.image_offset;
-        e.out = a.out ? a.out + it.image_offset : nullptr;
+        e.out = a.emit_out ? a.out + it.image_offset : nullptr;
         e.vec = (it.channels & 3) == 0 && ((reinterpret_cast<uintptr_t>(e.A) | reinterpret_cast<uintptr_t>(e.color) |
                                             reinterpret_cast<uintptr_t>(e.out)) & 15) == 0;
         fine_tile<TILE_LOG2, TPT>(ft, e);
@@ -257,6 +265,34 @@ __global__ void __launch_bounds__(256) batch_aa_fwd_kernel(BatchArgs a) {
                         it.height, it.channels, pix, a.out + it.image_offset + (long long)pix * it.channels);
 }
 
+// Antialias forward with the mean-absolute-error loss fused: every pixel's
+// output (written when out is set), sign gradient and |error| sum; one
+// partial per 256-pixel block, reduced in a fixed order (reproducible).
+__global__ void __launch_bounds__(256) batch_aa_l1_kernel(BatchArgs a) {
+    __shared__ float warp_sum[8];
+    const int2 blk = a.pix_blocks[blockIdx.x];
+    const drp_batch_item& it = a.items[blk.x];
+    const int pix = blk.y * 256 + threadIdx.x;
+    float s = 0.0f;
+    if (pix < it.width * it.height) {
+        const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
+        const long long row = it.image_offset + (long long)pix * it.channels;
+        s = aa_fwd_pixel_l1(R, a.color + it.image_offset, a.aa_rec + it.prim_offset * 2, it.tri_count, it.width,
+                            it.height, it.channels, pix, a.target + row, a.l1_scale, a.out ? a.out + row : nullptr,
+                            a.l1_grad + row);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.0f;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) t += warp_sum[w];
+        a.block_loss[blockIdx.x] = t;
+    }
+}
+
 // Fused backward of one pixel: antialias colour gradient -> interpolation
 // backward (attribute gradients, d/du, d/dv) -> rasterisation backward
 // (vertex gradients).  Warps never straddle items (256-pixel blocks).
@@ -276,12 +312,15 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
     float* GA = a.grad_attr + it.attr_offset;
     const float4* rec = a.aa_rec + it.prim_offset * 2;
 
+    // incoming gradients are multiplied by gsc as they are read (a fused
+    // loss's upstream gradient; exactly 1 otherwise)
+    const float gsc = a.grad_scale ? *a.grad_scale : 1.0f;
     AATerms at;
     at.any = false;
     int t = -1, i0 = 0, i1 = 0, i2 = 0;
     float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
     if (in) {
-        aa_bwd_terms(R, Cc, Gd, rec, it.tri_count, W, H, C, P, tri, GP, 1.0f, pix, at);
+        aa_bwd_terms(R, Cc, Gd, rec, it.tri_count, W, H, C, P, tri, GP, 1.0f, pix, at, gsc);
         r = R[pix];
         t = checked_tri(r.w, tri, it.tri_count, it.num_vertices, i0, i1, i2);
     }
@@ -299,7 +338,7 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
             const float4 q0 = __ldg(reinterpret_cast<const float4*>(A + (long long)i0 * C + c0));
             const float4 q1 = __ldg(reinterpret_cast<const float4*>(A + (long long)i1 * C + c0));
             const float4 q2 = __ldg(reinterpret_cast<const float4*>(A + (long long)i2 * C + c0));
-            g[0] = gq.x; g[1] = gq.y; g[2] = gq.z; g[3] = gq.w;
+            g[0] = gq.x * gsc; g[1] = gq.y * gsc; g[2] = gq.z * gsc; g[3] = gq.w * gsc;
             x0[0] = q0.x; x0[1] = q0.y; x0[2] = q0.z; x0[3] = q0.w;
             x1[0] = q1.x; x1[1] = q1.y; x1[2] = q1.z; x1[3] = q1.w;
             x2[0] = q2.x; x2[1] = q2.y; x2[2] = q2.z; x2[3] = q2.w;
@@ -307,7 +346,7 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int c = c0 + k < C ? c0 + k : C - 1;
-                g[k] = c0 + k < C ? Gd[(long long)pix * C + c] : 0.f;
+                g[k] = c0 + k < C ? Gd[(long long)pix * C + c] * gsc : 0.f;
                 x0[k] = A[(long long)i0 * C + c];
                 x1[k] = A[(long long)i1 * C + c];
                 x2[k] = A[(long long)i2 * C + c];
@@ -323,7 +362,7 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
             if (at.any) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
-                    if (c0 + k < C) g[k] = aa_bwd_channel(at, Gd, C, pix, c0 + k);
+                    if (c0 + k < C) g[k] = aa_bwd_channel(at, Gd, C, pix, c0 + k, gsc);
             }
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -469,8 +508,16 @@ int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream
     case 5: launch_batch_raster<5>(a, s); break;
     default: launch_batch_raster<4>(a, s); break;
     }
-    if (!a.out) return 0;  // raster + interpolation only (recomputing them for the backward)
     // (the antialias triangle records were written by the setup / count pass)
+    if (a.target) {
+        if (a.n_pix_blocks > 0) {
+            batch_aa_l1_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+            drp_note_launch();
+        }
+        launch_l1_final(a.block_loss, a.n_pix_blocks, a.l1_scale, a.loss, s);
+        return 0;
+    }
+    if (!a.out) return 0;  // raster + interpolation only (recomputing them for the backward)
     if (a.n_pix_blocks > 0) {
         batch_aa_fwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
         drp_note_launch();
@@ -621,8 +668,46 @@ DRP_API int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp
     a.rast = rast;
     a.color = color;
     a.out = out;
+    a.emit_out = out != nullptr;
     drp::launch_batch_forward(a, workspace, L, static_cast<cudaStream_t>(stream));
     return drp_check_launch("drp_batch_forward");
+}
+
+DRP_API int drp_batch_forward_l1(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
+                                 const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
+                                 long long pixel_blocks, long long total_prims, long long total_tiles,
+                                 const float* pos, const int* tri, const float* attr, const int* nbr, int tile_log2,
+                                 int threads_per_tri, unsigned long long list_capacity, unsigned bin_depth,
+                                 float* rast, float* color, float* out, const float* target, float scale,
+                                 float* grad, float* block_loss, float* loss, void* stream) {
+    drp::BatchArgs a;
+    drp::BatchLayout L;
+    int st = batch_common(workspace, workspace_bytes, items, num_items, prim_block_map, prim_blocks, pixel_block_map,
+                          pixel_blocks, total_prims, total_tiles, list_capacity, pos, tri, attr, a, L);
+    if (st) return st;
+    if (tile_log2 < 3 || tile_log2 > 5) return bfail("batch: tile_log2 must be 3, 4 or 5");
+    if (threads_per_tri < 0 || threads_per_tri > 32 || (threads_per_tri & (threads_per_tri - 1)))
+        return bfail("batch: threads_per_tri must be 0 or a power of two <= 32");
+    if (!rast || !color || !target || !grad || !loss || (pixel_blocks > 0 && !block_loss) ||
+        (reinterpret_cast<uintptr_t>(rast) & 15))
+        return bfail("batch: bad outputs");
+    if (bin_depth && (unsigned long long)total_tiles * bin_depth > list_capacity)
+        return bfail("batch: list_capacity below total_tiles * bin_depth");
+    a.nbr = nbr;
+    a.tile_log2 = tile_log2;
+    a.tpt = threads_per_tri;
+    a.bin_depth = bin_depth;
+    a.rast = rast;
+    a.color = color;
+    a.out = out;
+    a.emit_out = false;  // the fused antialias + loss pass writes every output pixel
+    a.target = target;
+    a.l1_scale = scale;
+    a.l1_grad = grad;
+    a.block_loss = block_loss;
+    a.loss = loss;
+    drp::launch_batch_forward(a, workspace, L, static_cast<cudaStream_t>(stream));
+    return drp_check_launch("drp_batch_forward_l1");
 }
 
 DRP_API int drp_batch_backward(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
@@ -630,7 +715,7 @@ DRP_API int drp_batch_backward(void* workspace, size_t workspace_bytes, const dr
                                long long pixel_blocks, long long total_prims, long long total_tiles,
                                const float* pos, const int* tri, const float* attr, const int* nbr,
                                const float* rast, const float* color, const float* grad_out, float* grad_pos,
-                               float* grad_attr, int flags, void* stream) {
+                               float* grad_attr, const float* grad_scale, int flags, void* stream) {
     drp::BatchArgs a;
     drp::BatchLayout L;
     int st = batch_common(workspace, workspace_bytes, items, num_items, prim_block_map, prim_blocks, pixel_block_map,
@@ -644,6 +729,7 @@ DRP_API int drp_batch_backward(void* workspace, size_t workspace_bytes, const dr
     a.grad_out = grad_out;
     a.grad_pos = grad_pos;
     a.grad_attr = grad_attr;
+    a.grad_scale = grad_scale;
     if (flags & ~DRP_BATCH_REUSE_AA_RECORDS) return bfail("batch: unknown flags");
     drp::launch_batch_backward(a, workspace, L, (flags & DRP_BATCH_REUSE_AA_RECORDS) != 0,
                                static_cast<cudaStream_t>(stream));

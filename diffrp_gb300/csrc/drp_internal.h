@@ -122,6 +122,9 @@ size_t aa_ws_bytes(int B, long long F);
 int launch_aa_fwd(const AAArgs& a, cudaStream_t s);
 int launch_aa_bwd(const AAArgs& a, cudaStream_t s);
 
+// loss = scale * (sum of nblocks partial sums, added in index order in double).
+void launch_l1_final(const float* partial, long long nblocks, float scale, float* loss, cudaStream_t s);
+
 }  // namespace drp
 
 // Thread-local error message of the C ABI (capi.cu).

@@ -80,6 +80,11 @@ __global__ void __launch_bounds__(1024) l1_final_kernel(const float* partial, lo
     }
 }
 
+void launch_l1_final(const float* partial, long long nblocks, float scale, float* loss, cudaStream_t s) {
+    l1_final_kernel<<<1, 1024, 0, s>>>(partial, nblocks, scale, loss);
+    drp_note_launch();
+}
+
 // Blocks for n elements: enough to fill every SM, never more than one
 // float4 group per thread.
 static long long l1_blocks(long long n) {

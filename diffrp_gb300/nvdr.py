@@ -105,6 +105,7 @@ class RasterizeCudaContext:
         self.threads_per_tri = int(threads_per_tri)
         self.validate = bool(validate)
         self._ws = None
+        self._retired = []  # replaced buffers, kept alive for CUDA graphs captured on them
         self._capacity = 0
         self._sized = False
         self._pending = None
@@ -116,6 +117,8 @@ class RasterizeCudaContext:
     def _workspace(self, nbytes):
         if self._ws is None or self._ws.numel() < nbytes:
             n = max(nbytes, int((self._ws.numel() if self._ws is not None else 0) * 1.25))
+            if self._ws is not None:
+                self._retired.append(self._ws)  # a captured CUDA graph may still use it
             self._ws = torch.empty(n, dtype=torch.uint8, device=self.device)
         return self._ws
 
@@ -183,6 +186,8 @@ class RasterizeCudaContext:
     def topology_workspace(self, F):
         nbytes = _ffi.size_out("drp_topology_workspace_size", F)
         if self._topo_ws is None or self._topo_ws.numel() < nbytes:
+            if self._topo_ws is not None:
+                self._retired.append(self._topo_ws)
             self._topo_ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
         return self._topo_ws
 
@@ -410,11 +415,14 @@ class _Scratch(threading.local):
 
     def __init__(self):
         self.buffers = {}
+        self.retired = []  # replaced buffers, kept alive for CUDA graphs captured on them
 
     def get(self, device, name, nbytes):
         key = (device.index, name)
         buf = self.buffers.get(key)
         if buf is None or buf.numel() < nbytes:
+            if buf is not None:
+                self.retired.append(buf)
             buf = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=device)
             self.buffers[key] = buf
         return buf
@@ -424,10 +432,11 @@ _scratch = _Scratch()
 
 
 def antialias_construct_topology_hash(tri):
-    """Edge topology of ``tri``: (F, 3) int32 table of the triangle across each
-    edge (edge k joins vertices k+1 and k+2), -1 where no single neighbour
-    exists.  Pass it as ``topology_hash`` to :func:`antialias` to avoid
-    rebuilding it every call."""
+    """Edge topology of ``tri``: (F, 3) int32 table holding, for each edge
+    (edge k joins vertices k+1 and k+2), the vertex of the neighbouring
+    triangle opposite that edge, -1 where no single neighbour exists.  Pass it
+    as ``topology_hash`` to :func:`antialias` to avoid rebuilding it every
+    call."""
     _check_tensor("tri", tri, torch.int32, (2,), last=3)
     tri = tri.contiguous()
     F = tri.shape[0]

@@ -155,9 +155,11 @@ int drp_topology_workspace_size(long long num_triangles, size_t* bytes);
 
 /*
  * dr.antialias_construct_topology_hash(tri) (implicit in the dr.antialias call
- * at diffrp/rendering/surface_deferred.py:775): nbr (F, 3) int32, the
- * triangle across edge k (vertices k+1, k+2) when exactly two triangles share
- * that vertex pair, else -1.
+ * at diffrp/rendering/surface_deferred.py:775): nbr (F, 3) int32; for edge k
+ * of triangle t (vertices k+1, k+2), when exactly two triangles share that
+ * vertex pair, the other triangle's vertex opposite the edge, else -1.  (The
+ * table is opaque to diffrp, like nvdiffrast's topology hash; the
+ * silhouette test only needs the opposite vertex.)
  */
 int drp_antialias_topology(void* workspace, size_t workspace_bytes, const int* tri, long long num_triangles,
                            int* nbr, void* stream);
@@ -302,19 +304,38 @@ int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp_batch_i
                       unsigned long long list_capacity, unsigned bin_depth, float* rast, float* color, float* out,
                       void* stream);
 
+/*
+ * drp_batch_forward with the mean-absolute-error loss against target (image
+ * floats, item layout) fused into the antialias pass: out (may be NULL) gets
+ * the antialiased images, grad = sign(out - target) * scale, loss (one
+ * float, device) = scale * sum |out - target|, reduced through block_loss
+ * (pixel_blocks floats of scratch) in a fixed order.  The other arguments and
+ * the workspace are those of drp_batch_forward.  No counterpart in the
+ * reference: its L1 objective is separate PyTorch code after the render.
+ */
+int drp_batch_forward_l1(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
+                         const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
+                         long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
+                         const int* tri, const float* attr, const int* nbr, int tile_log2, int threads_per_tri,
+                         unsigned long long list_capacity, unsigned bin_depth, float* rast, float* color, float* out,
+                         const float* target, float scale, float* grad, float* block_loss, float* loss, void* stream);
+
 /* drp_batch_backward flag: the workspace still holds the antialias triangle
  * records of the last drp_batch_forward, which ran on the same positions
  * (nothing else used the workspace since): they are not recomputed. */
 #define DRP_BATCH_REUSE_AA_RECORDS 1
 
 /* Fused backward: grad_out (image floats) -> grad_pos (accumulated, pos
- * layout) and grad_attr (accumulated, attr layout).  flags: 0 or
+ * layout) and grad_attr (accumulated, attr layout).  grad_scale: NULL, or a
+ * device float every grad_out value is multiplied by as it is read (the
+ * upstream gradient of drp_batch_forward_l1's loss).  flags: 0 or
  * DRP_BATCH_REUSE_AA_RECORDS. */
 int drp_batch_backward(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
                        const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
                        long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
                        const int* tri, const float* attr, const int* nbr, const float* rast, const float* color,
-                       const float* grad_out, float* grad_pos, float* grad_attr, int flags, void* stream);
+                       const float* grad_out, float* grad_pos, float* grad_attr, const float* grad_scale, int flags,
+                       void* stream);
 
 #ifdef __cplusplus
 }

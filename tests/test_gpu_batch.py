@@ -136,6 +136,39 @@ def test_batch_fixed_depth_bins_exact(cuda_lib, depth):
         assert r._depth > 2
 
 
+@pytest.mark.parametrize("recompute", [False, True])
+@pytest.mark.parametrize("use_images", [False, True])
+def test_batch_render_l1_matches_unfused(cuda_lib, recompute, use_images):
+    """render_l1 gives the images of the plain forward bit for bit, the loss
+    of l1_loss on them (summation order aside) and the same gradients, with
+    a non-unit upstream loss gradient and, optionally, a second loss on the
+    images."""
+    from diffrp_gb300.losses import l1_loss
+    r, pos, attr, _ = _renderer(recompute=recompute)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    target = torch.rand(r.image_floats, device="cuda", generator=g)
+    w = torch.linspace(-1, 1, r.image_floats, device="cuda")
+
+    def run(fused):
+        p = pos.clone().requires_grad_(True)
+        a = attr.clone().requires_grad_(True)
+        if fused:
+            loss, img = r.render_l1(p, a, target)
+        else:
+            img = r(p, a)
+            loss = l1_loss(img, target)
+        total = 3.0 * loss + ((img * w).sum() if use_images else 0.0)
+        total.backward()
+        return loss.detach(), img.detach(), p.grad, a.grad
+
+    lf, imf, gpf, gaf = run(True)
+    lu, imu, gpu_, gau = run(False)
+    assert torch.equal(imf, imu)
+    assert torch.allclose(lf, lu, rtol=2e-6, atol=0)
+    for got, ref in [(gpf, gpu_), (gaf, gau)]:
+        assert float((got - ref).abs().max() / ref.abs().max()) <= 1e-5
+
+
 def test_batch_raster_only_forward(cuda_lib):
     """A forward without an output buffer writes the same rast and colour as
     the full forward (the antialias pass is skipped)."""
