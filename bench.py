@@ -492,16 +492,18 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None, batc
         b_gp = torch.zeros_like(clip)
         b_ga = torch.zeros_like(a_t).reshape(-1)
         flat_attr = a_t.reshape(-1)
-        ops["batch_forward"] = lambda: batch._forward_raw(clip, flat_attr, b_rast, b_color, b_out)
+        b_flags = batch._flags()
+        ops["batch_forward"] = lambda: batch._forward_raw(clip, flat_attr, b_rast, b_color, b_out, flags=b_flags)
         b_target = torch.from_numpy(target).to(dev).reshape(-1)
         b_grad = torch.empty_like(b_color)
         b_blocks = torch.empty(max(1, batch.pixel_blocks), dtype=torch.float32, device=dev)
         b_loss = torch.empty((), dtype=torch.float32, device=dev)
         ops["batch_forward_l1"] = lambda: batch._forward_raw(
-            clip, flat_attr, b_rast, b_color, b_out, (b_target, 1.0 / b_color.numel(), b_grad, b_blocks, b_loss))
-        # the step's backward reuses the antialias records of its forward
+            clip, flat_attr, b_rast, b_color, b_out, (b_target, 1.0 / b_color.numel(), b_grad, b_blocks, b_loss),
+            flags=b_flags)
+        # the step's backward reuses the antialias records and slot bits of its forward
         ops["batch_backward"] = lambda: batch._backward_raw(clip, flat_attr, b_rast, b_color, b_g, b_gp, b_ga,
-                                                            batch._fwd_gen)
+                                                            batch._fwd_gen, aa_flags=b_flags)
     P = H * W
     # Algorithmic bytes per launch: every input read once, every output written once.
     algo = {

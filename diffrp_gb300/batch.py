@@ -49,11 +49,13 @@ def _register():
         "drp_batch_plan": [P, I, I, P],
         "drp_batch_block_maps": [P, I, P, P],
         "drp_batch_workspace_size": [LL, LL, ULL, ctypes.POINTER(ctypes.c_size_t)],
+        "drp_batch_aa_state_size": [LL, ctypes.POINTER(ctypes.c_size_t)],
         "drp_batch_forward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, I, I, ULL, ctypes.c_uint,
-                              P, P, P, P],
+                              P, P, P, P, LL, P],
         "drp_batch_forward_l1": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, I, I, ULL,
-                                 ctypes.c_uint, P, P, P, P, ctypes.c_float, P, P, P, P],
-        "drp_batch_backward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, P, P, P, P, P, P, I, P],
+                                 ctypes.c_uint, P, P, P, P, LL, P, ctypes.c_float, P, P, P, P],
+        "drp_batch_backward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, P, P, P, LL, P, P, P, P,
+                               P, I, P],
     }
     for name, args in sigs.items():
         fn = getattr(lib, name)
@@ -217,10 +219,11 @@ class BatchRenderer:
         ev.record(torch.cuda.current_stream(self.device))
         self._pending = ev
 
-    def _forward_raw(self, pos, attr, rast, color, out, l1=None):
+    def _forward_raw(self, pos, attr, rast, color, out, l1=None, flags=None):
         """out=None writes rast and colour only (no antialias pass).  l1 =
         (target, scale, grad, block_loss, loss) fuses the L1 loss into the
-        antialias pass (drp_batch_forward_l1)."""
+        antialias pass (drp_batch_forward_l1).  flags: an antialias state
+        block (_flags()) the forward fills for its backward, or None."""
         if not torch.cuda.is_current_stream_capturing():
             self._poll_stats()
         first = not self._capacity
@@ -230,6 +233,8 @@ class BatchRenderer:
         else:
             cap = self._capacity if self._capacity else 4 * self.total_prims + 4096
         optr = None if out is None else out.data_ptr()
+        fptr = None if flags is None else flags.data_ptr()
+        npix = self.total_pixels
         self._fwd_gen += 1
         ws = self._workspace(cap)
         stream = torch.cuda.current_stream(self.device).cuda_stream
@@ -245,7 +250,7 @@ class BatchRenderer:
             tail = (stream,)
             entry = "drp_batch_forward"
         _ffi.call(entry, ws.data_ptr(), ws.numel(), *args, cap, depth, rast.data_ptr(), color.data_ptr(), optr,
-                  *tail)
+                  fptr, npix, *tail)
         if first:
             # exact lists, sized synchronously; they also give the largest tile
             torch.cuda.current_stream(self.device).synchronize()
@@ -260,28 +265,39 @@ class BatchRenderer:
             if needed > cap:
                 ws = self._workspace(self._capacity)
                 _ffi.call(entry, ws.data_ptr(), ws.numel(), *args, self._capacity, 0, rast.data_ptr(),
-                          color.data_ptr(), optr, *tail)
+                          color.data_ptr(), optr, fptr, npix, *tail)
         else:
             self._queue_stats(ws)
         self._rec_ws = ws
 
-    def _backward_raw(self, pos, attr, rast, color, grad_out, grad_pos, grad_attr, gen=None, grad_scale=None):
+    def _backward_raw(self, pos, attr, rast, color, grad_out, grad_pos, grad_attr, gen=None, grad_scale=None,
+                      aa_flags=None):
         """gen: the forward generation that produced rast / colour from pos;
         when it is still the latest, its antialias records are reused.
-        grad_scale: a one-element device tensor multiplying grad_out."""
+        grad_scale: a one-element device tensor multiplying grad_out.
+        aa_flags: the antialias slot bits that forward wrote, or None."""
         ws = self._workspace(0)  # the backward reads no tile list
         stream = torch.cuda.current_stream(self.device).cuda_stream
         flags = REUSE_AA_RECORDS if gen is not None and gen == self._fwd_gen and ws is self._rec_ws else 0
+        aa_grad = None if aa_flags is None else torch.empty(self.image_floats, dtype=torch.float32,
+                                                            device=self.device)
         _ffi.call("drp_batch_backward", ws.data_ptr(), ws.numel(), self._items_dev.data_ptr(), len(self.items),
                   self._pmap.data_ptr(), self.prim_blocks, self._xmap.data_ptr(), self.pixel_blocks,
                   self.total_prims, self.total_tiles, pos.data_ptr(), self.tri.data_ptr(), attr.data_ptr(),
-                  self.nbr.data_ptr(), rast.data_ptr(), color.data_ptr(), grad_out.data_ptr(), grad_pos.data_ptr(),
+                  self.nbr.data_ptr(), rast.data_ptr(), color.data_ptr(), None if aa_flags is None else aa_flags.data_ptr(),
+                  self.total_pixels, None if aa_grad is None else aa_grad.data_ptr(), grad_out.data_ptr(),
+                  grad_pos.data_ptr(),
                   grad_attr.data_ptr(), None if grad_scale is None else grad_scale.data_ptr(), flags, stream)
 
     def _buffers(self):
         rast = torch.empty((self.total_pixels, 4), dtype=torch.float32, device=self.device)
         color = torch.empty(self.image_floats, dtype=torch.float32, device=self.device)
         return rast, color
+
+    def _flags(self):
+        """The antialias state block one forward fills for its backward."""
+        n = _ffi.size_out("drp_batch_aa_state_size", self.total_pixels)
+        return torch.empty(n, dtype=torch.uint8, device=self.device)
 
     def __call__(self, pos, attr):
         """pos: packed (rows, 4) clip positions; attr: packed attribute floats.
@@ -321,29 +337,30 @@ class _BatchFn(torch.autograd.Function):
     def forward(ctx, pos, attr, renderer):
         rast, color = renderer._buffers()
         out = torch.empty_like(color)
-        renderer._forward_raw(pos, attr, rast, color, out)
+        flags = renderer._flags()
+        renderer._forward_raw(pos, attr, rast, color, out, flags=flags)
         ctx.renderer = renderer
         ctx.gen = renderer._fwd_gen
         if renderer.recompute:
-            ctx.save_for_backward(pos, attr)
+            ctx.save_for_backward(pos, attr, flags)
         else:
-            ctx.save_for_backward(pos, attr, rast, color)
+            ctx.save_for_backward(pos, attr, flags, rast, color)
         return out
 
     @staticmethod
     def backward(ctx, grad_out):
         r = ctx.renderer
         if r.recompute:
-            pos, attr = ctx.saved_tensors
+            pos, attr, flags = ctx.saved_tensors
             rast, color = r._buffers()
             r._forward_raw(pos, attr, rast, color, None)
             gen = r._fwd_gen
         else:
-            pos, attr, rast, color = ctx.saved_tensors
+            pos, attr, flags, rast, color = ctx.saved_tensors
             gen = ctx.gen
         grad_pos = torch.zeros_like(pos)
         grad_attr = torch.zeros_like(attr)
-        r._backward_raw(pos, attr, rast, color, grad_out.contiguous(), grad_pos, grad_attr, gen)
+        r._backward_raw(pos, attr, rast, color, grad_out.contiguous(), grad_pos, grad_attr, gen, aa_flags=flags)
         return grad_pos, grad_attr, None
 
 
@@ -356,26 +373,27 @@ class _BatchL1Fn(torch.autograd.Function):
         grad = torch.empty_like(color)
         block_loss = torch.empty(max(1, renderer.pixel_blocks), dtype=torch.float32, device=pos.device)
         loss = torch.empty((), dtype=torch.float32, device=pos.device)
+        flags = renderer._flags()
         renderer._forward_raw(pos, attr, rast, color, out,
-                              (target, 1.0 / renderer.image_floats, grad, block_loss, loss))
+                              (target, 1.0 / renderer.image_floats, grad, block_loss, loss), flags=flags)
         ctx.renderer = renderer
         ctx.gen = renderer._fwd_gen
         if renderer.recompute:
-            ctx.save_for_backward(pos, attr, grad)
+            ctx.save_for_backward(pos, attr, grad, flags)
         else:
-            ctx.save_for_backward(pos, attr, grad, rast, color)
+            ctx.save_for_backward(pos, attr, grad, flags, rast, color)
         return loss, out
 
     @staticmethod
     def backward(ctx, g_loss, g_out):
         r = ctx.renderer
         if r.recompute:
-            pos, attr, grad = ctx.saved_tensors
+            pos, attr, grad, flags = ctx.saved_tensors
             rast, color = r._buffers()
             r._forward_raw(pos, attr, rast, color, None)
             gen = r._fwd_gen
         else:
-            pos, attr, grad, rast, color = ctx.saved_tensors
+            pos, attr, grad, flags, rast, color = ctx.saved_tensors
             gen = ctx.gen
         grad_pos = torch.zeros_like(pos)
         grad_attr = torch.zeros_like(attr)
@@ -389,5 +407,5 @@ class _BatchL1Fn(torch.autograd.Function):
             gout = g_out.contiguous()
         else:
             gout = (grad * g_loss + g_out).contiguous()
-        r._backward_raw(pos, attr, rast, color, gout, grad_pos, grad_attr, gen, scale)
+        r._backward_raw(pos, attr, rast, color, gout, grad_pos, grad_attr, gen, scale, aa_flags=flags)
         return grad_pos, grad_attr, None, None

@@ -182,9 +182,11 @@ __device__ __forceinline__ void copy_channels(const float* src, float* dst, int 
 // Blend terms of one pixel: for each pair slot (left, right, below, above)
 // whose pair blends into this pixel, the source pixel and its weight.  The
 // pixel's and its four neighbours' rast rows are loaded together, before any
-// of them is used.  Returns whether any slot blends.
+// of them is used.  Returns whether any slot blends.  pair_bits (may be null)
+// gets bit q set when slot q's pair blends in either direction -- the pixels
+// the antialias backward has to visit.
 __device__ __forceinline__ bool aa_fwd_terms(const float4* R, const float4* rec, long long F, int W, int H, int pix,
-                                             int (&src)[4], float (&wt)[4]) {
+                                             int (&src)[4], float (&wt)[4], unsigned* pair_bits = nullptr) {
     const int py = pix / W, px = pix - py * W;
     int A[4], B[4], ax[4], ay[4];
     bool vert[4], has[4];
@@ -196,6 +198,7 @@ __device__ __forceinline__ bool aa_fwd_terms(const float4* R, const float4* rec,
         if (has[q]) rn[q] = R[A[q] == pix ? B[q] : A[q]];
     }
     bool any = false;
+    unsigned bits = 0;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         src[q] = -1;
@@ -204,26 +207,29 @@ __device__ __forceinline__ bool aa_fwd_terms(const float4* R, const float4* rec,
         AAPair pr;
         const bool first = A[q] == pix;
         aa_pair(rec, F, A[q], B[q], ax[q], ay[q], vert[q], first ? rs : rn[q], first ? rn[q] : rs, pr);
+        if (pr.valid) bits |= 1u << q;
         if (pr.valid && pr.target == pix) {
             src[q] = pr.src;
             wt[q] = pr.w;
             any = true;
         }
     }
+    if (pair_bits) *pair_bits = bits;
     return any;
 }
 
 // Forward of one pixel: out = c + sum over pair slots targeting this pixel of
 // w (c[src] - c), in slot order (fmaf).  R, Cc: the view's rast and colour.
 // COPY = false: o already holds c (the caller wrote it), so pixels without a
-// blend are left untouched.
+// blend are left untouched.  pair_bits: as aa_fwd_terms.
 template <bool COPY>
 __device__ __forceinline__ void aa_fwd_pixel(const float4* R, const float* Cc, const float4* rec, long long F, int W,
-                                             int H, int C, int pix, float* o) {
+                                             int H, int C, int pix, float* o, unsigned* pair_bits = nullptr) {
     const float* cs = Cc + (long long)pix * C;
     int src[4];
     float wt[4];
-    if (!aa_fwd_terms(R, rec, F, W, H, pix, src, wt)) {
+    const bool any = aa_fwd_terms(R, rec, F, W, H, pix, src, wt, pair_bits);
+    if (!any) {
         if (COPY) copy_channels(cs, o, C);
         return;
     }
@@ -245,14 +251,14 @@ __device__ __forceinline__ float l1_sign(float d, float scale) {
 // value of every channel as aa_fwd_pixel computes it (written to o when o is
 // not null), g = sign(out - target) * scale, and the return value is the
 // pixel's sum of |out - target| in channel order.  tg, o, g: this pixel's
-// target, output and gradient rows.
+// target, output and gradient rows; pair_bits: as aa_fwd_terms.
 __device__ __forceinline__ float aa_fwd_pixel_l1(const float4* R, const float* Cc, const float4* rec, long long F,
                                                  int W, int H, int C, int pix, const float* tg, float scale, float* o,
-                                                 float* g) {
+                                                 float* g, unsigned* pair_bits = nullptr) {
     const float* cs = Cc + (long long)pix * C;
     int src[4];
     float wt[4];
-    const bool any = aa_fwd_terms(R, rec, F, W, H, pix, src, wt);
+    const bool any = aa_fwd_terms(R, rec, F, W, H, pix, src, wt, pair_bits);
     float s = 0.0f;
     const bool vec = (C & 3) == 0 &&
                      (((uintptr_t)cs | (uintptr_t)tg | (uintptr_t)g | (uintptr_t)(o ? o : g)) & 15) == 0;

@@ -42,6 +42,12 @@ struct BatchArgs {
     float* rast;
     float* color;
     float* out;
+    // antialias state (forward writes, backward reads): per pixel whether a
+    // blending pair touches it, and the list of those pixels
+    unsigned char* aa_flags;
+    int* aa_list;
+    unsigned* aa_count;
+    float* aa_grad;           // backward scratch: antialiased colour gradient of listed pixels
     bool emit_out;          // the fine raster also writes the colour into out
     // fused mean-absolute-error loss (null target: none)
     const float* target;
@@ -254,33 +260,59 @@ __global__ void __launch_bounds__(256) batch_aa_setup_kernel(BatchArgs a) {
                   it.tri_count, it.num_vertices, it.width, it.height, a.aa_rec + (it.prim_offset + j) * 2);
 }
 
+// Record a pixel some blending pair touches: its flag, and (warp-aggregated)
+// its global index in the list the antialias backward walks.  All 32 lanes
+// of the warp call it.
+__device__ __forceinline__ void aa_note_pixel(const BatchArgs& a, long long gpix, bool in, unsigned bits) {
+    if (!a.aa_flags) return;
+    if (in) a.aa_flags[gpix] = bits ? 1 : 0;
+    const bool need = in && bits != 0u;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(a.aa_count, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (need) a.aa_list[base + __popc(m & ((1u << lane) - 1u))] = (int)gpix;
+}
+
 __global__ void __launch_bounds__(256) batch_aa_fwd_kernel(BatchArgs a) {
     const int2 blk = a.pix_blocks[blockIdx.x];
     const drp_batch_item& it = a.items[blk.x];
     const int pix = blk.y * 256 + threadIdx.x;
-    if (pix >= it.width * it.height) return;
-    const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
-    // out already holds the colour (written by the fine raster): only blended pixels change
-    aa_fwd_pixel<false>(R, a.color + it.image_offset, a.aa_rec + it.prim_offset * 2, it.tri_count, it.width,
-                        it.height, it.channels, pix, a.out + it.image_offset + (long long)pix * it.channels);
+    const bool in = pix < it.width * it.height;
+    unsigned bits = 0;
+    if (in) {
+        const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
+        // out already holds the colour (written by the fine raster): only blended pixels change
+        aa_fwd_pixel<false>(R, a.color + it.image_offset, a.aa_rec + it.prim_offset * 2, it.tri_count, it.width,
+                            it.height, it.channels, pix, a.out + it.image_offset + (long long)pix * it.channels,
+                            &bits);
+    }
+    aa_note_pixel(a, it.pixel_offset + pix, in, bits);
 }
 
 // Antialias forward with the mean-absolute-error loss fused: every pixel's
 // output (written when out is set), sign gradient and |error| sum; one
-// partial per 256-pixel block, reduced in a fixed order (reproducible).
+// partial per 256-pixel block, added in index order by the final reduction
+// (reproducible loss).
 __global__ void __launch_bounds__(256) batch_aa_l1_kernel(BatchArgs a) {
     __shared__ float warp_sum[8];
     const int2 blk = a.pix_blocks[blockIdx.x];
     const drp_batch_item& it = a.items[blk.x];
     const int pix = blk.y * 256 + threadIdx.x;
     float s = 0.0f;
-    if (pix < it.width * it.height) {
+    const bool in = pix < it.width * it.height;
+    unsigned bits = 0;
+    if (in) {
         const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
         const long long row = it.image_offset + (long long)pix * it.channels;
         s = aa_fwd_pixel_l1(R, a.color + it.image_offset, a.aa_rec + it.prim_offset * 2, it.tri_count, it.width,
                             it.height, it.channels, pix, a.target + row, a.l1_scale, a.out ? a.out + row : nullptr,
-                            a.l1_grad + row);
+                            a.l1_grad + row, &bits);
     }
+    aa_note_pixel(a, it.pixel_offset + pix, in, bits);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
     if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = s;
@@ -290,6 +322,39 @@ __global__ void __launch_bounds__(256) batch_aa_l1_kernel(BatchArgs a) {
 #pragma unroll
         for (int w = 0; w < 8; ++w) t += warp_sum[w];
         a.block_loss[blockIdx.x] = t;
+    }
+}
+
+__device__ __forceinline__ int find_item_by_pixel(const drp_batch_item* items, int n, long long gpix) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (items[mid].pixel_offset <= gpix) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Antialias backward of the listed pixels (those a blending pair touches,
+// about the silhouettes): edge-vertex gradients (scattered once per pair by
+// its first pixel) and the pixel's antialiased colour gradient into aa_grad.
+// Grid-stride over the device-side count, so the launch needs no host sync.
+__global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
+    const unsigned n = *a.aa_count;
+    const float gsc = a.grad_scale ? *a.grad_scale : 1.0f;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long gpix = a.aa_list[i];
+        const drp_batch_item& it = a.items[find_item_by_pixel(a.items, a.num_items, gpix)];
+        const int pix = (int)(gpix - it.pixel_offset);
+        const int C = it.channels;
+        const float* Gd = a.grad_out + it.image_offset;
+        AATerms at;
+        aa_bwd_terms(reinterpret_cast<const float4*>(a.rast) + it.pixel_offset, a.color + it.image_offset, Gd,
+                     a.aa_rec + it.prim_offset * 2, it.tri_count, it.width, it.height, C,
+                     reinterpret_cast<const float4*>(a.pos) + it.pos_offset, a.tri + 3 * (long long)it.tri_first,
+                     reinterpret_cast<float4*>(a.grad_pos) + it.pos_offset, 1.0f, pix, at, gsc);
+        float* g2 = a.aa_grad + it.image_offset + (long long)pix * C;
+        for (int c = 0; c < C; ++c) g2[c] = aa_bwd_channel(at, Gd, C, pix, c, gsc);
     }
 }
 
@@ -319,8 +384,14 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
     at.any = false;
     int t = -1, i0 = 0, i1 = 0, i2 = 0;
     float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    // With the forward's antialias state, the pixels a blend touches were
+    // handled by batch_aa_bwd_kernel: their antialiased colour gradient is in
+    // aa_grad (already scaled).  Without it the terms are evaluated here.
+    const bool flagged = in && a.aa_flags && a.aa_flags[it.pixel_offset + pix];
+    const float* Gsrc = flagged ? a.aa_grad + it.image_offset : Gd;
+    const float gmul = flagged ? 1.0f : gsc;
     if (in) {
-        aa_bwd_terms(R, Cc, Gd, rec, it.tri_count, W, H, C, P, tri, GP, 1.0f, pix, at, gsc);
+        if (!a.aa_flags) aa_bwd_terms(R, Cc, Gd, rec, it.tri_count, W, H, C, P, tri, GP, 1.0f, pix, at, gsc);
         r = R[pix];
         t = checked_tri(r.w, tri, it.tri_count, it.num_vertices, i0, i1, i2);
     }
@@ -328,17 +399,17 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
     const float u = r.x, v = r.y, w = 1.0f - u - v;
     float gu = 0.f, gv = 0.f;
     const bool vec = (C & 3) == 0 && ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(GA) |
-                                       reinterpret_cast<uintptr_t>(Gd)) & 15) == 0;
+                                       reinterpret_cast<uintptr_t>(Gsrc)) & 15) == 0;
     // Channel groups of 4: the next group's loads are issued before this
     // group's reduction and atomics, which would otherwise hold them back.
     float g[4], x0[4], x1[4], x2[4];
     auto load_group = [&](int c0) {
         if (vec) {
-            const float4 gq = __ldg(reinterpret_cast<const float4*>(Gd + (long long)pix * C + c0));
+            const float4 gq = __ldg(reinterpret_cast<const float4*>(Gsrc + (long long)pix * C + c0));
             const float4 q0 = __ldg(reinterpret_cast<const float4*>(A + (long long)i0 * C + c0));
             const float4 q1 = __ldg(reinterpret_cast<const float4*>(A + (long long)i1 * C + c0));
             const float4 q2 = __ldg(reinterpret_cast<const float4*>(A + (long long)i2 * C + c0));
-            g[0] = gq.x * gsc; g[1] = gq.y * gsc; g[2] = gq.z * gsc; g[3] = gq.w * gsc;
+            g[0] = gq.x * gmul; g[1] = gq.y * gmul; g[2] = gq.z * gmul; g[3] = gq.w * gmul;
             x0[0] = q0.x; x0[1] = q0.y; x0[2] = q0.z; x0[3] = q0.w;
             x1[0] = q1.x; x1[1] = q1.y; x1[2] = q1.z; x1[3] = q1.w;
             x2[0] = q2.x; x2[1] = q2.y; x2[2] = q2.z; x2[3] = q2.w;
@@ -346,7 +417,7 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int c = c0 + k < C ? c0 + k : C - 1;
-                g[k] = c0 + k < C ? Gd[(long long)pix * C + c] * gsc : 0.f;
+                g[k] = c0 + k < C ? Gsrc[(long long)pix * C + c] * gmul : 0.f;
                 x0[k] = A[(long long)i0 * C + c];
                 x1[k] = A[(long long)i1 * C + c];
                 x2[k] = A[(long long)i2 * C + c];
@@ -442,6 +513,25 @@ BatchLayout batch_layout(long long total_prims, long long total_tiles, unsigned 
     return L;
 }
 
+// Antialias state block: list count at 0, per-pixel flags at 256, the pixel
+// list (int32) after them.
+static size_t aa_state_bytes(long long total_pixels, size_t* list_off) {
+    const size_t flags_end = 256 + (size_t)total_pixels;
+    const size_t lo = (flags_end + 255) / 256 * 256;
+    if (list_off) *list_off = lo;
+    return lo + (size_t)total_pixels * 4;
+}
+
+static void carve_aa_state(BatchArgs& a, void* state, long long total_pixels) {
+    if (!state) return;
+    size_t lo = 0;
+    aa_state_bytes(total_pixels, &lo);
+    char* p = static_cast<char*>(state);
+    a.aa_count = reinterpret_cast<unsigned*>(p);
+    a.aa_flags = reinterpret_cast<unsigned char*>(p + 256);
+    a.aa_list = reinterpret_cast<int*>(p + lo);
+}
+
 static void carve(BatchArgs& a, void* ws, const BatchLayout& L) {
     char* w = static_cast<char*>(ws);
     a.stats = reinterpret_cast<uint32_t*>(w + L.stats);
@@ -502,6 +592,7 @@ static void launch_batch_raster(const BatchArgs& a, cudaStream_t s) {
 int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream_t s) {
     carve(a, ws, L);
     cudaMemsetAsync(a.stats, 0, 256, s);  // stats and work queue
+    if (a.aa_count) cudaMemsetAsync(a.aa_count, 0, sizeof(unsigned), s);
     cudaMemsetAsync(a.tile_count, 0, sizeof(uint32_t) * a.total_tiles, s);
     switch (a.tile_log2) {
     case 3: launch_batch_raster<3>(a, s); break;
@@ -529,6 +620,18 @@ int launch_batch_backward(BatchArgs a, void* ws, const BatchLayout& L, bool reus
     carve(a, ws, L);
     if (a.n_prim_blocks > 0 && !reuse_records) {
         batch_aa_setup_kernel<<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+        drp_note_launch();
+    }
+    if (a.aa_flags && a.n_pix_blocks > 0) {
+        static int grid = 0;
+        if (grid == 0) {
+            int dev = 0, sms = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            grid = (sms > 0 ? sms : 1) * 4;
+        }
+        const long long g = a.n_pix_blocks < grid ? a.n_pix_blocks : grid;
+        batch_aa_bwd_kernel<<<(unsigned)g, 256, 0, s>>>(a);
         drp_note_launch();
     }
     if (a.n_pix_blocks > 0) {
@@ -603,6 +706,12 @@ DRP_API int drp_batch_block_maps(const drp_batch_item* items, int num_items, int
     return DRP_STATUS_OK;
 }
 
+DRP_API int drp_batch_aa_state_size(long long total_pixels, size_t* bytes) {
+    if (!bytes || total_pixels <= 0) return bfail("drp_batch_aa_state_size: bad arguments");
+    *bytes = drp::aa_state_bytes(total_pixels, nullptr);
+    return DRP_STATUS_OK;
+}
+
 DRP_API int drp_batch_workspace_size(long long total_prims, long long total_tiles, unsigned long long list_capacity,
                                      size_t* bytes) {
     if (!bytes || total_prims < 0 || total_tiles < 0 || list_capacity > 0x7fffffffull)
@@ -649,7 +758,7 @@ DRP_API int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp
                               long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
                               const int* tri, const float* attr, const int* nbr, int tile_log2, int threads_per_tri,
                               unsigned long long list_capacity, unsigned bin_depth, float* rast, float* color,
-                              float* out, void* stream) {
+                              float* out, void* aa_state, long long total_pixels, void* stream) {
     drp::BatchArgs a;
     drp::BatchLayout L;
     int st = batch_common(workspace, workspace_bytes, items, num_items, prim_block_map, prim_blocks, pixel_block_map,
@@ -668,6 +777,9 @@ DRP_API int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp
     a.rast = rast;
     a.color = color;
     a.out = out;
+    if (aa_state && ((reinterpret_cast<uintptr_t>(aa_state) & 255) || total_pixels <= 0))
+        return bfail("batch: aa_state must be 256-byte aligned, with total_pixels > 0");
+    carve_aa_state(a, aa_state, total_pixels);
     a.emit_out = out != nullptr;
     drp::launch_batch_forward(a, workspace, L, static_cast<cudaStream_t>(stream));
     return drp_check_launch("drp_batch_forward");
@@ -678,8 +790,9 @@ DRP_API int drp_batch_forward_l1(void* workspace, size_t workspace_bytes, const 
                                  long long pixel_blocks, long long total_prims, long long total_tiles,
                                  const float* pos, const int* tri, const float* attr, const int* nbr, int tile_log2,
                                  int threads_per_tri, unsigned long long list_capacity, unsigned bin_depth,
-                                 float* rast, float* color, float* out, const float* target, float scale,
-                                 float* grad, float* block_loss, float* loss, void* stream) {
+                                 float* rast, float* color, float* out, void* aa_state, long long total_pixels,
+                                 const float* target, float scale, float* grad, float* block_loss, float* loss,
+                                 void* stream) {
     drp::BatchArgs a;
     drp::BatchLayout L;
     int st = batch_common(workspace, workspace_bytes, items, num_items, prim_block_map, prim_blocks, pixel_block_map,
@@ -700,6 +813,9 @@ DRP_API int drp_batch_forward_l1(void* workspace, size_t workspace_bytes, const 
     a.rast = rast;
     a.color = color;
     a.out = out;
+    if (aa_state && ((reinterpret_cast<uintptr_t>(aa_state) & 255) || total_pixels <= 0))
+        return bfail("batch: aa_state must be 256-byte aligned, with total_pixels > 0");
+    carve_aa_state(a, aa_state, total_pixels);
     a.emit_out = false;  // the fused antialias + loss pass writes every output pixel
     a.target = target;
     a.l1_scale = scale;
@@ -714,8 +830,10 @@ DRP_API int drp_batch_backward(void* workspace, size_t workspace_bytes, const dr
                                const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
                                long long pixel_blocks, long long total_prims, long long total_tiles,
                                const float* pos, const int* tri, const float* attr, const int* nbr,
-                               const float* rast, const float* color, const float* grad_out, float* grad_pos,
-                               float* grad_attr, const float* grad_scale, int flags, void* stream) {
+                               const float* rast, const float* color, const void* aa_state, long long total_pixels,
+                               float* aa_grad,
+                               const float* grad_out, float* grad_pos, float* grad_attr, const float* grad_scale,
+                               int flags, void* stream) {
     drp::BatchArgs a;
     drp::BatchLayout L;
     int st = batch_common(workspace, workspace_bytes, items, num_items, prim_block_map, prim_blocks, pixel_block_map,
@@ -726,6 +844,10 @@ DRP_API int drp_batch_backward(void* workspace, size_t workspace_bytes, const dr
     a.nbr = nbr;
     a.rast = const_cast<float*>(rast);
     a.color = const_cast<float*>(color);
+    if (aa_state && ((reinterpret_cast<uintptr_t>(aa_state) & 255) || total_pixels <= 0 || !aa_grad))
+        return bfail("batch: aa_state needs 256-byte alignment, total_pixels > 0 and an aa_grad buffer");
+    carve_aa_state(a, const_cast<void*>(aa_state), total_pixels);
+    a.aa_grad = aa_grad;
     a.grad_out = grad_out;
     a.grad_pos = grad_pos;
     a.grad_attr = grad_attr;

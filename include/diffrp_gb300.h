@@ -296,13 +296,21 @@ int drp_batch_workspace_size(long long total_prims, long long total_tiles, unsig
  * a tile with more entries is still rasterised exactly (by scanning all of
  * its item's triangles), sets DRP_DEVERR_LIST_OVERFLOW (u32 at byte 8) and
  * raises the u32 at byte 12 to its count.
+ * aa_state (may be NULL; drp_batch_aa_state_size(total_pixels) bytes,
+ * 256-byte aligned): the antialias pass records there which pixels a
+ * blending pair touches (a flag per pixel and a list of them), so that
+ * drp_batch_backward evaluates the antialias terms of those pixels only.
  */
 int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
                       const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
                       long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
                       const int* tri, const float* attr, const int* nbr, int tile_log2, int threads_per_tri,
                       unsigned long long list_capacity, unsigned bin_depth, float* rast, float* color, float* out,
-                      void* stream);
+                      void* aa_state, long long total_pixels, void* stream);
+
+/* Bytes of the antialias state block of drp_batch_forward (total_pixels =
+ * totals[2] of drp_batch_plan). */
+int drp_batch_aa_state_size(long long total_pixels, size_t* bytes);
 
 /*
  * drp_batch_forward with the mean-absolute-error loss against target (image
@@ -318,7 +326,8 @@ int drp_batch_forward_l1(void* workspace, size_t workspace_bytes, const drp_batc
                          long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
                          const int* tri, const float* attr, const int* nbr, int tile_log2, int threads_per_tri,
                          unsigned long long list_capacity, unsigned bin_depth, float* rast, float* color, float* out,
-                         const float* target, float scale, float* grad, float* block_loss, float* loss, void* stream);
+                         void* aa_state, long long total_pixels, const float* target, float scale, float* grad,
+                         float* block_loss, float* loss, void* stream);
 
 /* drp_batch_backward flag: the workspace still holds the antialias triangle
  * records of the last drp_batch_forward, which ran on the same positions
@@ -326,16 +335,19 @@ int drp_batch_forward_l1(void* workspace, size_t workspace_bytes, const drp_batc
 #define DRP_BATCH_REUSE_AA_RECORDS 1
 
 /* Fused backward: grad_out (image floats) -> grad_pos (accumulated, pos
- * layout) and grad_attr (accumulated, attr layout).  grad_scale: NULL, or a
- * device float every grad_out value is multiplied by as it is read (the
- * upstream gradient of drp_batch_forward_l1's loss).  flags: 0 or
+ * layout) and grad_attr (accumulated, attr layout).  aa_state: NULL, or the
+ * block the forward filled for this rast; then aa_grad (image floats of
+ * scratch) receives the antialiased colour gradient of the listed pixels and
+ * the other pixels skip the antialias terms.  grad_scale: NULL, or a device
+ * float every grad_out value is multiplied by as it is read (the upstream
+ * gradient of drp_batch_forward_l1's loss).  flags: 0 or
  * DRP_BATCH_REUSE_AA_RECORDS. */
 int drp_batch_backward(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
                        const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
                        long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
                        const int* tri, const float* attr, const int* nbr, const float* rast, const float* color,
-                       const float* grad_out, float* grad_pos, float* grad_attr, const float* grad_scale, int flags,
-                       void* stream);
+                       const void* aa_state, long long total_pixels, float* aa_grad, const float* grad_out,
+                       float* grad_pos, float* grad_attr, const float* grad_scale, int flags, void* stream);
 
 #ifdef __cplusplus
 }
