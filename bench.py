@@ -469,17 +469,18 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None, batc
     grast = torch.empty_like(rast)
     out = torch.empty_like(col)
     aws = torch.empty(_ffi.size_out("drp_antialias_workspace_size", 1, F), dtype=torch.uint8, device=dev)
+    astate = torch.empty(_ffi.size_out("drp_antialias_state_size", 1, H, W), dtype=torch.uint8, device=dev)
     ops = {
         "rasterize_fwd": lambda: ctx._raster_call(clip, tri, None, 1, F, H, W, 0, None, rast, None, None),
         "interpolate_fwd": lambda: _ffi.call("drp_interpolate_fwd", a_t.data_ptr(), 0, V, C, rast.data_ptr(), None,
                                              tri.data_ptr(), F, 1, H, W, None, 0, out.data_ptr(), None, sp),
         "antialias_fwd": lambda: _ffi.call("drp_antialias_fwd", aws.data_ptr(), aws.numel(), col.data_ptr(), C,
                                            rast.data_ptr(), clip.data_ptr(), 0, V, tri.data_ptr(), F,
-                                           topo.data_ptr(), 1, H, W, out.data_ptr(), sp),
+                                           topo.data_ptr(), 1, H, W, out.data_ptr(), astate.data_ptr(), sp),
         "antialias_bwd": lambda: _ffi.call("drp_antialias_bwd", aws.data_ptr(), aws.numel(), col.data_ptr(), C,
                                            rast.data_ptr(), clip.data_ptr(), 0, V, tri.data_ptr(), F,
                                            topo.data_ptr(), 1, H, W, g.data_ptr(), 1.0, gcol.data_ptr(),
-                                           gpos.data_ptr(), sp),
+                                           gpos.data_ptr(), astate.data_ptr(), sp),
         "interpolate_bwd": lambda: _ffi.call("drp_interpolate_bwd", a_t.data_ptr(), 0, V, C, rast.data_ptr(), None,
                                              tri.data_ptr(), F, 1, H, W, None, 0, gcol.data_ptr(), None,
                                              gattr.data_ptr(), grast.data_ptr(), None, sp),

@@ -32,9 +32,10 @@ _SIGNATURES = {
     "drp_l1_loss_workspace_size": [_LL, _SZ],
     "drp_l1_loss_fwd": [_P, ctypes.c_size_t, _P, _P, _LL, _F, _P, _P, _P],
     "drp_antialias_fwd_noalloc": [_P, _I, _P, _P, _LL, _LL, _P, _LL, _P, _I, _I, _I, _P, _P],
-    "drp_antialias_fwd": [_P, ctypes.c_size_t, _P, _I, _P, _P, _LL, _LL, _P, _LL, _P, _I, _I, _I, _P, _P],
+    "drp_antialias_state_size": [_I, _I, _I, _SZ],
+    "drp_antialias_fwd": [_P, ctypes.c_size_t, _P, _I, _P, _P, _LL, _LL, _P, _LL, _P, _I, _I, _I, _P, _P, _P],
     "drp_antialias_bwd": [_P, ctypes.c_size_t, _P, _I, _P, _P, _LL, _LL, _P, _LL, _P, _I, _I, _I, _P, _F, _P, _P,
-                          _P],
+                          _P, _P],
 }
 
 ABI_VERSION = 1

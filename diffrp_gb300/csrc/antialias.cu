@@ -135,11 +135,60 @@ __global__ void __launch_bounds__(256) aa_fwd_kernel(AAArgs a) {
     const int b = blockIdx.y;
     const int npix = a.H * a.W;
     const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= npix) return;
-    const float4* R = reinterpret_cast<const float4*>(a.rast) + (long long)b * npix;
-    const float* Cc = a.color + (long long)b * npix * a.C;
-    const float4* rec = reinterpret_cast<const float4*>(a.tri_rec) + (long long)b * a.num_triangles * 2;
-    aa_fwd_pixel<true>(R, Cc, rec, a.num_triangles, a.W, a.H, a.C, pix, a.out + ((long long)b * npix + pix) * a.C);
+    const bool in = pix < npix;
+    unsigned bits = 0;
+    if (in) {
+        const float4* R = reinterpret_cast<const float4*>(a.rast) + (long long)b * npix;
+        const float* Cc = a.color + (long long)b * npix * a.C;
+        const float4* rec = reinterpret_cast<const float4*>(a.tri_rec) + (long long)b * a.num_triangles * 2;
+        aa_fwd_pixel<true>(R, Cc, rec, a.num_triangles, a.W, a.H, a.C, pix,
+                           a.out + ((long long)b * npix + pix) * a.C, &bits);
+    }
+    if (!a.list) return;
+    // warp-aggregated append of the pixels some blending pair touches
+    const bool need = in && bits != 0u;
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(a.list_count, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (need) a.list[base + __popc(m & ((1u << lane) - 1u))] = b * npix + pix;
+}
+
+// With the forward's pixel list the colour gradient is the incoming one
+// everywhere (this pass) except at the listed pixels (aa_bwd_list_kernel,
+// launched after it, overwrites them).
+__global__ void __launch_bounds__(256) aa_grad_copy_kernel(AAArgs a) {
+    const long long n = (long long)a.B * a.H * a.W * a.C;
+    const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if ((((uintptr_t)a.grad_out | (uintptr_t)a.grad_color) & 15) == 0) {
+        if (i + 4 <= n) {
+            *reinterpret_cast<float4*>(a.grad_color + i) = *reinterpret_cast<const float4*>(a.grad_out + i);
+            return;
+        }
+    }
+    for (long long k = i; k < i + 4 && k < n; ++k) a.grad_color[k] = a.grad_out[k];
+}
+
+__global__ void __launch_bounds__(256) aa_bwd_list_kernel(AAArgs a) {
+    const unsigned n = *a.list_count;
+    const int npix = a.H * a.W;
+    const int C = a.C;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int g = a.list[i];
+        const int b = g / npix, pix = g - b * npix;
+        const float4* R = reinterpret_cast<const float4*>(a.rast) + (long long)b * npix;
+        const float* Cc = a.color + (long long)b * npix * C;
+        const float* Gd = a.grad_out + (long long)b * npix * C;
+        const float4* P = reinterpret_cast<const float4*>(a.pos + (long long)b * a.pos_view_stride);
+        float4* GP = a.grad_pos ? reinterpret_cast<float4*>(a.grad_pos + (long long)b * a.pos_view_stride) : nullptr;
+        const float4* rec = reinterpret_cast<const float4*>(a.tri_rec) + (long long)b * a.num_triangles * 2;
+        AATerms at;
+        aa_bwd_terms(R, Cc, Gd, rec, a.num_triangles, a.W, a.H, C, P, a.tri, GP, a.boost, pix, at);
+        float* gc = a.grad_color + ((long long)b * npix + pix) * C;
+        for (int c = 0; c < C; ++c) gc[c] = aa_bwd_channel(at, Gd, C, pix, c);
+    }
 }
 
 __global__ void __launch_bounds__(256) aa_bwd_kernel(AAArgs a) {
@@ -172,6 +221,8 @@ __global__ void __launch_bounds__(256) aa_bwd_kernel(AAArgs a) {
 
 size_t aa_ws_bytes(int B, long long F) { return (size_t)B * (size_t)F * 32 + 256; }
 
+size_t aa_state_bytes(int B, int H, int W) { return 256 + (size_t)B * (size_t)H * (size_t)W * 4; }
+
 static void launch_aa_setup(const AAArgs& a, cudaStream_t s) {
     if (a.num_triangles <= 0) return;
     dim3 grid((unsigned)((a.num_triangles + 255) / 256), (unsigned)a.B);
@@ -182,6 +233,7 @@ static void launch_aa_setup(const AAArgs& a, cudaStream_t s) {
 int launch_aa_fwd(const AAArgs& a, cudaStream_t s) {
     const int npix = a.H * a.W;
     if (npix == 0) return 0;
+    if (a.list_count) cudaMemsetAsync(a.list_count, 0, sizeof(unsigned), s);
     launch_aa_setup(a, s);
     dim3 grid((unsigned)((npix + 255) / 256), (unsigned)a.B);
     aa_fwd_kernel<<<grid, 256, 0, s>>>(a);
@@ -193,6 +245,21 @@ int launch_aa_bwd(const AAArgs& a, cudaStream_t s) {
     const int npix = a.H * a.W;
     if (npix == 0) return 0;
     launch_aa_setup(a, s);
+    if (a.list_count) {
+        const long long n4 = ((long long)a.B * npix * a.C + 3) / 4;
+        aa_grad_copy_kernel<<<(unsigned)((n4 + 255) / 256), 256, 0, s>>>(a);
+        drp_note_launch();
+        static int grid = 0;
+        if (grid == 0) {
+            int dev = 0, sms = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            grid = (sms > 0 ? sms : 1) * 4;
+        }
+        aa_bwd_list_kernel<<<grid, 256, 0, s>>>(a);
+        drp_note_launch();
+        return 0;
+    }
     dim3 grid((unsigned)((npix + 255) / 256), (unsigned)a.B);
     aa_bwd_kernel<<<grid, 256, 0, s>>>(a);
     drp_note_launch();

@@ -363,15 +363,24 @@ static int aa_ws_check(void* workspace, size_t workspace_bytes, int num_views, l
     return DRP_STATUS_OK;
 }
 
+DRP_API int drp_antialias_state_size(int num_views, int height, int width, size_t* bytes) {
+    if (num_views <= 0 || !res_ok(height, width) || !bytes) return fail(DRP_STATUS_INVALID_ARGUMENT, "bad arguments");
+    *bytes = drp::aa_state_bytes(num_views, height, width);
+    return DRP_STATUS_OK;
+}
+
 DRP_API int drp_antialias_fwd(void* workspace, size_t workspace_bytes, const float* color, int channels,
                               const float* rast, const float* pos, long long pos_view_stride, long long num_vertices,
                               const int* tri, long long num_triangles, const int* nbr, int num_views, int height,
-                              int width, float* out, void* stream) {
+                              int width, float* out, void* aa_state, void* stream) {
     int st = aa_common(color, channels, rast, pos, pos_view_stride, tri, num_views, height, width);
     if (st) return st;
     st = aa_ws_check(workspace, workspace_bytes, num_views, num_triangles);
     if (st) return st;
     if (!out) return fail(DRP_STATUS_INVALID_ARGUMENT, "null output");
+    if (!aligned(aa_state, 256)) return fail(DRP_STATUS_INVALID_ARGUMENT, "aa_state must be 256-byte aligned");
+    if ((long long)num_views * height * width > 0x7fffffffll)
+        return fail(DRP_STATUS_INVALID_ARGUMENT, "num_views * height * width above 2^31 - 1");
     drp::AAArgs a{};
     a.color = color;
     a.C = channels;
@@ -387,6 +396,10 @@ DRP_API int drp_antialias_fwd(void* workspace, size_t workspace_bytes, const flo
     a.H = height;
     a.W = width;
     a.out = out;
+    if (aa_state) {
+        a.list_count = static_cast<unsigned*>(aa_state);
+        a.list = reinterpret_cast<int*>(static_cast<char*>(aa_state) + 256);
+    }
     drp::launch_aa_fwd(a, static_cast<cudaStream_t>(stream));
     return check_launch("drp_antialias_fwd");
 }
@@ -395,7 +408,7 @@ DRP_API int drp_antialias_bwd(void* workspace, size_t workspace_bytes, const flo
                               const float* rast, const float* pos, long long pos_view_stride, long long num_vertices,
                               const int* tri, long long num_triangles, const int* nbr, int num_views, int height,
                               int width, const float* grad_out, float pos_gradient_boost, float* grad_color,
-                              float* grad_pos, void* stream) {
+                              float* grad_pos, const void* aa_state, void* stream) {
     int st = aa_common(color, channels, rast, pos, pos_view_stride, tri, num_views, height, width);
     if (st) return st;
     st = aa_ws_check(workspace, workspace_bytes, num_views, num_triangles);
@@ -420,6 +433,11 @@ DRP_API int drp_antialias_bwd(void* workspace, size_t workspace_bytes, const flo
     a.grad_color = grad_color;
     a.grad_pos = grad_pos;
     a.boost = pos_gradient_boost;
+    if (aa_state) {
+        if (!aligned(aa_state, 256)) return fail(DRP_STATUS_INVALID_ARGUMENT, "aa_state must be 256-byte aligned");
+        a.list_count = const_cast<unsigned*>(static_cast<const unsigned*>(aa_state));
+        a.list = reinterpret_cast<int*>(static_cast<char*>(const_cast<void*>(aa_state)) + 256);
+    }
     drp::launch_aa_bwd(a, static_cast<cudaStream_t>(stream));
     return check_launch("drp_antialias_bwd");
 }

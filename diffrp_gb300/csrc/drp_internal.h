@@ -108,7 +108,14 @@ struct AAArgs {
     float* grad_color;
     float* grad_pos;
     float boost;
+    // optional pixel list (forward appends every pixel a blending pair
+    // touches; the backward then evaluates the antialias terms of those only)
+    unsigned* list_count;
+    int* list;
 };
+
+// Bytes of the drp_antialias_fwd / _bwd pixel-list state for B views of H x W.
+size_t aa_state_bytes(int B, int H, int W);
 
 int launch_rasterize(const RasterArgs& a, cudaStream_t s);
 int launch_raster_bwd(const RasterBwdArgs& a, cudaStream_t s);

@@ -336,33 +336,6 @@ __device__ __forceinline__ uint32_t block_mask(int x0, int x1, int y0, int y1) {
     return (uint32_t)(cols * REP & rows);
 }
 
-// Clear the blocks of mask m (block_mask numbering) that lie wholly outside
-// one of the primitive's edges: the edge function is linear, so its largest
-// value over a block's pixels sits at a block corner.  BIG primitives keep
-// their bbox mask.  All terms stay below 2^30 in magnitude (prepare_tile_prim
-// only keeps 32-bit edges under that bound over the tile).
-template <int T>
-__device__ __forceinline__ uint32_t refine_block_mask(const TilePrim& tp, uint32_t m) {
-    if (tp.e2.y & TP_BIG) return m;
-    constexpr int CW = T / 8;
-    const int4 e0 = tp.e0, e1 = tp.e1, e2 = tp.e2;
-    const int A[3] = {e0.x, e0.w, e1.z}, B[3] = {e0.y, e1.x, e1.w}, C[3] = {e0.z, e1.y, e2.x};
-    uint32_t out = m;
-    for (uint32_t r = m; r; r &= r - 1u) {
-        const int b = __ffs(r) - 1;
-        const int bx = (b % CW) * 8, by = (b / CW) * 4;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const int mx = C[k] + max(A[k] * bx, A[k] * (bx + 7)) + max(B[k] * by, B[k] * (by + 3));
-            if (mx < 0) {
-                out &= ~(1u << b);
-                break;
-            }
-        }
-    }
-    return out;
-}
-
 // One tile's work for the fine raster.
 struct FineTile {
     const int4* recs;           // primitive records
@@ -432,12 +405,9 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
             prepare_tile_prim<T>(recs + pidx * 3, tx0, ty0, W, H, tp);
             const int fl = tp.e2.y;
             if (fl & TP_COMPLEX) atomicAdd(&n_complex, 1);
-            uint32_t bm = 0u;
-            if (fl & TP_ACTIVE) {
-                bm = block_mask<T>(tp.v2b.z & 0xffff, tp.v2b.z >> 16, tp.v2b.w & 0xffff, tp.v2b.w >> 16);
-                if (TPT == 0) bm = refine_block_mask<T>(tp, bm);
-            }
-            pmask[tid] = bm;
+            pmask[tid] = (fl & TP_ACTIVE) ? block_mask<T>(tp.v2b.z & 0xffff, tp.v2b.z >> 16, tp.v2b.w & 0xffff,
+                                                          tp.v2b.w >> 16)
+                                          : 0u;
         }
         __syncthreads();
         if (TPT == 0) {

@@ -455,16 +455,19 @@ class _AntialiasFn(torch.autograd.Function):
         stride = pos.shape[1] * 4 if pos.dim() == 3 else 0
         out = torch.empty_like(color)
         ws = _scratch.get(color.device, "antialias", _ffi.size_out("drp_antialias_workspace_size", B, tri.shape[0]))
+        # the list of pixels a blending pair touches, for the backward
+        state = torch.empty(_ffi.size_out("drp_antialias_state_size", B, H, W), dtype=torch.uint8,
+                            device=color.device)
         _ffi.call("drp_antialias_fwd", ws.data_ptr(), ws.numel(), color.data_ptr(), C, rast.data_ptr(),
                   pos.data_ptr(), stride, pos.shape[-2], tri.data_ptr(), tri.shape[0], nbr.data_ptr(), B, H, W,
-                  out.data_ptr(), _stream(color.device))
-        ctx.save_for_backward(color, rast, pos, tri, nbr)
+                  out.data_ptr(), state.data_ptr(), _stream(color.device))
+        ctx.save_for_backward(color, rast, pos, tri, nbr, state)
         ctx.meta = (B, H, W, C, stride, boost)
         return out
 
     @staticmethod
     def backward(ctx, grad_out):
-        color, rast, pos, tri, nbr = ctx.saved_tensors
+        color, rast, pos, tri, nbr, state = ctx.saved_tensors
         B, H, W, C, stride, boost = ctx.meta
         grad_out = grad_out.contiguous()
         grad_color = torch.empty_like(color)
@@ -473,7 +476,8 @@ class _AntialiasFn(torch.autograd.Function):
         ws = _scratch.get(color.device, "antialias", _ffi.size_out("drp_antialias_workspace_size", B, tri.shape[0]))
         _ffi.call("drp_antialias_bwd", ws.data_ptr(), ws.numel(), color.data_ptr(), C, rast.data_ptr(),
                   pos.data_ptr(), stride, pos.shape[-2], tri.data_ptr(), tri.shape[0], nbr.data_ptr(), B, H, W,
-                  grad_out.data_ptr(), float(boost), grad_color.data_ptr(), _ptr(grad_pos), _stream(color.device))
+                  grad_out.data_ptr(), float(boost), grad_color.data_ptr(), _ptr(grad_pos), state.data_ptr(),
+                  _stream(color.device))
         return grad_color, None, grad_pos, None, None, None
 
 

@@ -66,7 +66,8 @@ unsigned long long drp_kernel_launches(void);
 /*
  * Workspace bytes for drp_rasterize_fwd.  The first 16 bytes of the workspace
  * are a stats block written by every call: bytes [0, 8) = tile-list entries the
- * call needed (uint64), bytes [8, 12) = DRP_DEVERR_* bits.  Callers grow
+ * call needed (uint64), bytes [8, 12) = DRP_DEVERR_* bits, bytes [12, 16) =
+ * the largest per-tile entry count (uint32).  Callers grow
  * list_capacity from the first field; a call whose lists overflow is still
  * exact (overflowing tiles fall back to scanning the view's primitives).
  */
@@ -168,15 +169,21 @@ int drp_antialias_topology(void* workspace, size_t workspace_bytes, const int* t
  * view and triangle: screen-space vertices and silhouette-edge mask). */
 int drp_antialias_workspace_size(int num_views, long long num_triangles, size_t* bytes);
 
+/* Bytes of the optional pixel-list state of drp_antialias_fwd / _bwd. */
+int drp_antialias_state_size(int num_views, int height, int width, size_t* bytes);
+
 /*
  * dr.antialias(color, rast, pos, tri) (diffrp/rendering/surface_deferred.py:775).
  * color (B, H, W, C); nbr from drp_antialias_topology or NULL (every edge
  * is treated as a silhouette).  The workspace is scratch for this call only.
+ * aa_state (may be NULL; drp_antialias_state_size bytes, 256-byte aligned)
+ * receives the list of pixels a blending pair touches; handing it to the
+ * matching drp_antialias_bwd lets the backward evaluate only those pixels.
  */
 int drp_antialias_fwd(void* workspace, size_t workspace_bytes, const float* color, int channels, const float* rast,
                       const float* pos, long long pos_view_stride, long long num_vertices, const int* tri,
                       long long num_triangles, const int* nbr, int num_views, int height, int width, float* out,
-                      void* stream);
+                      void* aa_state, void* stream);
 
 /* Most num_views * num_triangles that drp_antialias_fwd_noalloc accepts
  * (its fixed scratch holds 32 bytes per triangle and view: 8 MiB). */
@@ -204,12 +211,13 @@ int drp_antialias_fwd_noalloc(const float* color, int channels, const float* ras
                               float* out, void* stream);
 
 /* Backward: grad_color overwritten, grad_pos accumulated (times
- * pos_gradient_boost); grad_pos may be NULL. */
+ * pos_gradient_boost); grad_pos may be NULL.  aa_state: NULL, or the state
+ * the forward on the same color / rast / pos filled. */
 int drp_antialias_bwd(void* workspace, size_t workspace_bytes, const float* color, int channels, const float* rast,
                       const float* pos, long long pos_view_stride, long long num_vertices, const int* tri,
                       long long num_triangles, const int* nbr, int num_views, int height, int width,
                       const float* grad_out, float pos_gradient_boost, float* grad_color, float* grad_pos,
-                      void* stream);
+                      const void* aa_state, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Edge-gradient visibility operator                                         */

@@ -44,7 +44,7 @@ def _run(lib, noalloc, pos, tri, rast, color, nbr, H, W):
     else:
         ws = torch.empty(_ffi.size_out("drp_antialias_workspace_size", 1, tri.shape[0]), dtype=torch.uint8,
                          device="cuda")
-        status = lib.drp_antialias_fwd(ws.data_ptr(), ws.numel(), *common)
+        status = lib.drp_antialias_fwd(ws.data_ptr(), ws.numel(), *common[:-1], None, stream)
         assert status == 0, lib.drp_last_error()
     torch.cuda.synchronize()
     return out
