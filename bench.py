@@ -98,6 +98,19 @@ class Step:
         return loss
 
 
+def packed_attr_offset(nv):
+    return (nv + 63) // 64 * 64
+
+
+def pack_inputs(verts_np, attr_np):
+    """Vertices, then attributes at a 256-byte aligned offset, in one array."""
+    a0 = packed_attr_offset(verts_np.size)
+    buf = np.zeros(a0 + attr_np.size, np.float32)
+    buf[:verts_np.size] = verts_np.reshape(-1)
+    buf[a0:] = attr_np.reshape(-1)
+    return buf
+
+
 class GraphedStep:
     """The same step captured once as a CUDA graph (static parameter tensors,
     gradients allocated in the graph's pool) and replayed."""
@@ -105,8 +118,13 @@ class GraphedStep:
     def __init__(self, step, verts_np, attr_np, dev):
         import torch
         self.torch = torch
-        self.verts = torch.from_numpy(verts_np).to(dev).requires_grad_(True)
-        self.attr = torch.from_numpy(attr_np).to(dev).requires_grad_(True)
+        # parameters as views of one packed buffer: one host->device copy per step
+        nv, na = verts_np.size, attr_np.size
+        self.inbuf = torch.from_numpy(pack_inputs(verts_np, attr_np)).to(dev)
+        a0 = packed_attr_offset(nv)  # attributes start 256-byte aligned (128-bit row access)
+        self.verts = self.inbuf[:nv].view(verts_np.shape).requires_grad_(True)
+        self.attr = self.inbuf[a0:a0 + na].view(attr_np.shape).requires_grad_(True)
+        self.outbuf = torch.empty(1 + nv + na, dtype=torch.float32, device=dev)
         side = torch.cuda.Stream(dev)
         side.wait_stream(torch.cuda.current_stream(dev))
         with torch.cuda.stream(side):
@@ -122,10 +140,16 @@ class GraphedStep:
         self.launches_per_step = kernel_launches() - n0
         torch.cuda.synchronize(dev)
 
-    def load(self, h_verts, h_attr):
+    def load(self, h_in):
+        """h_in: pinned host floats, vertices then attributes."""
         with self.torch.no_grad():
-            self.verts.copy_(h_verts, non_blocking=True)
-            self.attr.copy_(h_attr, non_blocking=True)
+            self.inbuf.copy_(h_in, non_blocking=True)
+
+    def pack_result(self):
+        """Loss and gradients into one device buffer (one device->host copy)."""
+        torch = self.torch
+        torch.cat([self.loss.detach().view(1), self.verts.grad.view(-1), self.attr.grad.view(-1)], out=self.outbuf)
+        return self.outbuf
 
     def __call__(self):
         self.graph.replay()
@@ -347,6 +371,8 @@ def run_batched(dev, name, steps, warmup, plain=True, recompute=False, tune=True
     s = torch.cuda.current_stream(dev)
 
     def timed(fn, n):
+        for _ in range(max(3, warmup)):  # untimed warm-up of this exact callable
+            fn()
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
         torch.cuda.synchronize(dev)
         for i in range(n):
@@ -702,6 +728,8 @@ def main():
     s = torch.cuda.current_stream(dev)
 
     def timed(fn, n):
+        for _ in range(W_):  # untimed warm-up of this exact callable (first launches load their kernels)
+            fn()
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
         barrier()
         for i in range(n):
@@ -730,19 +758,16 @@ def main():
     eager_ms = timed(lambda: step(verts, attr), args.steps)
 
     # -- end-to-end through the public API with host buffers -----------------
-    h_verts = torch.from_numpy(verts_np).pin_memory()
-    h_attr = torch.from_numpy(attr_np).pin_memory()
-    h_loss = torch.empty((), dtype=torch.float32).pin_memory()
-    h_gv = torch.empty_like(h_verts).pin_memory()
-    h_ga = torch.empty_like(h_attr).pin_memory()
+    # inputs from one pinned host buffer (vertices, attributes), outputs (loss,
+    # vertex and attribute gradients) back into one pinned host buffer
+    h_in = torch.from_numpy(pack_inputs(verts_np, attr_np)).pin_memory()
+    h_out = torch.empty(1 + verts_np.size + attr_np.size, dtype=torch.float32).pin_memory()
 
     def e2e_of(gs):
         def e2e_step():
-            gs.load(h_verts, h_attr)
-            loss = gs()
-            h_loss.copy_(loss.detach(), non_blocking=True)
-            h_gv.copy_(gs.verts.grad, non_blocking=True)
-            h_ga.copy_(gs.attr.grad, non_blocking=True)
+            gs.load(h_in)
+            gs()
+            h_out.copy_(gs.pack_result(), non_blocking=True)
         return e2e_step
 
     e2e_ms = timed(e2e_of(batched), args.steps)
@@ -756,8 +781,8 @@ def main():
     pix = H * W * args.steps * world
     value = pix / (total_ms / 1e3) / 1e6
     e2e_value = pix / (e2e_ms / 1e3) / 1e6
-    h2d = h_verts.numel() * 4 + h_attr.numel() * 4
-    d2h = 4 + h_gv.numel() * 4 + h_ga.numel() * 4
+    h2d = h_in.numel() * 4
+    d2h = h_out.numel() * 4
 
     if rank == 0:
         times, algo = kernel_breakdown(dev, verts_np, f, attr_np, mvp, target, tuned=tuned, batch=bstep.renderer)
