@@ -214,6 +214,7 @@ __device__ __noinline__ void raster_complex_tile(const float4* P, const int* tri
 #define TP_ACTIVE 1
 #define TP_BIG 2
 #define TP_COMPLEX 4
+#define TP_NEG 8  // clockwise in the snapped screen frame (the other facing class)
 
 struct __align__(16) TilePrim {
     int4 e0;    // A0, B0, C0, A1
@@ -272,13 +273,35 @@ __device__ __forceinline__ void prepare_tile_prim(const int4* rec, int tx0, int 
     }
     tp.e0 = make_int4(A[0], B[0], C[0], A[1]);
     tp.e1 = make_int4(B[1], C[1], A[2], B[2]);
-    tp.e2 = make_int4(C[2], TP_ACTIVE | (big ? TP_BIG : 0), (int)X0, (int)Y0);
+    tp.e2 = make_int4(C[2], TP_ACTIVE | (big ? TP_BIG : 0) | (area2 < 0 ? TP_NEG : 0), (int)X0, (int)Y0);
     tp.z.x = __int_as_float(r2.x);
     tp.z.y = __int_as_float(r2.y);
     tp.z.z = __int_as_float(r2.z);
     tp.v01 = make_int4((int)vx[0], (int)vy[0], (int)vx[1], (int)vy[1]);
     tp.v2b.x = (int)vx[2];
     tp.v2b.y = (int)vy[2];
+}
+
+// A lower bound of the depth (z/w) of every fragment the primitive can
+// produce: the plane's minimum over the triangle is at a vertex; fragments are
+// evaluated as (Z0 + A dx) + B dy in float, so the bound is lowered by a few
+// ulps of the largest term (2^-20 relative; each of the three roundings is at
+// most 2^-24 of its result).
+__device__ __forceinline__ float prim_depth_lower_bound(const TilePrim& tp) {
+    const float Z0 = tp.z.x, A = tp.z.y, B = tp.z.z;
+    const int X0 = tp.e2.z, Y0 = tp.e2.w;
+    const float dx[3] = {(float)(tp.v01.x - X0), (float)(tp.v01.z - X0), (float)(tp.v2b.x - X0)};
+    const float dy[3] = {(float)(tp.v01.y - Y0), (float)(tp.v01.w - Y0), (float)(tp.v2b.y - Y0)};
+    float zmin = 3.0e38f, ax = 0.0f, by = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float za = A * dx[i], zb = B * dy[i];
+        zmin = fminf(zmin, (Z0 + za) + zb);
+        ax = fmaxf(ax, fabsf(za));
+        by = fmaxf(by, fabsf(zb));
+    }
+    const float m = fabsf(Z0) + ax + by;
+    return zmin - m * 9.5367431640625e-7f - 1.0e-30f;  // 2^-20 of the magnitude
 }
 
 __device__ __forceinline__ bool tile_prim_covers(const TilePrim& tp, const int4& e0, const int4& e1, const int4& e2,
@@ -368,6 +391,7 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
     __shared__ unsigned long long keys[NPIX];
     __shared__ TilePrim prims[CHUNK];
     __shared__ uint32_t pmask[CHUNK];  // 8x4 blocks each prepared primitive's bbox overlaps
+    __shared__ uint32_t pzlo[CHUNK];   // depth_order of a lower bound of the primitive's fragment depths
     __shared__ int n_complex;
     __shared__ float col_ndc[T], row_ndc[T];
 
@@ -408,35 +432,59 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
             pmask[tid] = (fl & TP_ACTIVE) ? block_mask<T>(tp.v2b.z & 0xffff, tp.v2b.z >> 16, tp.v2b.w & 0xffff,
                                                           tp.v2b.w >> 16)
                                           : 0u;
+            if (TPT == 0 && (fl & TP_ACTIVE)) pzlo[tid] = depth_order(prim_depth_lower_bound(tp));
         }
         __syncthreads();
         if (TPT == 0) {
             // Each warp ballots the primitives whose block mask meets its own
-            // blocks, then walks only those (warp-uniform loop).
+            // blocks, then walks only those (warp-uniform loop).  The facing
+            // class holding the nearest primitive goes first; the other class
+            // is then skipped per 8x4 block wherever its depth lower bound lies
+            // behind every key the block already holds (such a primitive
+            // cannot win any of the block's pixels, so the result is exact).
             const int lane = tid & 31;
             uint32_t wbits = 0;
 #pragma unroll
             for (int q = 0; q < PPT; ++q) wbits |= 1u << tile_block<TILE_LOG2, NTHREADS>(tid, q);
-            for (int j0 = 0; j0 < n; j0 += 32) {
-                const uint32_t pm = j0 + lane < n ? pmask[j0 + lane] : 0u;
-                uint32_t hits = __ballot_sync(0xffffffffu, (pm & wbits) != 0u);
-                while (hits) {
-                    const int b = __ffs(hits) - 1;
-                    hits &= hits - 1;
-                    const uint32_t mj = __shfl_sync(0xffffffffu, pm, b);
-                    const TilePrim& tp = prims[j0 + b];
-                    const int4 e0 = tp.e0, e1 = tp.e1, e2 = tp.e2;
+            uint32_t zmin0 = 0xffffffffu, zmin1 = 0xffffffffu;
+            for (int j = lane; j < n; j += 32) {
+                const int f = prims[j].e2.y;
+                if (!(f & TP_ACTIVE)) continue;
+                if (f & TP_NEG) zmin1 = min(zmin1, pzlo[j]);
+                else zmin0 = min(zmin0, pzlo[j]);
+            }
+            const int first = __reduce_min_sync(0xffffffffu, zmin0) <= __reduce_min_sync(0xffffffffu, zmin1) ? 0 : 1;
+            for (int pass = 0; pass < 2; ++pass) {
+                const int want = pass == 0 ? first : 1 - first;
+                uint32_t bmax[PPT];
 #pragma unroll
-                    for (int q = 0; q < PPT; ++q) {
-                        if (!((mj >> tile_block<TILE_LOG2, NTHREADS>(tid, q)) & 1u)) continue;  // warp-uniform
-                        int dx, dy, bx, by;
-                        tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
-                        const int sx = (tx0 + dx) * DRP_SUBPIX + DRP_HALF_SUBPIX;
-                        const int sy = (ty0 + dy) * DRP_SUBPIX + DRP_HALF_SUBPIX;
-                        if (!tile_prim_covers(tp, e0, e1, e2, dx, dy, sx, sy)) continue;
-                        bool ok;
-                        const unsigned long long k = tile_prim_key(tp.z, e2.z, e2.w, sx, sy, ok);
-                        if (ok && k < best[q] && (!prev_g || k > prevk[q])) best[q] = k;
+                for (int q = 0; q < PPT; ++q)
+                    bmax[q] = pass == 0 ? 0xffffffffu : __reduce_max_sync(0xffffffffu, (uint32_t)(best[q] >> 32));
+                for (int j0 = 0; j0 < n; j0 += 32) {
+                    const int j = j0 + lane;
+                    const uint32_t pm =
+                        (j < n && ((prims[j].e2.y & TP_NEG) ? 1 : 0) == want) ? pmask[j] : 0u;
+                    uint32_t hits = __ballot_sync(0xffffffffu, (pm & wbits) != 0u);
+                    while (hits) {
+                        const int b = __ffs(hits) - 1;
+                        hits &= hits - 1;
+                        const uint32_t mj = __shfl_sync(0xffffffffu, pm, b);
+                        const uint32_t zj = pzlo[j0 + b];
+                        const TilePrim& tp = prims[j0 + b];
+                        const int4 e0 = tp.e0, e1 = tp.e1, e2 = tp.e2;
+#pragma unroll
+                        for (int q = 0; q < PPT; ++q) {
+                            if (!((mj >> tile_block<TILE_LOG2, NTHREADS>(tid, q)) & 1u)) continue;  // warp-uniform
+                            if (zj > bmax[q]) continue;  // behind the whole block: warp-uniform
+                            int dx, dy, bx, by;
+                            tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+                            const int sx = (tx0 + dx) * DRP_SUBPIX + DRP_HALF_SUBPIX;
+                            const int sy = (ty0 + dy) * DRP_SUBPIX + DRP_HALF_SUBPIX;
+                            if (!tile_prim_covers(tp, e0, e1, e2, dx, dy, sx, sy)) continue;
+                            bool ok;
+                            const unsigned long long k = tile_prim_key(tp.z, e2.z, e2.w, sx, sy, ok);
+                            if (ok && k < best[q] && (!prev_g || k > prevk[q])) best[q] = k;
+                        }
                     }
                 }
             }

@@ -108,8 +108,8 @@ class RasterizeCudaContext:
         self._retired = []  # replaced buffers, kept alive for CUDA graphs captured on them
         self._capacity = 0
         self._sized = False
-        self._pending = None
-        self._pinned = None
+        self._pending = []  # (event, pinned stats copy) of raster calls not read back yet
+        self._pinned_free = []
         self._topo_ws = None
         self.last_list_entries = 0
 
@@ -123,15 +123,20 @@ class RasterizeCudaContext:
         return self._ws
 
     def _poll_stats(self):
-        if self._pending is None:
-            return
-        ev, pinned = self._pending
-        if ev.query():
-            needed = int(pinned[0].item())
-            self.last_list_entries = needed
-            if needed > self._capacity:
-                self._capacity = int(needed * 1.25) + 1024
-            self._pending = None
+        """Grow the list capacity from every finished call's stats (a call
+        that needed more than it had was still exact, through the slow
+        per-tile scan; the next calls get room)."""
+        keep = []
+        for ev, pinned in self._pending:
+            if ev.query():
+                needed = int(pinned[0])
+                self.last_list_entries = needed
+                if needed > self._capacity:
+                    self._capacity = int(needed * 1.25) + 1024
+                self._pinned_free.append(pinned)
+            else:
+                keep.append((ev, pinned))
+        self._pending = keep
 
     def _read_stats_sync(self):
         torch.cuda.current_stream(self.device).synchronize()
@@ -143,12 +148,15 @@ class RasterizeCudaContext:
     def _queue_stats(self):
         if _capturing():
             return
-        if self._pinned is None:
-            self._pinned = torch.empty(2, dtype=torch.int64, pin_memory=True)
-        self._pinned.copy_(self._ws[:16].view(torch.int64), non_blocking=True)
+        pinned = self._pinned_free.pop() if self._pinned_free else torch.empty(2, dtype=torch.int64,
+                                                                               pin_memory=True)
+        pinned.copy_(self._ws[:16].view(torch.int64), non_blocking=True)
         ev = torch.cuda.Event()
         ev.record(torch.cuda.current_stream(self.device))
-        self._pending = (ev, self._pinned)
+        self._pending.append((ev, pinned))
+        if len(self._pending) > 64:  # bound the queue: wait for the oldest read-back
+            self._pending[0][0].synchronize()
+            self._poll_stats()
 
     def ensure_capacity(self, entries):
         """Pre-size the tile-list capacity (used by graph capture paths)."""
@@ -156,6 +164,8 @@ class RasterizeCudaContext:
         self._sized = True
 
     def _raster_call(self, pos, tri, ranges_dev, B, max_view_tris, H, W, stride, prev_key, rast, db, out_key):
+        if not _capturing():
+            self._poll_stats()
         cap = self._capacity
         first = not self._sized
         if first:

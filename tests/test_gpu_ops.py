@@ -111,6 +111,27 @@ def test_tile_scan_across_chunks(cuda_lib):
     assert total == per_view > 0
 
 
+def test_list_capacity_grows_across_mixed_calls(cuda_lib):
+    """One context serving a small and then a much denser view: the dense
+    call overflows the capacity sized by the first (still exact), its stats
+    are read back later, and the next dense call has room."""
+    dr = _dr()
+    ctx = _ctx()
+    small_pos, small_tri = scenes.random_soup(20, seed=1)
+    dr.rasterize(ctx, _t(small_pos), _t(small_tri), (64, 64), grad_db=False)
+    cap0 = ctx._capacity
+    pos, tri = scenes.random_soup(3000, seed=2)
+    ref, _, _ = O.rasterize(pos, tri, (64, 64), grad_db=False)
+    rast, _ = dr.rasterize(ctx, _t(pos), _t(tri), (64, 64), grad_db=False)
+    np.testing.assert_array_equal(rast.cpu().numpy(), ref)
+    torch.cuda.synchronize()
+    rast, _ = dr.rasterize(ctx, _t(pos), _t(tri), (64, 64), grad_db=False)  # polls the earlier stats first
+    assert ctx._capacity > cap0
+    _, err = ctx._read_stats_sync()
+    assert err & 2 == 0, "the list still overflowed after the read-back"
+    np.testing.assert_array_equal(rast.cpu().numpy(), ref)
+
+
 def test_depth_peeling(cuda_lib):
     pos, tri = scenes.random_soup(120, seed=2)
     dr = _dr()
