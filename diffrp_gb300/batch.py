@@ -146,7 +146,8 @@ class BatchRenderer:
         self._pinned = None
         self.last_list_entries = 0
         self.last_max_tile = 0
-        self._rec_ws = None  # the workspace buffer holding the latest forward's AA records
+        self._rec_ws = None  # the workspace buffer holding the latest AA records ...
+        self._rec_gen = -1  # ... and the forward generation that wrote them
 
     def set_raster_shape(self, tile_log2, threads_per_tri):
         """Change the fine-raster tile size / threads per primitive (re-plans;
@@ -268,7 +269,9 @@ class BatchRenderer:
                           color.data_ptr(), optr, fptr, npix, *tail)
         else:
             self._queue_stats(ws)
-        self._rec_ws = ws
+        if out is not None or l1 is not None:  # a raster-only forward writes no AA records
+            self._rec_ws = ws
+            self._rec_gen = self._fwd_gen
 
     def _backward_raw(self, pos, attr, rast, color, grad_out, grad_pos, grad_attr, gen=None, grad_scale=None,
                       aa_flags=None):
@@ -278,7 +281,7 @@ class BatchRenderer:
         aa_flags: the antialias slot bits that forward wrote, or None."""
         ws = self._workspace(0)  # the backward reads no tile list
         stream = torch.cuda.current_stream(self.device).cuda_stream
-        flags = REUSE_AA_RECORDS if gen is not None and gen == self._fwd_gen and ws is self._rec_ws else 0
+        flags = REUSE_AA_RECORDS if gen is not None and gen == self._rec_gen and ws is self._rec_ws else 0
         aa_grad = None if aa_flags is None else torch.empty(self.image_floats, dtype=torch.float32,
                                                             device=self.device)
         _ffi.call("drp_batch_backward", ws.data_ptr(), ws.numel(), self._items_dev.data_ptr(), len(self.items),
@@ -354,7 +357,7 @@ class _BatchFn(torch.autograd.Function):
             pos, attr, flags = ctx.saved_tensors
             rast, color = r._buffers()
             r._forward_raw(pos, attr, rast, color, None)
-            gen = r._fwd_gen
+            gen = ctx.gen  # the raster-only pass wrote no records; the original forward's may remain
         else:
             pos, attr, flags, rast, color = ctx.saved_tensors
             gen = ctx.gen
@@ -391,7 +394,7 @@ class _BatchL1Fn(torch.autograd.Function):
             pos, attr, grad, flags = ctx.saved_tensors
             rast, color = r._buffers()
             r._forward_raw(pos, attr, rast, color, None)
-            gen = r._fwd_gen
+            gen = ctx.gen  # the raster-only pass wrote no records; the original forward's may remain
         else:
             pos, attr, grad, flags, rast, color = ctx.saved_tensors
             gen = ctx.gen

@@ -49,6 +49,7 @@ struct BatchArgs {
     unsigned* aa_count;
     float* aa_grad;           // backward scratch: antialiased colour gradient of listed pixels
     bool emit_out;          // the fine raster also writes the colour into out
+    bool aa_records;        // the setup pass writes the antialias triangle records
     // fused mean-absolute-error loss (null target: none)
     const float* target;
     float l1_scale;
@@ -109,10 +110,11 @@ __global__ void __launch_bounds__(256) batch_setup_bin_kernel(BatchArgs a) {
                            (uint32_t)pidx);
     } else {
         // The antialias triangle record rides along with the setup pass (same
-        // triangle, same vertices).
-        aa_tri_record(reinterpret_cast<const float4*>(a.pos) + it.pos_offset, a.tri + 3 * (long long)it.tri_first,
-                      a.nbr ? a.nbr + 3 * (long long)it.tri_first : nullptr, j, it.tri_count, it.num_vertices,
-                      it.width, it.height, a.aa_rec + pidx * 2);
+        // triangle, same vertices); a raster-only forward skips it.
+        if (a.aa_records)
+            aa_tri_record(reinterpret_cast<const float4*>(a.pos) + it.pos_offset,
+                          a.tri + 3 * (long long)it.tri_first, a.nbr ? a.nbr + 3 * (long long)it.tri_first : nullptr,
+                          j, it.tri_count, it.num_vertices, it.width, it.height, a.aa_rec + pidx * 2);
         if (MODE == kSetupBins)
             bin_box<TILE_LOG2>(bx, live, it.tiles_x, a.tile_count + it.tile_offset,
                                a.tile_list + (unsigned long long)it.tile_offset * a.bin_depth, 0, (uint32_t)pidx,
@@ -781,6 +783,7 @@ DRP_API int drp_batch_forward(void* workspace, size_t workspace_bytes, const drp
         return bfail("batch: aa_state must be 256-byte aligned, with total_pixels > 0");
     carve_aa_state(a, aa_state, total_pixels);
     a.emit_out = out != nullptr;
+    a.aa_records = out != nullptr;  // raster only: no antialias pass, no records
     drp::launch_batch_forward(a, workspace, L, static_cast<cudaStream_t>(stream));
     return drp_check_launch("drp_batch_forward");
 }
@@ -817,6 +820,7 @@ DRP_API int drp_batch_forward_l1(void* workspace, size_t workspace_bytes, const 
         return bfail("batch: aa_state must be 256-byte aligned, with total_pixels > 0");
     carve_aa_state(a, aa_state, total_pixels);
     a.emit_out = false;  // the fused antialias + loss pass writes every output pixel
+    a.aa_records = true;
     a.target = target;
     a.l1_scale = scale;
     a.l1_grad = grad;

@@ -67,7 +67,15 @@ __global__ void __launch_bounds__(1024) l1_final_kernel(const float* partial, lo
                                                         float* loss) {
     __shared__ double warp_sum[32];
     double s = 0.0;
-    for (long long i = threadIdx.x; i < nblocks; i += blockDim.x) s += (double)partial[i];
+    // eight independent loads in flight per thread, added in index order
+    const long long step = (long long)blockDim.x;
+    for (long long i = threadIdx.x; i < nblocks; i += 8 * step) {
+        float v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = i + k * step < nblocks ? partial[i + k * step] : 0.0f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) s += (double)v[k];
+    }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
     if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = s;

@@ -294,9 +294,9 @@ int drp_batch_workspace_size(long long total_prims, long long total_tiles, unsig
  * work queue), interpolate attr into colour (fused), antialias into out.
  * items / block maps are device copies.  nbr: per-mesh topology from
  * drp_antialias_topology at the mesh's triangle offset, or NULL.  out may be
- * NULL: then only rast and colour are written (the antialias pass is
- * skipped), which is how a backward without stored per-pixel buffers
- * regenerates them.
+ * NULL: then only rast and colour are written (the antialias pass and its
+ * triangle records are skipped), which is how a backward without stored
+ * per-pixel buffers regenerates them.
  * bin_depth 0: exact tile lists (count, scan, fill; list_capacity entries);
  * the workspace's stats then hold the total list entries (u64 at byte 0) and
  * the largest tile count (u32 at byte 12).  bin_depth > 0: one setup pass
