@@ -386,7 +386,7 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
     constexpr int NPIX = T * T;
     constexpr int NTHREADS = NPIX < 256 ? NPIX : 256;
     constexpr int PPT = NPIX / NTHREADS;
-    constexpr int CHUNK = NTHREADS < 128 ? NTHREADS : 128;
+    constexpr int CHUNK = NTHREADS;  // primitives prepared per pass: one per thread
     constexpr int GROUPS = TPT > 0 ? NTHREADS / TPT : 1;
     __shared__ unsigned long long keys[NPIX];
     __shared__ TilePrim prims[CHUNK];
