@@ -89,13 +89,19 @@ class Step:
         torch, dr = self.torch, self.dr
         verts.grad = None
         attr.grad = None
-        clip = torch.nn.functional.pad(verts, (0, 1), value=1.0) @ self.mvp.T
+        clip = clip_space(verts, self.mvp)
         rast, _ = dr.rasterize(self.ctx, clip, self.tri, (H, W), grad_db=False)
         col, _ = dr.interpolate(attr, rast, self.tri)
         aa = dr.antialias(col, rast, clip, self.tri, topology_hash=self.topo)
         loss = l1_loss(aa, self.target)
         loss.backward()
         return loss
+
+
+def clip_space(verts, mvp):
+    """Clip-space positions [v, 1] @ mvp^T of (V, 3) vertices: one addmm."""
+    import torch
+    return torch.addmm(mvp[:, 3], verts, mvp[:, :3].T)
 
 
 def packed_attr_offset(nv):
@@ -175,7 +181,7 @@ class BatchStep:
         torch = self.torch
         verts.grad = None
         attr.grad = None
-        clip = torch.nn.functional.pad(verts, (0, 1), value=1.0) @ self.mvp.T
+        clip = clip_space(verts, self.mvp)
         if self.fused_loss:
             loss, _ = self.renderer.render_l1(clip, attr.reshape(-1), self.target)
         else:
@@ -252,7 +258,7 @@ class MultiViewWorkload:
 
     def _clip(self, m, k):
         torch = self.torch
-        return torch.nn.functional.pad(self.verts[m], (0, 1), value=1.0) @ self.mvps[k].T
+        return clip_space(self.verts[m], self.mvps[k])
 
     def _zero(self):
         for t in self.verts + self.attrs:
@@ -265,6 +271,7 @@ class MultiViewWorkload:
         parts = []
         for v, mv in zip(self.verts, self.mesh_mvps):
             if mv is not None:
+                # (n, V, 4) = [v, 1] @ (n, 4, 4)^T: one batched GEMM per mesh (K = 4, aligned rows)
                 vh = torch.nn.functional.pad(v, (0, 1), value=1.0)
                 parts.append(torch.matmul(vh, mv.transpose(1, 2)).reshape(-1, 4))
         return torch.cat(parts) if len(parts) > 1 else parts[0]
@@ -480,7 +487,7 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None, batc
         autotune.apply(ctx, tuned)
     tri = torch.from_numpy(f).to(dev)
     v_t = torch.from_numpy(verts).to(dev)
-    clip = (torch.nn.functional.pad(v_t, (0, 1), value=1.0) @ torch.from_numpy(mvp).to(dev).T).contiguous()
+    clip = clip_space(v_t, torch.from_numpy(mvp).to(dev)).contiguous()
     a_t = torch.from_numpy(attr).to(dev)
     topo = dr.antialias_construct_topology_hash(tri)
     rast, _ = dr.rasterize(ctx, clip, tri, (H, W), grad_db=False)
@@ -683,7 +690,7 @@ def main():
     step = Step(dev, f, mvp, target)
     from diffrp_gb300 import autotune
     with torch.no_grad():
-        clip0 = (torch.nn.functional.pad(torch.from_numpy(verts_np).to(dev), (0, 1), value=1.0) @ step.mvp.T)
+        clip0 = clip_space(torch.from_numpy(verts_np).to(dev), step.mvp)
     if args.tile:
         tl, tpt = [int(x) for x in args.tile.split(",")]
         tuned = {"tile_log2": tl, "threads_per_tri": tpt}

@@ -335,6 +335,13 @@ class BatchRenderer:
         return rast, color, out
 
 
+def _zero_grads(pos, attr):
+    """Zeroed gradient buffers for pos and attr from one fill (the fused
+    backward accumulates into them); pos rows stay 16-byte aligned."""
+    buf = torch.zeros(pos.numel() + attr.numel(), dtype=torch.float32, device=pos.device)
+    return buf[:pos.numel()].view_as(pos), buf[pos.numel():].view_as(attr)
+
+
 class _BatchFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, pos, attr, renderer):
@@ -361,8 +368,7 @@ class _BatchFn(torch.autograd.Function):
         else:
             pos, attr, flags, rast, color = ctx.saved_tensors
             gen = ctx.gen
-        grad_pos = torch.zeros_like(pos)
-        grad_attr = torch.zeros_like(attr)
+        grad_pos, grad_attr = _zero_grads(pos, attr)
         r._backward_raw(pos, attr, rast, color, grad_out.contiguous(), grad_pos, grad_attr, gen, aa_flags=flags)
         return grad_pos, grad_attr, None
 
@@ -398,8 +404,7 @@ class _BatchL1Fn(torch.autograd.Function):
         else:
             pos, attr, grad, flags, rast, color = ctx.saved_tensors
             gen = ctx.gen
-        grad_pos = torch.zeros_like(pos)
-        grad_attr = torch.zeros_like(attr)
+        grad_pos, grad_attr = _zero_grads(pos, attr)
         if g_loss is None and g_out is None:
             return grad_pos, grad_attr, None, None
         scale = None
