@@ -158,9 +158,11 @@ def rasterize(pos, tri, resolution, ranges=None, prev_key=None, grad_db=True, pr
     return rast, db, key
 
 
-def raster_bwd(pos, tri, rast, grad_rast, grad_db=None, nthreads=None):
-    """dL/dpos in float64 (same layout as pos)."""
-    dt = np.float64
+def raster_bwd(pos, tri, rast, grad_rast, grad_db=None, nthreads=None, precision="f64"):
+    """dL/dpos in float64 (same layout as pos).  precision "f32" evaluates
+    every per-pixel term in float32 (the arithmetic of the CUDA path, so the
+    same branch at near-ties) and still accumulates in float64."""
+    dt = _dt(precision)
     posr = np.ascontiguousarray(pos, dtype=dt)
     tri = np.ascontiguousarray(tri, dtype=np.int32)
     rast = np.ascontiguousarray(rast, dtype=dt)
@@ -170,7 +172,7 @@ def raster_bwd(pos, tri, rast, grad_rast, grad_db=None, nthreads=None):
     gp = np.zeros(posr.shape, np.float64)
     gr = np.ascontiguousarray(grad_rast, dtype=dt)
     gd = None if grad_db is None else np.ascontiguousarray(grad_db, dtype=dt)
-    lib = load("f64")
+    lib = load(precision)
     _check(lib.orc_raster_bwd(_ptr(posr), stride, V, _ptr(tri), tri.shape[0], _ptr(rast), _ptr(gr), _ptr(gd), B, H, W,
                               _ptr(gp), nthreads or default_threads()), "raster_bwd")
     return gp
@@ -206,9 +208,12 @@ def interpolate(attr, rast, tri, rast_db=None, diff_attrs=None, precision="f32",
     return out, da
 
 
-def interpolate_bwd(attr, rast, tri, grad_out, rast_db=None, diff_attrs=None, grad_da=None, nthreads=None):
-    """Returns (grad_attr f64, grad_rast f64, grad_db f64 or None)."""
-    dt = np.float64
+def interpolate_bwd(attr, rast, tri, grad_out, rast_db=None, diff_attrs=None, grad_da=None, nthreads=None,
+                    precision="f64"):
+    """Returns (grad_attr f64, grad_rast, grad_db or None); grad_rast /
+    grad_db in the evaluation precision ("f32": float32 terms, see
+    raster_bwd)."""
+    dt = _dt(precision)
     attr = np.ascontiguousarray(attr, dtype=dt)
     rast = np.ascontiguousarray(rast, dtype=dt)
     tri = np.ascontiguousarray(tri, dtype=np.int32)
@@ -224,7 +229,7 @@ def interpolate_bwd(attr, rast, tri, grad_out, rast_db=None, diff_attrs=None, gr
     ga = np.zeros(attr.shape, np.float64)
     gr = np.empty((B, H, W, 4), dt)
     gdb = np.empty((B, H, W, 4), dt) if db is not None else None
-    lib = load("f64")
+    lib = load(precision)
     _check(lib.orc_interp_bwd(_ptr(attr), stride, V, C, _ptr(rast), _ptr(db), _ptr(tri), tri.shape[0], B, H, W,
                               _ptr(didx), nd, _ptr(go), _ptr(gda), _ptr(ga), _ptr(gr), _ptr(gdb),
                               nthreads or default_threads()), "interp_bwd")
@@ -268,9 +273,11 @@ def antialias(color, rast, pos, tri, nbr=None, precision="f32", nthreads=None):
     return out
 
 
-def antialias_bwd(color, rast, pos, tri, grad_out, nbr=None, pos_gradient_boost=1.0, nthreads=None):
-    """Returns (grad_color f64, grad_pos f64)."""
-    dt = np.float64
+def antialias_bwd(color, rast, pos, tri, grad_out, nbr=None, pos_gradient_boost=1.0, nthreads=None,
+                  precision="f64"):
+    """Returns (grad_color, grad_pos f64); grad_color in the evaluation
+    precision ("f32": float32 terms, see raster_bwd)."""
+    dt = _dt(precision)
     color = np.ascontiguousarray(color, dtype=dt)
     rast = np.ascontiguousarray(rast, dtype=dt)
     posr = np.ascontiguousarray(pos, dtype=dt)
@@ -282,7 +289,7 @@ def antialias_bwd(color, rast, pos, tri, grad_out, nbr=None, pos_gradient_boost=
     stride = posr.shape[1] * 4 if posr.ndim == 3 else 0
     gc = np.empty_like(color)
     gp = np.zeros(posr.shape, np.float64)
-    lib = load("f64")
+    lib = load(precision)
     _check(lib.orc_aa_bwd(_ptr(color), C, _ptr(rast), _ptr(posr), stride, posr.shape[-2], _ptr(tri), tri.shape[0],
                           _ptr(nbr), B, H, W, _ptr(go), float(pos_gradient_boost), _ptr(gc), _ptr(gp),
                           nthreads or default_threads()), "aa_bwd")

@@ -194,3 +194,23 @@ def test_fd_antialias_bwd():
     fdp = _fd(loss_p, pos)
     assert np.abs(gp - fdp).max() <= 1e-5 * max(1.0, np.abs(fdp).max())
     assert np.abs(gc - _fd(loss_c, col)).max() < 1e-6
+
+
+def test_backward_precision_f32_terms_match_f64():
+    """The oracle's float32-term backward (used to mirror the CUDA path's
+    branches at full size) stays within float32 rounding of the float64
+    one on a small scene."""
+    from tests import scenes
+    pos, tri = scenes.sphere_view(3, res=(48, 48), sigma=0.03, seed=6)
+    rng = np.random.default_rng(6)
+    rast, _, _ = O.rasterize(pos, tri, (48, 48), grad_db=False)
+    color = rng.uniform(0, 1, (1, 48, 48, 3)).astype(np.float32)
+    go = rng.normal(size=(1, 48, 48, 3)).astype(np.float32)
+    out = {}
+    for prec in ("f32", "f64"):
+        gc, gp = O.antialias_bwd(color, rast, pos, tri, go, precision=prec)
+        ga, gr, _ = O.interpolate_bwd(color[0, :1, :1].reshape(1, 3).repeat(len(pos), 0), rast, tri, gc,
+                                      precision=prec)
+        out[prec] = (gp + O.raster_bwd(pos, tri, rast, gr, precision=prec), ga)
+    for a, b in zip(out["f32"], out["f64"]):
+        assert np.abs(a - b).max() <= 1e-4 * np.abs(b).max()
