@@ -311,6 +311,36 @@ __device__ __forceinline__ float aa_fwd_pixel_l1(const float4* R, const float* C
 // pixel is the blend target, 2 the source), the target pixel and the weight;
 // the edge-vertex gradients of each pair are scattered here, once per pair
 // (by its first pixel), into GP (may be null).
+// Edge-vertex gradient of one valid, unclamped pair (scattered by the pair's
+// first pixel): dL/dt through the blend weight, then t through the exit
+// edge's two screen vertices to their clip coordinates.
+__device__ __forceinline__ void aa_edge_grad(const AAPair& p, const float* Cc, const float* Gd, int C,
+                                             const float4* P, const int* tri, float4* GP, float boost, float gscale,
+                                             int W, int H) {
+    float dLdw = 0.f;
+    for (int c = 0; c < C; ++c)
+        dLdw = fmaf(Gd[(long long)p.target * C + c] * gscale,
+                    Cc[(long long)p.src * C + c] - Cc[(long long)p.target * C + c], dLdw);
+    const float dLdt = dLdw * p.sign * boost;
+    const float den = p.eF - p.eO;
+    const float inv2 = 1.0f / (den * den);
+    const float dtF = -p.eO * inv2, dtO = p.eF * inv2;
+    const float2 ea = p.s[(p.k + 1) % 3], eb = p.s[(p.k + 2) % 3];
+    const float fF = dLdt * dtF * p.sgn, fO = dLdt * dtO * p.sgn;
+    const float gA0 = fmaf(fF, eb.y - p.cF.y, fO * (eb.y - p.cO.y));
+    const float gA1 = fmaf(fF, p.cF.x - eb.x, fO * (p.cO.x - eb.x));
+    const float gB0 = fmaf(fF, p.cF.y - ea.y, fO * (p.cO.y - ea.y));
+    const float gB1 = fmaf(fF, ea.x - p.cF.x, fO * (ea.x - p.cO.x));
+    const int vA = tri[3 * (long long)p.T + (p.k + 1) % 3], vB = tri[3 * (long long)p.T + (p.k + 2) % 3];
+    const float hx = 0.5f * (float)W, hy = 0.5f * (float)H;
+    const float4 pA = P[vA], pB = P[vB];
+    const float iwA = 1.0f / pA.w, iwB = 1.0f / pB.w;
+    atomic_add4(GP + vA, make_float4(gA0 * hx * iwA, gA1 * hy * iwA, 0.f,
+                                     -(gA0 * hx * pA.x + gA1 * hy * pA.y) * iwA * iwA));
+    atomic_add4(GP + vB, make_float4(gB0 * hx * iwB, gB1 * hy * iwB, 0.f,
+                                     -(gB0 * hx * pB.x + gB1 * hy * pB.y) * iwB * iwB));
+}
+
 struct AATerms {
     int role[4], tgt[4];
     float wt[4];
@@ -348,28 +378,7 @@ __device__ __forceinline__ void aa_bwd_terms(const float4* R, const float* Cc, c
         at.wt[q] = p.w;
         at.any = true;
         if (!GP || A != pix || p.clamped) continue;
-        float dLdw = 0.f;
-        for (int c = 0; c < C; ++c)
-            dLdw = fmaf(Gd[(long long)p.target * C + c] * gscale,
-                        Cc[(long long)p.src * C + c] - Cc[(long long)p.target * C + c], dLdw);
-        const float dLdt = dLdw * p.sign * boost;
-        const float den = p.eF - p.eO;
-        const float inv2 = 1.0f / (den * den);
-        const float dtF = -p.eO * inv2, dtO = p.eF * inv2;
-        const float2 ea = p.s[(p.k + 1) % 3], eb = p.s[(p.k + 2) % 3];
-        const float fF = dLdt * dtF * p.sgn, fO = dLdt * dtO * p.sgn;
-        const float gA0 = fmaf(fF, eb.y - p.cF.y, fO * (eb.y - p.cO.y));
-        const float gA1 = fmaf(fF, p.cF.x - eb.x, fO * (p.cO.x - eb.x));
-        const float gB0 = fmaf(fF, p.cF.y - ea.y, fO * (p.cO.y - ea.y));
-        const float gB1 = fmaf(fF, ea.x - p.cF.x, fO * (ea.x - p.cO.x));
-        const int vA = tri[3 * (long long)p.T + (p.k + 1) % 3], vB = tri[3 * (long long)p.T + (p.k + 2) % 3];
-        const float hx = 0.5f * (float)W, hy = 0.5f * (float)H;
-        const float4 pA = P[vA], pB = P[vB];
-        const float iwA = 1.0f / pA.w, iwB = 1.0f / pB.w;
-        atomic_add4(GP + vA, make_float4(gA0 * hx * iwA, gA1 * hy * iwA, 0.f,
-                                         -(gA0 * hx * pA.x + gA1 * hy * pA.y) * iwA * iwA));
-        atomic_add4(GP + vB, make_float4(gB0 * hx * iwB, gB1 * hy * iwB, 0.f,
-                                         -(gB0 * hx * pB.x + gB1 * hy * pB.y) * iwB * iwB));
+        aa_edge_grad(p, Cc, Gd, C, P, tri, GP, boost, gscale, W, H);
     }
 }
 

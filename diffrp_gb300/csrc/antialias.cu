@@ -171,23 +171,60 @@ __global__ void __launch_bounds__(256) aa_grad_copy_kernel(AAArgs a) {
     for (long long k = i; k < i + 4 && k < n; ++k) a.grad_color[k] = a.grad_out[k];
 }
 
+// One quad of lanes per listed pixel: lane q evaluates pair slot q (and
+// scatters its edge gradient when it owns the pair); the quad exchanges the
+// slot terms by shuffles and shares the channels (c = q, q + 4, ...).
 __global__ void __launch_bounds__(256) aa_bwd_list_kernel(AAArgs a) {
     const unsigned n = *a.list_count;
-    const int npix = a.H * a.W;
-    const int C = a.C;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int g = a.list[i];
-        const int b = g / npix, pix = g - b * npix;
-        const float4* R = reinterpret_cast<const float4*>(a.rast) + (long long)b * npix;
-        const float* Cc = a.color + (long long)b * npix * C;
-        const float* Gd = a.grad_out + (long long)b * npix * C;
-        const float4* P = reinterpret_cast<const float4*>(a.pos + (long long)b * a.pos_view_stride);
-        float4* GP = a.grad_pos ? reinterpret_cast<float4*>(a.grad_pos + (long long)b * a.pos_view_stride) : nullptr;
-        const float4* rec = reinterpret_cast<const float4*>(a.tri_rec) + (long long)b * a.num_triangles * 2;
+    const int npix = a.H * a.W, W = a.W, H = a.H, C = a.C;
+    const int lane = threadIdx.x & 31, q = lane & 3, qbase = lane & ~3;
+    const long long quads = ((long long)gridDim.x * blockDim.x) >> 2;
+    for (long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 2;; i += quads) {
+        const bool active = i < n;
+        if (!__any_sync(0xffffffffu, active)) break;  // warp-uniform exit (quads step together)
+        int role = 0, tgt = 0, b = 0, pix = 0;
+        float wt = 0.f;
+        if (active) {
+            const int g = a.list[i];
+            b = g / npix;
+            pix = g - b * npix;
+            const int py = pix / W, px = pix - py * W;
+            int A, B, ax, ay;
+            bool vert;
+            if (pair_slot(q, pix, px, py, W, H, A, B, ax, ay, vert)) {
+                const float4* R = reinterpret_cast<const float4*>(a.rast) + (long long)b * npix;
+                const float4 rs = R[pix], ro = R[A == pix ? B : A];
+                if (ro.w != rs.w) {
+                    AAPair p;
+                    const float4* rec = reinterpret_cast<const float4*>(a.tri_rec) + (long long)b * a.num_triangles * 2;
+                    aa_pair(rec, a.num_triangles, A, B, ax, ay, vert, A == pix ? rs : ro, A == pix ? ro : rs, p);
+                    if (p.valid) {
+                        role = p.target == pix ? 1 : 2;
+                        tgt = p.target;
+                        wt = p.w;
+                        if (a.grad_pos && A == pix && !p.clamped)
+                            aa_edge_grad(p, a.color + (long long)b * npix * C, a.grad_out + (long long)b * npix * C, C,
+                                         reinterpret_cast<const float4*>(a.pos + (long long)b * a.pos_view_stride),
+                                         a.tri, reinterpret_cast<float4*>(a.grad_pos + (long long)b * a.pos_view_stride),
+                                         a.boost, 1.0f, W, H);
+                    }
+                }
+            }
+        }
         AATerms at;
-        aa_bwd_terms(R, Cc, Gd, rec, a.num_triangles, a.W, a.H, C, P, a.tri, GP, a.boost, pix, at);
-        float* gc = a.grad_color + ((long long)b * npix + pix) * C;
-        for (int c = 0; c < C; ++c) gc[c] = aa_bwd_channel(at, Gd, C, pix, c);
+        at.any = false;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            at.role[k] = __shfl_sync(0xffffffffu, role, qbase | k);
+            at.tgt[k] = __shfl_sync(0xffffffffu, tgt, qbase | k);
+            at.wt[k] = __shfl_sync(0xffffffffu, wt, qbase | k);
+            at.any = at.any || at.role[k] != 0;
+        }
+        if (active) {
+            const float* Gd = a.grad_out + (long long)b * npix * C;
+            float* gc = a.grad_color + ((long long)b * npix + pix) * C;
+            for (int c = q; c < C; c += 4) gc[c] = aa_bwd_channel(at, Gd, C, pix, c);
+        }
     }
 }
 

@@ -340,23 +340,66 @@ __device__ __forceinline__ int find_item_by_pixel(const drp_batch_item* items, i
 // Antialias backward of the listed pixels (those a blending pair touches,
 // about the silhouettes): edge-vertex gradients (scattered once per pair by
 // its first pixel) and the pixel's antialiased colour gradient into aa_grad.
+// The list is short and each pixel's chain of dependent loads is long, so a
+// quad of lanes takes one pixel: lane q evaluates pair slot q (and scatters
+// its edge gradient when it owns the pair), the quad exchanges the slot terms
+// by shuffles, and the lanes share the channels (c = q, q + 4, ...).
 // Grid-stride over the device-side count, so the launch needs no host sync.
 __global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
     const unsigned n = *a.aa_count;
     const float gsc = a.grad_scale ? *a.grad_scale : 1.0f;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const long long gpix = a.aa_list[i];
-        const drp_batch_item& it = a.items[find_item_by_pixel(a.items, a.num_items, gpix)];
-        const int pix = (int)(gpix - it.pixel_offset);
-        const int C = it.channels;
-        const float* Gd = a.grad_out + it.image_offset;
+    const int lane = threadIdx.x & 31, q = lane & 3, qbase = lane & ~3;
+    const long long quads = ((long long)gridDim.x * blockDim.x) >> 2;
+    for (long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 2;; i += quads) {
+        const bool active = i < n;
+        if (!__any_sync(0xffffffffu, active)) break;  // warp-uniform exit (quads step together)
+        int role = 0, tgt = 0, pix = 0, C = 0;
+        float wt = 0.f;
+        const drp_batch_item* itp = nullptr;
+        if (active) {
+            const long long gpix = a.aa_list[i];
+            itp = &a.items[find_item_by_pixel(a.items, a.num_items, gpix)];
+            const drp_batch_item& it = *itp;
+            pix = (int)(gpix - it.pixel_offset);
+            C = it.channels;
+            const int W = it.width, H = it.height;
+            const int py = pix / W, px = pix - py * W;
+            int A, B, ax, ay;
+            bool vert;
+            if (pair_slot(q, pix, px, py, W, H, A, B, ax, ay, vert)) {
+                const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
+                const float4 rs = R[pix], ro = R[A == pix ? B : A];
+                if (ro.w != rs.w) {
+                    AAPair p;
+                    aa_pair(a.aa_rec + it.prim_offset * 2, it.tri_count, A, B, ax, ay, vert, A == pix ? rs : ro,
+                            A == pix ? ro : rs, p);
+                    if (p.valid) {
+                        role = p.target == pix ? 1 : 2;
+                        tgt = p.target;
+                        wt = p.w;
+                        if (A == pix && !p.clamped)
+                            aa_edge_grad(p, a.color + it.image_offset, a.grad_out + it.image_offset, C,
+                                         reinterpret_cast<const float4*>(a.pos) + it.pos_offset,
+                                         a.tri + 3 * (long long)it.tri_first,
+                                         reinterpret_cast<float4*>(a.grad_pos) + it.pos_offset, 1.0f, gsc, W, H);
+                    }
+                }
+            }
+        }
         AATerms at;
-        aa_bwd_terms(reinterpret_cast<const float4*>(a.rast) + it.pixel_offset, a.color + it.image_offset, Gd,
-                     a.aa_rec + it.prim_offset * 2, it.tri_count, it.width, it.height, C,
-                     reinterpret_cast<const float4*>(a.pos) + it.pos_offset, a.tri + 3 * (long long)it.tri_first,
-                     reinterpret_cast<float4*>(a.grad_pos) + it.pos_offset, 1.0f, pix, at, gsc);
-        float* g2 = a.aa_grad + it.image_offset + (long long)pix * C;
-        for (int c = 0; c < C; ++c) g2[c] = aa_bwd_channel(at, Gd, C, pix, c, gsc);
+        at.any = false;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            at.role[k] = __shfl_sync(0xffffffffu, role, qbase | k);
+            at.tgt[k] = __shfl_sync(0xffffffffu, tgt, qbase | k);
+            at.wt[k] = __shfl_sync(0xffffffffu, wt, qbase | k);
+            at.any = at.any || at.role[k] != 0;
+        }
+        if (active) {
+            const float* Gd = a.grad_out + itp->image_offset;
+            float* g2 = a.aa_grad + itp->image_offset + (long long)pix * C;
+            for (int c = q; c < C; c += 4) g2[c] = aa_bwd_channel(at, Gd, C, pix, c, gsc);
+        }
     }
 }
 
