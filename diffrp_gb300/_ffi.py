@@ -86,10 +86,26 @@ def call(name, *args):
     return status
 
 
+_sizes = {}
+
+
 def size_out(name, *args):
-    out = ctypes.c_size_t(0)
-    call(name, *args, ctypes.byref(out))
-    return out.value
+    """A workspace-size query (a pure function of its integer arguments),
+    answered from a cache after the first call."""
+    key = (name,) + args
+    v = _sizes.get(key)
+    if v is None:
+        out = ctypes.c_size_t(0)
+        call(name, *args, ctypes.byref(out))
+        v = _sizes[key] = out.value
+    return v
+
+
+def stream_of(device):
+    """Raw cudaStream_t (as an int) of the current torch stream on device."""
+    import torch
+    idx = device.index if device.index is not None else torch.cuda.current_device()
+    return torch._C._cuda_getCurrentRawStream(idx)
 
 
 def kernel_launches():

@@ -238,7 +238,7 @@ class BatchRenderer:
         npix = self.total_pixels
         self._fwd_gen += 1
         ws = self._workspace(cap)
-        stream = torch.cuda.current_stream(self.device).cuda_stream
+        stream = _ffi.stream_of(self.device)
         args = (self._items_dev.data_ptr(), len(self.items), self._pmap.data_ptr(), self.prim_blocks,
                 self._xmap.data_ptr(), self.pixel_blocks, self.total_prims, self.total_tiles, pos.data_ptr(),
                 self.tri.data_ptr(), attr.data_ptr(), self.nbr.data_ptr(), self.tile_log2, self.threads_per_tri)
@@ -280,7 +280,7 @@ class BatchRenderer:
         grad_scale: a one-element device tensor multiplying grad_out.
         aa_flags: the antialias slot bits that forward wrote, or None."""
         ws = self._workspace(0)  # the backward reads no tile list
-        stream = torch.cuda.current_stream(self.device).cuda_stream
+        stream = _ffi.stream_of(self.device)
         flags = REUSE_AA_RECORDS if gen is not None and gen == self._rec_gen and ws is self._rec_ws else 0
         aa_grad = None if aa_flags is None else torch.empty(self.image_floats, dtype=torch.float32,
                                                             device=self.device)

@@ -23,7 +23,7 @@ class _L1(torch.autograd.Function):
         loss = torch.empty((), dtype=torch.float32, device=p.device)
         ws = torch.empty(_ffi.size_out("drp_l1_loss_workspace_size", n), dtype=torch.uint8, device=p.device)
         _ffi.call("drp_l1_loss_fwd", ws.data_ptr(), ws.numel(), p.data_ptr(), t.data_ptr(), n, 1.0 / n,
-                  loss.data_ptr(), grad.data_ptr(), torch.cuda.current_stream(p.device).cuda_stream)
+                  loss.data_ptr(), grad.data_ptr(), _ffi.stream_of(p.device))
         ctx.save_for_backward(grad)
         ctx.target_grad = target.requires_grad
         return loss

@@ -45,7 +45,7 @@ def _ptr(t):
 
 
 def _stream(device):
-    return torch.cuda.current_stream(device).cuda_stream
+    return _ffi.stream_of(device)
 
 
 def _capturing():
@@ -109,6 +109,7 @@ class RasterizeCudaContext:
         self._capacity = 0
         self._sized = False
         self._pending = []  # (event, pinned stats copy) of raster calls not read back yet
+        self._calls = 0
         self._pinned_free = []
         self._topo_ws = None
         self.last_list_entries = 0
@@ -191,7 +192,11 @@ class RasterizeCudaContext:
                 self._capacity = max(self._capacity, cap)
             self._sized = True
         else:
-            self._queue_stats()
+            # read the stats back on the first calls, then on every 8th (an
+            # overflowing call is still exact; only the growth waits)
+            self._calls += 1
+            if self._calls <= 8 or self._calls % 8 == 0:
+                self._queue_stats()
 
     def topology_workspace(self, F):
         nbytes = _ffi.size_out("drp_topology_workspace_size", F)

@@ -31,5 +31,5 @@ class EdgeGradientFn(torch.autograd.Function):
         out = torch.empty((H, W, 2), dtype=torch.float32, device=frag_xy.device)
         _ffi.call("drp_edge_gradient_bwd", fxy.data_ptr(), txy.data_ptr(), txy.shape[0], r.data_ptr(),
                   rgb_c.data_ptr(), rgb_c.shape[-1], g.data_ptr(), H, W, out.data_ptr(),
-                  torch.cuda.current_stream(frag_xy.device).cuda_stream)
+                  _ffi.stream_of(frag_xy.device))
         return out.to(frag_xy.dtype), None, None, grad_output.clone()

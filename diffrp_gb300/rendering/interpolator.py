@@ -35,7 +35,7 @@ class _SparseInterp(torch.autograd.Function):
         n, C = vi.shape[0], vb.shape[1]
         out = torch.empty((n, C), dtype=torch.float32, device=vb.device)
         _ffi.call("drp_interpolate_sparse_fwd", vb.data_ptr(), vb.shape[0], C, vi.data_ptr(), tri_idx.data_ptr(), n,
-                  out.data_ptr(), torch.cuda.current_stream(vb.device).cuda_stream)
+                  out.data_ptr(), _ffi.stream_of(vb.device))
         ctx.save_for_backward(vb, vi, tri_idx)
         return out
 
@@ -47,7 +47,7 @@ class _SparseInterp(torch.autograd.Function):
         gvi = torch.empty_like(vi)
         _ffi.call("drp_interpolate_sparse_bwd", vb.data_ptr(), vb.shape[0], vb.shape[1], vi.data_ptr(),
                   tri_idx.data_ptr(), vi.shape[0], g.data_ptr(), gvb.data_ptr(), gvi.data_ptr(),
-                  torch.cuda.current_stream(vb.device).cuda_stream)
+                  _ffi.stream_of(vb.device))
         return gvb, gvi, None
 
 
