@@ -508,9 +508,11 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
             }
         }
     }
-    float pv[12];
+    // u and v do not depend on clip z, so each vertex gradient is (x, y, 0, w):
+    // nine values to reduce
+    float pv[9];
 #pragma unroll
-    for (int k = 0; k < 12; ++k) pv[k] = 0.f;
+    for (int k = 0; k < 9; ++k) pv[k] = 0.f;
     if (t >= 0) {
         const int py = pix / W, px = pix - py * W;
         const float X = fmaf((float)(2 * px + 1), __frcp_rn((float)W), -1.0f);
@@ -519,17 +521,16 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
         uv_grad_fast(P[i0], P[i1], P[i2], X, Y, gu, gv, g3);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            pv[4 * k] = g3[k].x;
-            pv[4 * k + 1] = g3[k].y;
-            pv[4 * k + 2] = g3[k].z;
-            pv[4 * k + 3] = g3[k].w;
+            pv[3 * k] = g3[k].x;
+            pv[3 * k + 1] = g3[k].y;
+            pv[3 * k + 2] = g3[k].w;
         }
     }
-    seg_reduce<12>(seg, pv);
+    seg_reduce<9>(seg, pv);
     if (t >= 0 && seg.head) {
-        atomic_add4(GP + i0, make_float4(pv[0], pv[1], pv[2], pv[3]));
-        atomic_add4(GP + i1, make_float4(pv[4], pv[5], pv[6], pv[7]));
-        atomic_add4(GP + i2, make_float4(pv[8], pv[9], pv[10], pv[11]));
+        atomic_add4(GP + i0, make_float4(pv[0], pv[1], 0.f, pv[2]));
+        atomic_add4(GP + i1, make_float4(pv[3], pv[4], 0.f, pv[5]));
+        atomic_add4(GP + i2, make_float4(pv[6], pv[7], 0.f, pv[8]));
     }
 }
 
