@@ -113,7 +113,9 @@ def tune_batch(renderer, pos, attr, reps=5, candidates=None):
     its own items for every (tile size, threads per primitive) candidate and
     keep the fastest; returns the choice with the measured times."""
     if candidates is None:
-        candidates = [(t, p) for t in TILE_CHOICES for p in (0, 4)]
+        # pixel-parallel, or 1 / 2 / 4 threads per primitive (tiny triangles
+        # favour one thread walking each small bounding box)
+        candidates = [(t, p) for t in TILE_CHOICES for p in (0, 1, 2, 4)]
     stream = torch.cuda.current_stream(pos.device)
     times = {}
     best = None
