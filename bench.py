@@ -98,6 +98,9 @@ class Step:
         return loss
 
 
+WORKLOAD_SINGLE = "icosphere5-displaced 20480 tris, 1024x1024, 8 ch, L1 loss, fwd+bwd (single mesh, full gradients)"
+
+
 def clip_space(verts, mvp):
     """Clip-space positions [v, 1] @ mvp^T of (V, 3) vertices: one addmm."""
     import torch
@@ -619,7 +622,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": H * W / base["value"] / 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "icosphere5-displaced 20480 tris, 1024x1024, 8 ch, L1 loss, fwd+bwd",
+        "config": {"workload": WORKLOAD_SINGLE,
                    "global_batch": 1, "resolution": [H, W], "channels": C, "parallelism": "cpu threads"},
         "cpu_baseline": base,
         "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -808,8 +811,7 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": W_, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded icosphere, attributes and target)",
-            "config": {"workload": "icosphere5-displaced 20480 tris, 1024x1024, 8 ch, L1 loss, fwd+bwd "
-                                   "(single mesh, full gradients)",
+            "config": {"workload": WORKLOAD_SINGLE,
                        "global_batch": world, "resolution": [H, W], "channels": C,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "flushed between steps (256 MiB write outside the timed events)",
