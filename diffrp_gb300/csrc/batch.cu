@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(256) batch_aa_fwd_kernel(BatchArgs a) {
 // output (written when out is set), sign gradient and |error| sum; one
 // partial per 256-pixel block, added in index order by the final reduction
 // (reproducible loss).
-__global__ void __launch_bounds__(256) batch_aa_l1_kernel(BatchArgs a) {
+__global__ void __launch_bounds__(256, 5) batch_aa_l1_kernel(BatchArgs a) {
     __shared__ float warp_sum[8];
     const int2 blk = a.pix_blocks[blockIdx.x];
     const drp_batch_item& it = a.items[blk.x];
