@@ -286,14 +286,8 @@ int launch_aa_bwd(const AAArgs& a, cudaStream_t s) {
         const long long n4 = ((long long)a.B * npix * a.C + 3) / 4;
         aa_grad_copy_kernel<<<(unsigned)((n4 + 255) / 256), 256, 0, s>>>(a);
         drp_note_launch();
-        static int grid = 0;
-        if (grid == 0) {
-            int dev = 0, sms = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            grid = (sms > 0 ? sms : 1) * 4;
-        }
-        aa_bwd_list_kernel<<<grid, 256, 0, s>>>(a);
+        const int sms = drp_current_sm_count();
+        aa_bwd_list_kernel<<<(sms > 0 ? sms : 1) * 4, 256, 0, s>>>(a);
         drp_note_launch();
         return 0;
     }

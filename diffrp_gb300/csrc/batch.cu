@@ -17,6 +17,8 @@
 // antialias colour gradient, the attribute gradient (interpolation backward)
 // and the vertex gradient (rasterisation backward), scattered with
 // warp-segmented float4 atomics.
+#include <atomic>
+
 #include "../../include/diffrp_gb300.h"
 #include "aa_core.cuh"
 #include "drp_internal.h"
@@ -594,14 +596,17 @@ static void carve(BatchArgs& a, void* ws, const BatchLayout& L) {
 template <int TL, int TPT>
 static void launch_batch_fine(const BatchArgs& a, cudaStream_t s) {
     constexpr int NT = (1 << (2 * TL)) < 256 ? (1 << (2 * TL)) : 256;
-    static int grid = 0;
-    if (grid == 0) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // persistent grid: every resident CTA slot of the device (occupancy per
+    // kernel instantiation is device-independent for one architecture)
+    static std::atomic<int> per_sm{0};
+    int per = per_sm.load(std::memory_order_relaxed);
+    if (per == 0) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_fine_kernel<TL, TPT>, NT, 0);
-        grid = sms * (per > 0 ? per : 1);
+        per = per > 0 ? per : 1;
+        per_sm.store(per, std::memory_order_relaxed);
     }
+    const int sms = drp_current_sm_count();
+    const long long grid = (long long)(sms > 0 ? sms : 1) * per;
     const long long g = a.total_tiles < grid ? a.total_tiles : grid;
     if (g > 0) {
         batch_fine_kernel<TL, TPT><<<(unsigned)g, NT, 0, s>>>(a);
@@ -669,13 +674,8 @@ int launch_batch_backward(BatchArgs a, void* ws, const BatchLayout& L, bool reus
         drp_note_launch();
     }
     if (a.aa_flags && a.n_pix_blocks > 0) {
-        static int grid = 0;
-        if (grid == 0) {
-            int dev = 0, sms = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            grid = (sms > 0 ? sms : 1) * 4;
-        }
+        const int sms = drp_current_sm_count();
+        const long long grid = (long long)(sms > 0 ? sms : 1) * 4;
         const long long g = a.n_pix_blocks < grid ? a.n_pix_blocks : grid;
         batch_aa_bwd_kernel<<<(unsigned)g, 256, 0, s>>>(a);
         drp_note_launch();

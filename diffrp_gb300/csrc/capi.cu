@@ -69,6 +69,24 @@ std::atomic<unsigned long long> g_kernel_launches{0};
 
 void drp_note_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
 
+namespace {
+constexpr int kSmCacheDevices = 64;
+std::atomic<int> g_sm_count[kSmCacheDevices];
+}
+
+int drp_current_sm_count() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 0;
+    if (dev < kSmCacheDevices) {
+        const int v = g_sm_count[dev].load(std::memory_order_relaxed);
+        if (v > 0) return v;
+    }
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (dev < kSmCacheDevices && sms > 0) g_sm_count[dev].store(sms, std::memory_order_relaxed);
+    return sms;
+}
+
 DRP_API unsigned long long drp_kernel_launches(void) { return g_kernel_launches.load(std::memory_order_relaxed); }
 
 DRP_API int drp_abi_version(void) { return DRP_ABI_VERSION; }

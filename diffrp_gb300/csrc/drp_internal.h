@@ -140,3 +140,5 @@ void drp_set_last_error(const char* msg);
 int drp_check_launch(const char* what);
 // Count one kernel launch enqueued by this library (drp_kernel_launches).
 void drp_note_launch();
+// Multiprocessors of the current device, cached per device (0 without one).
+int drp_current_sm_count();

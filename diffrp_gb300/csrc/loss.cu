@@ -96,14 +96,9 @@ void launch_l1_final(const float* partial, long long nblocks, float scale, float
 // Blocks for n elements: enough to fill every SM, never more than one
 // float4 group per thread.
 static long long l1_blocks(long long n) {
-    static int max_blocks = 0;
-    if (max_blocks == 0) {
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) return 1;  // no device: callers fail at launch
-        max_blocks = sms * kLossBlocksPerSM;
-    }
+    const int sms = drp_current_sm_count();
+    if (sms <= 0) return 1;  // no device: callers fail at launch
+    const long long max_blocks = (long long)sms * kLossBlocksPerSM;
     const long long need = ((n + 3) / 4 + kLossThreads - 1) / kLossThreads;
     return need < max_blocks ? (need > 0 ? need : 1) : max_blocks;
 }
@@ -115,7 +110,10 @@ extern "C" __attribute__((visibility("default"))) int drp_l1_loss_workspace_size
         drp_set_last_error("drp_l1_loss_workspace_size: bad arguments");
         return 1;
     }
-    *bytes = (size_t)drp::l1_blocks(n) * sizeof(float) + 256;
+    // the most blocks any device uses: one float4 group per thread (the grid
+    // is capped below that by the SM count), so the size is device-independent
+    const long long most = ((n + 3) / 4 + drp::kLossThreads - 1) / drp::kLossThreads;
+    *bytes = (size_t)(most > 0 ? most : 1) * sizeof(float) + 256;
     return 0;
 }
 
