@@ -77,10 +77,23 @@ struct BatchArgs {
 constexpr int kSetupCount = 0, kSetupFill = 1, kSetupBins = 2;
 
 template <int TILE_LOG2, int MODE>
-__global__ void __launch_bounds__(256) batch_setup_bin_kernel(BatchArgs a) {
+__global__ void __launch_bounds__(512) batch_setup_bin_kernel(BatchArgs a) {
     constexpr bool FILL = MODE == kSetupFill;
     const int2 blk = a.prim_blocks[blockIdx.x];
     const drp_batch_item& it = a.items[blk.x];
+    // Count / bin launches with antialias records use 512 threads: the upper
+    // half writes the records of the block's 256 triangles while the lower
+    // half sets them up and bins them (two shorter chains of dependent loads
+    // instead of one).  Whole warps take one side.
+    if (threadIdx.x >= 256) {
+        const long long jr = (long long)blk.y * 256 + (threadIdx.x - 256);
+        if (!FILL && a.aa_records && jr < it.tri_count)
+            aa_tri_record(reinterpret_cast<const float4*>(a.pos) + it.pos_offset,
+                          a.tri + 3 * (long long)it.tri_first, a.nbr ? a.nbr + 3 * (long long)it.tri_first : nullptr,
+                          jr, it.tri_count, it.num_vertices, it.width, it.height,
+                          a.aa_rec + (it.prim_offset + jr) * 2);
+        return;
+    }
     const long long j = (long long)blk.y * 256 + threadIdx.x;
     if (j >= it.tri_count) return;
     const long long pidx = it.prim_offset + j;
@@ -111,12 +124,6 @@ __global__ void __launch_bounds__(256) batch_setup_bin_kernel(BatchArgs a) {
         bin_box<TILE_LOG2>(bx, live, it.tiles_x, a.tile_cursor + it.tile_offset, a.tile_list, a.list_capacity,
                            (uint32_t)pidx);
     } else {
-        // The antialias triangle record rides along with the setup pass (same
-        // triangle, same vertices); a raster-only forward skips it.
-        if (a.aa_records)
-            aa_tri_record(reinterpret_cast<const float4*>(a.pos) + it.pos_offset,
-                          a.tri + 3 * (long long)it.tri_first, a.nbr ? a.nbr + 3 * (long long)it.tri_first : nullptr,
-                          j, it.tri_count, it.num_vertices, it.width, it.height, a.aa_rec + pidx * 2);
         if (MODE == kSetupBins)
             bin_box<TILE_LOG2>(bx, live, it.tiles_x, a.tile_count + it.tile_offset,
                                a.tile_list + (unsigned long long)it.tile_offset * a.bin_depth, 0, (uint32_t)pidx,
@@ -617,10 +624,10 @@ static void launch_batch_fine(const BatchArgs& a, cudaStream_t s) {
 template <int TL>
 static void launch_batch_raster(const BatchArgs& a, cudaStream_t s) {
     if (a.n_prim_blocks > 0 && a.bin_depth) {
-        batch_setup_bin_kernel<TL, kSetupBins><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+        batch_setup_bin_kernel<TL, kSetupBins><<<(unsigned)a.n_prim_blocks, a.aa_records ? 512 : 256, 0, s>>>(a);
         drp_note_launch();
     } else if (a.n_prim_blocks > 0) {
-        batch_setup_bin_kernel<TL, kSetupCount><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+        batch_setup_bin_kernel<TL, kSetupCount><<<(unsigned)a.n_prim_blocks, a.aa_records ? 512 : 256, 0, s>>>(a);
         drp_note_launch();
         launch_tile_scan(a.tile_count, a.tile_offset, a.tile_cursor, a.total_tiles, a.chunk_sums,
                          reinterpret_cast<unsigned long long*>(a.stats), s);
