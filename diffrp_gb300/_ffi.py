@@ -76,10 +76,36 @@ def load():
     return _lib
 
 
+_fast = None
+
+
+def _fast_table():
+    """Entry points of the CPython fast path (csrc/pyext.cpp), or {} when it
+    was not built; the library itself must already be loaded."""
+    global _fast
+    if _fast is None:
+        table = {}
+        path = os.path.join(os.path.dirname(lib_path()), "_drp_fast.so")
+        if os.path.exists(path) and not os.environ.get("DRP_NO_FAST_PATH"):
+            import importlib.machinery
+            import importlib.util
+            try:
+                loader = importlib.machinery.ExtensionFileLoader("_drp_fast", path)
+                spec = importlib.util.spec_from_file_location("_drp_fast", path, loader=loader)
+                mod = importlib.util.module_from_spec(spec)
+                loader.exec_module(mod)
+                table = {k: getattr(mod, k) for k in dir(mod) if k.startswith("drp_")}
+            except ImportError:
+                table = {}
+        _fast = table
+    return _fast
+
+
 def call(name, *args):
     """Call an entry point; a non-zero status becomes RuntimeError."""
     lib = load()
-    status = getattr(lib, name)(*args)
+    fn = (_fast if _fast is not None else _fast_table()).get(name)
+    status = fn(*args) if fn is not None else getattr(lib, name)(*args)
     if status != 0:
         msg = lib.drp_last_error().decode(errors="replace")
         raise RuntimeError("%s failed (%s): %s" % (name, lib.drp_status_string(status).decode(), msg))

@@ -78,7 +78,39 @@ def build(verbose=False, force=False):
     target = lib_path()
     if force or jobs or _stale(target, objs):
         run([cc] + ARCH + ["-shared", "-o", target] + objs + ["-lcudart"])
+    build_fast(force or bool(jobs), verbose)
     return target
+
+
+FAST_NAME = "_drp_fast.so"
+
+
+def fast_path():
+    return os.path.join(LIBDIR, FAST_NAME)
+
+
+def build_fast(force=False, verbose=False):
+    """The CPython fast path (csrc/pyext.cpp, host C++ only) linked against
+    libdiffrp_gb300.so.  Optional: without Python headers or a C++ compiler
+    the ctypes binding is used alone."""
+    import sysconfig
+    src = os.path.join(CSRC, "pyext.cpp")
+    out = fast_path()
+    header = os.path.join(os.path.dirname(HERE), "include", "diffrp_gb300.h")
+    if not force and not _stale(out, [src, header, lib_path()]):
+        return out
+    inc = sysconfig.get_paths().get("include")
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx or not inc or not os.path.exists(os.path.join(inc, "Python.h")):
+        return None
+    cmd = [cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-fvisibility=hidden", "-I", inc, src, "-o", out,
+           "-L", LIBDIR, "-ldiffrp_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        if verbose:
+            print("CPython fast path not built:", r.stderr[-2000:])
+        return None
+    return out
 
 
 if __name__ == "__main__":

@@ -69,3 +69,17 @@ def test_workspace_queries_and_validation(lib):
     assert st == 1 and b"threads_per_tri" in lib.drp_last_error()
     with pytest.raises(RuntimeError, match="invalid argument"):
         _ffi.call("drp_interpolate_fwd", None, 0, 0, 0, None, None, None, 0, 1, 4, 4, None, 0, None, None, None)
+
+
+def test_fast_path_matches_ctypes_on_validation(lib):
+    """The CPython fast path (when built) wraps entry points the header
+    declares and reports the same status and message as ctypes."""
+    from diffrp_gb300 import _ffi
+    table = _ffi._fast_table()
+    if not table:
+        pytest.skip("CPython fast path not built (no Python headers)")
+    assert set(table) <= set(declared_symbols())
+    bad = (None, 0, None, None, 0, 1.0, None, None, None)  # drp_l1_loss_fwd with nothing to do
+    assert table["drp_l1_loss_fwd"](*bad) == lib.drp_l1_loss_fwd(*bad) == 1
+    with pytest.raises(TypeError):
+        table["drp_l1_loss_fwd"](*bad[:-1])
