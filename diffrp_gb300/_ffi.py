@@ -18,8 +18,8 @@ _SZ = ctypes.POINTER(ctypes.c_size_t)
 _SIGNATURES = {
     "drp_abi_version": [],
     "drp_raster_workspace_size": [_I, _LL, _I, _I, _I, _ULL, _SZ],
-    "drp_rasterize_fwd": [_P, ctypes.c_size_t, _P, _LL, _LL, _P, _LL, _I, _P, _LL, _I, _I, _I, _I, _ULL, _P, _P,
-                          _P, _P, _P],
+    "drp_rasterize_fwd": [_P, ctypes.c_size_t, _P, _LL, _LL, _P, _LL, _I, _P, _LL, _I, _I, _I, _I, _ULL,
+                          ctypes.c_uint, _P, _P, _P, _P, _P],
     "drp_rasterize_bwd": [_P, _LL, _LL, _P, _LL, _I, _I, _I, _P, _P, _P, _P, _P],
     "drp_interpolate_fwd": [_P, _LL, _LL, _I, _P, _P, _P, _LL, _I, _I, _I, _P, _I, _P, _P, _P],
     "drp_interpolate_bwd": [_P, _LL, _LL, _I, _P, _P, _P, _LL, _I, _I, _I, _P, _I, _P, _P, _P, _P, _P, _P],

@@ -120,7 +120,7 @@ DRP_API int drp_raster_workspace_size(int num_views, long long max_view_tris, in
 DRP_API int drp_rasterize_fwd(void* workspace, size_t workspace_bytes, const float* pos, long long pos_view_stride,
                               long long num_vertices, const int* tri, long long num_triangles, int num_views,
                               const int* ranges, long long max_view_tris, int height, int width, int tile_log2,
-                              int threads_per_tri, unsigned long long list_capacity,
+                              int threads_per_tri, unsigned long long list_capacity, unsigned bin_depth,
                               const unsigned long long* prev_key, float* rast, float* rast_db,
                               unsigned long long* out_key, void* stream) {
     if (num_views <= 0) return fail(DRP_STATUS_INVALID_ARGUMENT, "num_views must be positive");
@@ -143,6 +143,12 @@ DRP_API int drp_rasterize_fwd(void* workspace, size_t workspace_bytes, const flo
         return fail(DRP_STATUS_INVALID_ARGUMENT, "pos / rast / rast_db must be 16-byte aligned float4 rows");
     if (!workspace || !aligned(workspace, 256)) return fail(DRP_STATUS_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
     if (list_capacity > 0x7fffffffull) return fail(DRP_STATUS_INVALID_ARGUMENT, "list_capacity above 2^31 - 1");
+    {
+        const long long tiles = (long long)num_views * (((long long)width + (1 << tile_log2) - 1) >> tile_log2) *
+                                (((long long)height + (1 << tile_log2) - 1) >> tile_log2);
+        if (bin_depth && (unsigned long long)tiles * bin_depth > list_capacity)
+            return fail(DRP_STATUS_INVALID_ARGUMENT, "list_capacity below tiles * bin_depth");
+    }
     const RasterLayout L = raster_layout(num_views, max_view_tris, height, width, tile_log2, list_capacity);
     if (workspace_bytes < L.total)
         return fail(DRP_STATUS_WORKSPACE_TOO_SMALL, "raster workspace needs %zu bytes, got %zu", L.total, workspace_bytes);
@@ -163,6 +169,7 @@ DRP_API int drp_rasterize_fwd(void* workspace, size_t workspace_bytes, const flo
     a.tiles_y = (height + (1 << tile_log2) - 1) >> tile_log2;
     a.threads_per_tri = threads_per_tri;
     a.list_capacity = list_capacity;
+    a.bin_depth = bin_depth;
     a.prev_key = prev_key;
     a.rast = rast;
     a.rast_db = rast_db;

@@ -36,6 +36,7 @@ struct RasterArgs {
     int H, W;
     int tiles_x, tiles_y, tile_log2, threads_per_tri;
     unsigned long long list_capacity;
+    uint32_t bin_depth;  // 0: exact tile lists (count, scan, fill); > 0: fixed-depth bins (one pass)
     const unsigned long long* prev_key;
     float* rast;
     float* rast_db;

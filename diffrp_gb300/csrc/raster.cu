@@ -41,10 +41,14 @@ __device__ __forceinline__ ViewRange view_range(const int* ranges, int b, int F)
 }
 
 // One thread per (view, triangle slot): build the primitive record, then
-// count (FILL = false) or list (FILL = true) the tiles it overlaps.  The fill
-// pass re-reads the record written by the count pass.
-template <int TILE_LOG2, bool FILL>
+// count (kSetupCount) or list (kSetupFill, after the scan; it re-reads the
+// record written by the count pass) the tiles it overlaps, or both at once
+// into fixed-depth bins (kSetupBins).
+constexpr int kSetupCount = 0, kSetupFill = 1, kSetupBins = 2;
+
+template <int TILE_LOG2, int MODE>
 __global__ void __launch_bounds__(256) setup_bin_kernel(RasterArgs a) {
+    constexpr bool FILL = MODE == kSetupFill;
     const int b = blockIdx.y;
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= a.max_view_tris) return;
@@ -80,6 +84,10 @@ __global__ void __launch_bounds__(256) setup_bin_kernel(RasterArgs a) {
     if (FILL)
         bin_box<TILE_LOG2>(bx, live, a.tiles_x, a.ws.tile_cursor + b * tiles, a.ws.tile_list, a.list_capacity,
                            (uint32_t)pidx);
+    else if (MODE == kSetupBins)
+        bin_box<TILE_LOG2>(bx, live, a.tiles_x, a.ws.tile_count + b * tiles,
+                           a.ws.tile_list + (unsigned long long)(b * tiles) * a.bin_depth, 0, (uint32_t)pidx,
+                           a.bin_depth);
     else
         bin_box<TILE_LOG2>(bx, live, a.tiles_x, a.ws.tile_count + b * tiles, nullptr, 0, 0);
 }
@@ -120,10 +128,16 @@ fine_raster_kernel(RasterArgs a) {
     const long long tidx = (long long)b * a.tiles_x * a.tiles_y + tile;
     FineTile ft;
     ft.recs = reinterpret_cast<const int4*>(a.ws.prims);
-    const uint32_t off = a.ws.tile_offset[tidx];
     ft.cnt = a.ws.tile_count[tidx];
-    ft.list = a.ws.tile_list + off;
-    ft.overflow = (unsigned long long)off + ft.cnt > a.list_capacity;
+    if (a.bin_depth) {
+        ft.list = a.ws.tile_list + (unsigned long long)tidx * a.bin_depth;
+        ft.overflow = ft.cnt > a.bin_depth;
+        if (ft.overflow && threadIdx.x == 0) atomicMax(a.ws.stats + 3, ft.cnt);  // sizes the next depth
+    } else {
+        const uint32_t off = a.ws.tile_offset[tidx];
+        ft.list = a.ws.tile_list + off;
+        ft.overflow = (unsigned long long)off + ft.cnt > a.list_capacity;
+    }
     ft.scan_base = (long long)b * a.max_view_tris;
     ft.scan_count = a.max_view_tris;
     ft.tx0 = (tile % a.tiles_x) << TILE_LOG2;
@@ -218,12 +232,17 @@ static void launch_fine(const RasterArgs& a, int tpt, cudaStream_t s) {
 template <int TL>
 static void launch_bin(const RasterArgs& a, cudaStream_t s) {
     dim3 grid((unsigned)((a.max_view_tris + 255) / 256), (unsigned)a.B);
-    setup_bin_kernel<TL, false><<<grid, 256, 0, s>>>(a);
+    if (a.bin_depth) {
+        setup_bin_kernel<TL, kSetupBins><<<grid, 256, 0, s>>>(a);
+        drp_note_launch();
+        return;
+    }
+    setup_bin_kernel<TL, kSetupCount><<<grid, 256, 0, s>>>(a);
     drp_note_launch();
     const long long n = (long long)a.B * a.tiles_x * a.tiles_y;
     launch_tile_scan(a.ws.tile_count, a.ws.tile_offset, a.ws.tile_cursor, n, a.ws.chunk_sums,
                      reinterpret_cast<unsigned long long*>(a.ws.stats), s);
-    setup_bin_kernel<TL, true><<<grid, 256, 0, s>>>(a);
+    setup_bin_kernel<TL, kSetupFill><<<grid, 256, 0, s>>>(a);
     drp_note_launch();
 }
 

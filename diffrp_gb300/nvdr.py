@@ -108,11 +108,13 @@ class RasterizeCudaContext:
         self._retired = []  # replaced buffers, kept alive for CUDA graphs captured on them
         self._capacity = 0
         self._sized = False
-        self._pending = []  # (event, pinned stats copy) of raster calls not read back yet
+        self._pending = []  # (event, pinned stats copy, call shape, bin depth) not read back yet
         self._calls = 0
+        self._depth = {}  # call shape (views, triangles, H, W, tile) -> fixed-depth bin size
         self._pinned_free = []
         self._topo_ws = None
         self.last_list_entries = 0
+        self.last_max_tile = 0
 
     # -- workspace management ------------------------------------------------
     def _workspace(self, nbytes):
@@ -123,20 +125,36 @@ class RasterizeCudaContext:
             self._ws = torch.empty(n, dtype=torch.uint8, device=self.device)
         return self._ws
 
+    def _choose_depth(self, shape, max_tile, needed):
+        """Fixed-depth bins for a call shape, while they stay near the exact
+        lists' size (else 0: keep exact lists)."""
+        B, _, H, W, tl = shape
+        tiles = B * ((W + (1 << tl) - 1) >> tl) * ((H + (1 << tl) - 1) >> tl)
+        depth = int(max_tile * 1.25) + 8
+        return depth if tiles * depth <= 2 * needed + (4 << 20) else 0
+
+    def _note_stats(self, shape, depth, needed, err, max_tile):
+        if depth == 0:
+            self.last_list_entries = needed
+            if needed > self._capacity:
+                self._capacity = int(needed * 1.25) + 1024
+            if shape not in self._depth:
+                self._depth[shape] = self._choose_depth(shape, max_tile, needed)
+        elif err & 2:  # a bin overflowed (still exact, but slow): deeper bins next time
+            self._depth[shape] = max(int(depth * 1.5), int(max_tile * 1.25) + 8)
+
     def _poll_stats(self):
-        """Grow the list capacity from every finished call's stats (a call
-        that needed more than it had was still exact, through the slow
-        per-tile scan; the next calls get room)."""
+        """Grow the list capacity / bin depth from every finished call's
+        stats (a call that needed more than it had was still exact, through
+        the slow per-tile scan; the next calls get room)."""
         keep = []
-        for ev, pinned in self._pending:
+        for ev, pinned, shape, depth in self._pending:
             if ev.query():
-                needed = int(pinned[0])
-                self.last_list_entries = needed
-                if needed > self._capacity:
-                    self._capacity = int(needed * 1.25) + 1024
+                w = pinned.view(torch.int32)
+                self._note_stats(shape, depth, int(pinned[0]), int(w[2]), int(w[3]))
                 self._pinned_free.append(pinned)
             else:
-                keep.append((ev, pinned))
+                keep.append((ev, pinned, shape, depth))
         self._pending = keep
 
     def _read_stats_sync(self):
@@ -144,9 +162,10 @@ class RasterizeCudaContext:
         st = self._ws[:16].view(torch.int64).cpu()
         needed = int(st[0].item())
         err = int(st[1].item()) & 0xffffffff
+        self.last_max_tile = int(st[1].item()) >> 32
         return needed, err
 
-    def _queue_stats(self):
+    def _queue_stats(self, shape, depth):
         if _capturing():
             return
         pinned = self._pinned_free.pop() if self._pinned_free else torch.empty(2, dtype=torch.int64,
@@ -154,7 +173,7 @@ class RasterizeCudaContext:
         pinned.copy_(self._ws[:16].view(torch.int64), non_blocking=True)
         ev = torch.cuda.Event()
         ev.record(torch.cuda.current_stream(self.device))
-        self._pending.append((ev, pinned))
+        self._pending.append((ev, pinned, shape, depth))
         if len(self._pending) > 64:  # bound the queue: wait for the oldest read-back
             self._pending[0][0].synchronize()
             self._poll_stats()
@@ -171,10 +190,18 @@ class RasterizeCudaContext:
         first = not self._sized
         if first:
             cap = max(cap, 4 * B * max_view_tris + 4096)
-        nbytes = _ffi.size_out("drp_raster_workspace_size", B, max_view_tris, H, W, self.tile_log2, cap)
+        tl = self.tile_log2
+        shape = (B, max_view_tris, H, W, tl)
+        # fixed-depth bins (one setup pass) once this call shape has been seen
+        # with exact lists; validate mode always uses exact lists
+        depth = 0 if (first or self.validate) else self._depth.get(shape, 0)
+        if depth:
+            tiles = B * ((W + (1 << tl) - 1) >> tl) * ((H + (1 << tl) - 1) >> tl)
+            cap = max(cap, tiles * depth)
+        nbytes = _ffi.size_out("drp_raster_workspace_size", B, max_view_tris, H, W, tl, cap)
         ws = self._workspace(nbytes)
         args = (pos.data_ptr(), stride, pos.shape[-2], tri.data_ptr(), tri.shape[0], B, _ptr(ranges_dev),
-                max_view_tris, H, W, self.tile_log2, self.threads_per_tri, cap, _ptr(prev_key), rast.data_ptr(),
+                max_view_tris, H, W, tl, self.threads_per_tri, cap, depth, _ptr(prev_key), rast.data_ptr(),
                 _ptr(db), _ptr(out_key), _stream(self.device))
         _ffi.call("drp_rasterize_fwd", ws.data_ptr(), ws.numel(), *args)
         if first or self.validate:
@@ -184,19 +211,22 @@ class RasterizeCudaContext:
                 raise RuntimeError("rasterize: triangle vertex index out of range")
             if needed > cap:
                 self._capacity = int(needed * 1.25) + 1024
-                nbytes = _ffi.size_out("drp_raster_workspace_size", B, max_view_tris, H, W, self.tile_log2,
-                                       self._capacity)
+                nbytes = _ffi.size_out("drp_raster_workspace_size", B, max_view_tris, H, W, tl, self._capacity)
                 ws = self._workspace(nbytes)
-                _ffi.call("drp_rasterize_fwd", ws.data_ptr(), ws.numel(), *args[:12], self._capacity, *args[13:])
+                _ffi.call("drp_rasterize_fwd", ws.data_ptr(), ws.numel(), *args[:12], self._capacity,
+                          *args[13:])
             else:
                 self._capacity = max(self._capacity, cap)
+            if shape not in self._depth:
+                self._depth[shape] = self._choose_depth(shape, self.last_max_tile, needed)
             self._sized = True
         else:
-            # read the stats back on the first calls, then on every 8th (an
-            # overflowing call is still exact; only the growth waits)
+            # read the stats back on the first calls of a shape, then on
+            # every 8th call (an overflowing call is still exact; only the
+            # growth waits)
             self._calls += 1
-            if self._calls <= 8 or self._calls % 8 == 0:
-                self._queue_stats()
+            if shape not in self._depth or self._calls <= 8 or self._calls % 8 == 0:
+                self._queue_stats(shape, depth)
 
     def topology_workspace(self, F):
         nbytes = _ffi.size_out("drp_topology_workspace_size", F)

@@ -89,6 +89,12 @@ int drp_raster_workspace_size(int num_views, long long max_view_tris, int height
  *                    against each primitive (no atomics); 1, 2, 4, 8, 16 or
  *                    32: that many threads walk one primitive's bounding box
  *                    and resolve depth with shared-memory atomics.
+ *   bin_depth        0: exact tile lists (count, scan, fill passes);
+ *                    > 0: one setup pass appends into fixed-depth bins
+ *                    (list_capacity >= num_views * tiles * bin_depth); a
+ *                    tile with more entries stays exact (it scans the view's
+ *                    primitives), sets DRP_DEVERR_LIST_OVERFLOW and raises
+ *                    the largest-count field to its count.
  *   prev_key         previous layer's keys (depth peeling) or NULL.
  *   rast             out (B, H, W, 4); rast_db out (B, H, W, 4) or NULL;
  *   out_key          out (B, H, W) uint64 visibility keys or NULL.
@@ -96,8 +102,9 @@ int drp_raster_workspace_size(int num_views, long long max_view_tris, int height
 int drp_rasterize_fwd(void* workspace, size_t workspace_bytes, const float* pos, long long pos_view_stride,
                       long long num_vertices, const int* tri, long long num_triangles, int num_views,
                       const int* ranges, long long max_view_tris, int height, int width, int tile_log2,
-                      int threads_per_tri, unsigned long long list_capacity, const unsigned long long* prev_key,
-                      float* rast, float* rast_db, unsigned long long* out_key, void* stream);
+                      int threads_per_tri, unsigned long long list_capacity, unsigned bin_depth,
+                      const unsigned long long* prev_key, float* rast, float* rast_db, unsigned long long* out_key,
+                      void* stream);
 
 /*
  * Backward of rasterisation: grad_rast (B, H, W, 4) on (u, v, z/w, -) and

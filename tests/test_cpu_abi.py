@@ -61,10 +61,10 @@ def test_workspace_queries_and_validation(lib):
     assert b"tile_log2" in lib.drp_last_error()
     assert lib.drp_raster_workspace_size(1, 10, 0, 512, 4, 0, ctypes.byref(out)) == 1
     # invalid calls are rejected before any device work
-    st = lib.drp_rasterize_fwd(None, 0, None, 0, 0, None, 0, 0, None, 0, 16, 16, 4, 0, 0, None, None, None, None,
+    st = lib.drp_rasterize_fwd(None, 0, None, 0, 0, None, 0, 0, None, 0, 16, 16, 4, 0, 0, 0, None, None, None, None,
                                None)
     assert st == 1
-    st = lib.drp_rasterize_fwd(None, 0, None, 0, 0, None, 0, 1, None, 0, 16, 16, 4, 3, 0, None, None, None, None,
+    st = lib.drp_rasterize_fwd(None, 0, None, 0, 0, None, 0, 1, None, 0, 16, 16, 4, 3, 0, 0, None, None, None, None,
                                None)
     assert st == 1 and b"threads_per_tri" in lib.drp_last_error()
     with pytest.raises(RuntimeError, match="invalid argument"):

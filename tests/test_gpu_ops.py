@@ -132,6 +132,26 @@ def test_list_capacity_grows_across_mixed_calls(cuda_lib):
     np.testing.assert_array_equal(rast.cpu().numpy(), ref)
 
 
+@pytest.mark.parametrize("tile_log2,tpt", [(4, 0), (3, 1), (5, 4)])
+def test_fixed_depth_bins_exact(cuda_lib, tile_log2, tpt):
+    """After the first call of a shape (exact lists, synchronous sizing) the
+    context bins in one pass; repeated calls stay bit-exact, including a
+    forced too-shallow depth (overflowing tiles scan the view exactly)."""
+    pos, tri = scenes.multi_view(2, n_views=3, res=(72, 56))
+    ref, _, _ = O.rasterize(pos, tri, (72, 56), grad_db=False)
+    ctx = _ctx(tile_log2=tile_log2, threads_per_tri=tpt)
+    for _ in range(3):
+        rast, _ = _dr().rasterize(ctx, _t(pos), _t(tri), (72, 56), grad_db=False)
+        np.testing.assert_array_equal(rast.cpu().numpy(), ref)
+    assert any(d > 0 for d in ctx._depth.values())
+    for k in ctx._depth:
+        ctx._depth[k] = 1
+    rast, _ = _dr().rasterize(ctx, _t(pos), _t(tri), (72, 56), grad_db=False)
+    np.testing.assert_array_equal(rast.cpu().numpy(), ref)
+    _, err = ctx._read_stats_sync()
+    assert err & 2
+
+
 def test_depth_peeling(cuda_lib):
     pos, tri = scenes.random_soup(120, seed=2)
     dr = _dr()
