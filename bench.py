@@ -102,9 +102,9 @@ WORKLOAD_SINGLE = "icosphere5-displaced 20480 tris, 1024x1024, 8 ch, L1 loss, fw
 
 
 def clip_space(verts, mvp):
-    """Clip-space positions [v, 1] @ mvp^T of (V, 3) vertices: one addmm."""
-    import torch
-    return torch.addmm(mvp[:, 3], verts, mvp[:, :3].T)
+    """Clip-space positions [v, 1] @ mvp^T of (V, 3) vertices: one transform kernel."""
+    from diffrp_gb300.transform import clip_space as cs
+    return cs(verts, mvp)
 
 
 def packed_attr_offset(nv):
@@ -260,7 +260,6 @@ class MultiViewWorkload:
         self.topos = [nvdr.antialias_construct_topology_hash(t) for t in self.tris]
 
     def _clip(self, m, k):
-        torch = self.torch
         return clip_space(self.verts[m], self.mvps[k])
 
     def _zero(self):
@@ -268,16 +267,12 @@ class MultiViewWorkload:
             t.grad = None
 
     def _packed_clip(self):
-        torch = self.torch
+        from diffrp_gb300.transform import clip_space_packed
         if not self.grouped:
-            return torch.cat([self._clip(m, k) for k, (m, _) in enumerate(self.items)])
-        parts = []
-        for v, mv in zip(self.verts, self.mesh_mvps):
-            if mv is not None:
-                # (n, V, 4) = [v, 1] @ (n, 4, 4)^T: one batched GEMM per mesh (K = 4, aligned rows)
-                vh = torch.nn.functional.pad(v, (0, 1), value=1.0)
-                parts.append(torch.matmul(vh, mv.transpose(1, 2)).reshape(-1, 4))
-        return torch.cat(parts) if len(parts) > 1 else parts[0]
+            return clip_space_packed([(self.verts[m], self.mvps[k]) for k, (m, _) in enumerate(self.items)])
+        # one transform launch per mesh over its (n, 4, 4) view matrices,
+        # written straight into the packed position buffer
+        return clip_space_packed([(v, mv) for v, mv in zip(self.verts, self.mesh_mvps) if mv is not None])
 
     def batched_step(self):
         """The batching form with the L1 loss fused into its antialias pass."""

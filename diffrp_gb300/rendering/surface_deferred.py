@@ -16,11 +16,12 @@ from typing import Callable, List, Optional, Tuple, Union
 import torch
 
 from .. import nvdr as dr
+from ..transform import clip_space
 from ..materials.base_material import SurfaceInput, SurfaceOutputStandard, SurfaceUniform
 from ..utils.cache import cached
 from ..utils.composite import alpha_additive, alpha_blend
 from ..utils.shader_ops import (float3, float4, floatx, gpu_f32, length, normalized, ones_like_vec,
-                                transform_point, transform_point4x3, transform_vector3x3)
+                                transform_point4x3, transform_vector3x3)
 from .camera import Camera
 from .interpolator import FullScreenInterpolator, MaskedSparseInterpolator, float_to_triidx
 from .mixin import RenderSessionMixin
@@ -98,9 +99,10 @@ class SurfaceDeferredRenderSession(RenderSessionMixin):
     # -- geometry -----------------------------------------------------------
     @cached
     def clip_space(self):
-        """All vertices in GL clip space, (V, 4) contiguous."""
+        """All vertices in GL clip space, (V, 4) contiguous: [world_pos, 1] @ VP^T
+        in one transform kernel."""
         vao = self.vertex_array_object()
-        return transform_point(vao.world_pos, self.camera_VP()).contiguous()
+        return clip_space(vao.world_pos.contiguous(), self.camera_VP().contiguous())
 
     @cached
     def rasterize(self):

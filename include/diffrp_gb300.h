@@ -259,6 +259,27 @@ int drp_l1_loss_fwd(void* workspace, size_t workspace_bytes, const float* pred, 
                     float scale, float* loss, float* grad, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Clip-space transform                                                     */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * out[b * V + i] = M_b [v_i, 1] for V float32 xyz vertices and num_views
+ * (<= 65535) row-major 4x4 matrices; out is 16-byte aligned float4 rows.
+ * Replaces SurfaceDeferredRenderSession.clip_space
+ * (diffrp/rendering/surface_deferred.py:229-238) through transform_point
+ * (diffrp/utils/shader_ops.py:123-136), one small GEMM per view there.
+ */
+int drp_transform_points_fwd(const float* verts, long long num_vertices, const float* mats, int num_views,
+                             float* out, void* stream);
+
+/*
+ * grad_verts[i] = sum over b (in view order) of M_b[:, :3]^T grad_out[b * V + i]:
+ * writes (does not accumulate) V x 3 floats; grad_out as out above.
+ */
+int drp_transform_points_bwd(const float* grad_out, long long num_vertices, const float* mats, int num_views,
+                             float* grad_verts, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Batching form: many (mesh, view, resolution) items per launch             */
 /* ------------------------------------------------------------------------ */
 
