@@ -69,6 +69,7 @@ struct BatchArgs {
     uint32_t *tile_count, *tile_offset, *tile_cursor, *tile_list;
     unsigned long long* chunk_sums;  // tile-scan chunk sums
     float4* aa_rec;
+    const uint32_t* tile_order = nullptr;  // fine-raster work order (null: tile index order)
 };
 
 // MODE kSetupCount: triangle setup, antialias record, per-tile counts;
@@ -213,8 +214,9 @@ batch_fine_kernel(BatchArgs a) {
     __shared__ int job_item;
     for (;;) {
         if (threadIdx.x == 0) {
-            job = (long long)atomicAdd(a.queue, 1u);
-            job_item = job < a.total_tiles ? find_item_by_tile(a.items, a.num_items, job) : -1;
+            const long long j = (long long)atomicAdd(a.queue, 1u);
+            job = j < a.total_tiles && a.tile_order ? (long long)a.tile_order[j] : j;
+            job_item = j < a.total_tiles ? find_item_by_tile(a.items, a.num_items, job) : -1;
         }
         __syncthreads();
         const long long t = job;
@@ -600,6 +602,9 @@ static void carve(BatchArgs& a, void* ws, const BatchLayout& L) {
     a.aa_rec = reinterpret_cast<float4*>(w + L.aa);
 }
 
+// Up to this many tiles per resident fine CTA the work order is sorted.
+constexpr long long kOrderTilesPerCTA = 8;
+
 template <int TL, int TPT>
 static void launch_batch_fine(const BatchArgs& a, cudaStream_t s) {
     constexpr int NT = (1 << (2 * TL)) < 256 ? (1 << (2 * TL)) : 256;
@@ -615,10 +620,17 @@ static void launch_batch_fine(const BatchArgs& a, cudaStream_t s) {
     const int sms = drp_current_sm_count();
     const long long grid = (long long)(sms > 0 ? sms : 1) * per;
     const long long g = a.total_tiles < grid ? a.total_tiles : grid;
-    if (g > 0) {
-        batch_fine_kernel<TL, TPT><<<(unsigned)g, NT, 0, s>>>(a);
-        drp_note_launch();
+    if (g <= 0) return;
+    // With a few tiles per resident CTA, hand the longest tile lists out
+    // first (the order goes into the fill cursors, which are spent by now).
+    BatchArgs b = a;
+    b.tile_order = nullptr;
+    if (a.total_tiles > g && a.total_tiles <= kOrderTilesPerCTA * grid) {
+        launch_tile_order(a.tile_count, a.total_tiles, a.tile_cursor, s);
+        b.tile_order = a.tile_cursor;
     }
+    batch_fine_kernel<TL, TPT><<<(unsigned)g, NT, 0, s>>>(b);
+    drp_note_launch();
 }
 
 template <int TL>

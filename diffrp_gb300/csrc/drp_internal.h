@@ -42,6 +42,7 @@ struct RasterArgs {
     float* rast_db;
     unsigned long long* out_key;
     RasterWs ws;
+    const uint32_t* tile_order = nullptr;  // fine-raster block -> tile (null: identity)
 };
 
 struct RasterBwdArgs {

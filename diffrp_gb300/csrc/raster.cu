@@ -122,10 +122,12 @@ template <int TILE_LOG2, int TPT>
 __global__ void __launch_bounds__((1 << (2 * TILE_LOG2)) < 256 ? (1 << (2 * TILE_LOG2)) : 256,
                                   TILE_LOG2 == 3 ? 12 : 4)
 fine_raster_kernel(RasterArgs a) {
-    const int b = blockIdx.y;
-    const int tile = blockIdx.x;
+    const long long tiles = (long long)a.tiles_x * a.tiles_y;
+    long long tidx = (long long)blockIdx.y * tiles + blockIdx.x;  // blocks start in this order
+    if (a.tile_order) tidx = a.tile_order[tidx];
+    const int b = (int)(tidx / tiles);
+    const int tile = (int)(tidx - (long long)b * tiles);
     const long long npix = (long long)a.H * a.W;
-    const long long tidx = (long long)b * a.tiles_x * a.tiles_y + tile;
     FineTile ft;
     ft.recs = reinterpret_cast<const int4*>(a.ws.prims);
     ft.cnt = a.ws.tile_count[tidx];
@@ -214,10 +216,24 @@ __global__ void __launch_bounds__(256) raster_bwd_kernel(RasterBwdArgs a) {
 // ---------------------------------------------------------------------------
 // Host-side launchers.
 // ---------------------------------------------------------------------------
+// Up to this many tiles per resident fine CTA the blocks take the tiles in
+// order of decreasing list length (tile_order_kernel).
+constexpr long long kOrderTilesPerCTA = 8;
+
 template <int TL>
-static void launch_fine(const RasterArgs& a, int tpt, cudaStream_t s) {
+static void launch_fine(const RasterArgs& args, int tpt, cudaStream_t s) {
     constexpr int NT = (1 << (2 * TL)) < 256 ? (1 << (2 * TL)) : 256;
-    dim3 grid((unsigned)(a.tiles_x * a.tiles_y), (unsigned)a.B);
+    dim3 grid((unsigned)(args.tiles_x * args.tiles_y), (unsigned)args.B);
+    // resident CTAs per SM of the instantiations (launch bounds: 4 above
+    // 8-pixel tiles); the fill cursors are spent by now and hold the order
+    const long long slots = (long long)drp_current_sm_count() * (TL == 3 ? 12 : 4);
+    const long long ntiles = (long long)grid.x * grid.y;
+    RasterArgs a = args;
+    a.tile_order = nullptr;
+    if (a.max_view_tris > 0 && ntiles > slots && ntiles <= kOrderTilesPerCTA * slots) {
+        launch_tile_order(a.ws.tile_count, ntiles, a.ws.tile_cursor, s);
+        a.tile_order = a.ws.tile_cursor;
+    }
     switch (tpt) {
     case 0: fine_raster_kernel<TL, 0><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
     case 1: fine_raster_kernel<TL, 1><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;

@@ -720,4 +720,51 @@ static inline void launch_tile_scan(const uint32_t* counts, uint32_t* offsets, u
     drp_note_launch();
 }
 
+// Fine-raster work order: the n tiles by decreasing list length (counting
+// sort on min(count, 1023), ties in any order), so the longest tiles start
+// first and the short ones fill in behind them (longest-processing-time-first
+// list scheduling; with about one tile per resident CTA the tail otherwise
+// waits on whichever long tiles were handed out last).  Any permutation gives
+// the same raster: tiles are independent.  One CTA; meant for launches of a
+// few tiles per resident fine CTA.
+constexpr int kOrderThreads = 1024;
+static __global__ void __launch_bounds__(kOrderThreads) tile_order_kernel(const uint32_t* __restrict__ counts, long long n,
+                                                                          uint32_t* __restrict__ order) {
+    __shared__ uint32_t start[kOrderThreads];  // bucket k holds tiles of count 1023 - k (1023: or more)
+    __shared__ uint32_t warp_tot[kOrderThreads / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    start[tid] = 0;
+    __syncthreads();
+    for (long long t = tid; t < n; t += kOrderThreads) atomicAdd(&start[1023 - min(counts[t], 1023u)], 1u);
+    __syncthreads();
+    const uint32_t v = start[tid];
+    uint32_t x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_tot[lane];
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += y;
+        }
+        warp_tot[lane] = w;
+    }
+    __syncthreads();
+    start[tid] = x - v + (warp > 0 ? warp_tot[warp - 1] : 0u);
+    __syncthreads();
+    for (long long t = tid; t < n; t += kOrderThreads)
+        order[atomicAdd(&start[1023 - min(counts[t], 1023u)], 1u)] = (uint32_t)t;
+}
+
+static inline void launch_tile_order(const uint32_t* counts, long long n, uint32_t* order, cudaStream_t s) {
+    tile_order_kernel<<<1, kOrderThreads, 0, s>>>(counts, n, order);
+    drp_note_launch();
+}
+
 }  // namespace drp
