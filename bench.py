@@ -14,7 +14,9 @@ Lines printed (rank 0, one JSON line):
               L2 flushed (256 MiB write) between steps outside the events;
   e2e         the same step through the public API with the parameters copied
               from pinned host memory and loss + gradients copied back, inside
-              the timed region;
+              the timed region (copies and step captured as one CUDA graph; the
+              copies by kernels over the host link, copy_engine_value with
+              cudaMemcpyAsync transfers instead);
   roofline    dominant kernel (entry point) of the step: algorithmic bytes /
               CUDA-event time vs the measured HBM copy bandwidth;
   cpu_baseline  the CPU oracle (a restatement of the path, all host threads)
@@ -122,9 +124,13 @@ def pack_inputs(verts_np, attr_np):
 
 class GraphedStep:
     """The same step captured once as a CUDA graph (static parameter tensors,
-    gradients allocated in the graph's pool) and replayed."""
+    gradients allocated in the graph's pool) and replayed.  With io = (h_in,
+    h_out) pinned host buffers the graph also copies the parameters in from
+    h_in before the step and the loss and gradients out to h_out after it:
+    by kernels over the host link (zero_copy, diffrp_gb300.hostio) or by
+    copy-engine transfers."""
 
-    def __init__(self, step, verts_np, attr_np, dev):
+    def __init__(self, step, verts_np, attr_np, dev, io=None, zero_copy=True):
         import torch
         self.torch = torch
         # parameters as views of one packed buffer: one host->device copy per step
@@ -143,8 +149,24 @@ class GraphedStep:
         torch.cuda.synchronize(dev)
         self.graph = torch.cuda.CUDAGraph()
         n0 = kernel_launches()
+        if io is not None and zero_copy:
+            from diffrp_gb300 import hostio
+            io = (hostio.device_view(io[0], dev), hostio.device_view(io[1], dev))
         with torch.cuda.graph(self.graph):
+            if io is not None:
+                with torch.no_grad():
+                    if zero_copy:
+                        hostio.copy_(self.inbuf, io[0])
+                    else:
+                        self.inbuf.copy_(io[0], non_blocking=True)
             self.loss = step(self.verts, self.attr)
+            if io is not None:
+                with torch.no_grad():
+                    if zero_copy:  # packed straight into the host buffer
+                        torch.cat([self.loss.detach().view(1), self.verts.grad.view(-1),
+                                   self.attr.grad.view(-1)], out=io[1])
+                    else:
+                        io[1].copy_(self.pack_result(), non_blocking=True)
         # our kernels in one step, counted by the library as they are captured
         self.launches_per_step = kernel_launches() - n0
         torch.cuda.synchronize(dev)
@@ -768,20 +790,18 @@ def main():
     h_in = torch.from_numpy(pack_inputs(verts_np, attr_np)).pin_memory()
     h_out = torch.empty(1 + verts_np.size + attr_np.size, dtype=torch.float32).pin_memory()
 
-    def e2e_of(gs):
-        def e2e_step():
-            gs.load(h_in)
-            gs()
-            h_out.copy_(gs.pack_result(), non_blocking=True)
-        return e2e_step
+    def e2e_of(st, zero_copy=True):
+        # the host->device copy, the step and the device->host copy of its
+        # results captured together as one CUDA graph
+        return GraphedStep(st, verts_np, attr_np, dev, io=(h_in, h_out), zero_copy=zero_copy)
 
-    e2e_ms = timed(e2e_of(batched), args.steps)
-    e2e_plain_ms = timed(e2e_of(graphed), args.steps)
+    e2e_graphs = [e2e_of(bstep), e2e_of(bstep, zero_copy=False), e2e_of(step)]
+    e2e_ms, e2e_engine_ms, e2e_plain_ms = [timed(gs, args.steps) for gs in e2e_graphs]
     clocks = _clock_summary(clk, clk_path, dev.index if dev.index is not None else 0)
     if world > 1:
-        t = torch.tensor([total_ms, e2e_ms, eager_ms, plain_ms, e2e_plain_ms], device=dev)
+        t = torch.tensor([total_ms, e2e_ms, eager_ms, plain_ms, e2e_plain_ms, e2e_engine_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, e2e_ms, eager_ms, plain_ms, e2e_plain_ms = [float(x) for x in t]
+        total_ms, e2e_ms, eager_ms, plain_ms, e2e_plain_ms, e2e_engine_ms = [float(x) for x in t]
 
     pix = H * W * args.steps * world
     value = pix / (total_ms / 1e3) / 1e6
@@ -816,7 +836,11 @@ def main():
                                          "threads_per_tri": btuned["threads_per_tri"],
                                          "plain_path": {"tile": 1 << tuned["tile_log2"],
                                                         "threads_per_tri": tuned["threads_per_tri"]}}},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "path": "pinned host -> device copy, the step, device -> pinned host copy of loss and "
+                            "gradients, captured together as one CUDA graph; the copies are kernels loading / "
+                            "storing the mapped pinned buffers over the host link (diffrp_gb300.hostio)",
+                    "copy_engine_value": pix / (e2e_engine_ms / 1e3) / 1e6},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                          "algorithmic_bytes": algo[dom], "kernel_ms": times[dom]},
@@ -830,12 +854,13 @@ def main():
             "eager": {"value": pix / (eager_ms / 1e3) / 1e6, "unit": UNIT,
                       "note": "same step, drop-in nvdr ops, eager per-op launches (host-launch bound)"},
             "e2e_dropin": {"value": pix / (e2e_plain_ms / 1e3) / 1e6, "unit": UNIT,
-                           "note": "end to end through the drop-in nvdr ops (graph), host buffers"},
+                           "note": "end to end through the drop-in nvdr ops, host buffers (copies and step in one graph)"},
             "clocks": clocks,
-            # timed regions: batched graph and its e2e (2x), the unfused-loss batched graph, drop-in graph,
-            # its e2e and eager (3x)
-            "gpu_launches": (batched.launches_per_step * 2 + batched_unfused.launches_per_step +
-                             graphed.launches_per_step * 3) * args.steps,
+            # timed regions: batched graph, its two e2e graphs, the unfused-loss batched graph, drop-in
+            # graph, its e2e graph and the eager drop-in step
+            "gpu_launches": (batched.launches_per_step + batched_unfused.launches_per_step +
+                             graphed.launches_per_step * 2 + sum(gs.launches_per_step for gs in e2e_graphs)) *
+                            args.steps,
             "launches_per_step": {"batched": batched.launches_per_step,
                                   "batched_unfused_loss": batched_unfused.launches_per_step,
                                   "dropin": graphed.launches_per_step},

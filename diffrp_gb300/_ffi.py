@@ -33,6 +33,8 @@ _SIGNATURES = {
     "drp_l1_loss_fwd": [_P, ctypes.c_size_t, _P, _P, _LL, _F, _P, _P, _P],
     "drp_transform_points_fwd": [_P, _LL, _P, ctypes.c_int, _P, _P],
     "drp_transform_points_bwd": [_P, _LL, _P, ctypes.c_int, _P, _P],
+    "drp_host_device_pointer": [_P, _P],
+    "drp_copy_async": [_P, _P, ctypes.c_size_t, _P],
     "drp_antialias_fwd_noalloc": [_P, _I, _P, _P, _LL, _LL, _P, _LL, _P, _I, _I, _I, _P, _P],
     "drp_antialias_state_size": [_I, _I, _I, _SZ],
     "drp_antialias_fwd": [_P, ctypes.c_size_t, _P, _I, _P, _P, _LL, _LL, _P, _LL, _P, _I, _I, _I, _P, _P, _P],
