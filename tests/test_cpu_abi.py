@@ -83,3 +83,27 @@ def test_fast_path_matches_ctypes_on_validation(lib):
     assert table["drp_l1_loss_fwd"](*bad) == lib.drp_l1_loss_fwd(*bad) == 1
     with pytest.raises(TypeError):
         table["drp_l1_loss_fwd"](*bad[:-1])
+
+
+def test_transform_and_transport_validation(lib):
+    """The clip-space transform and the host-transport entry points reject
+    bad arguments on the host, launching nothing; the Python wrappers refuse
+    CPU / unpinned tensors before calling the library."""
+    import torch
+    from diffrp_gb300 import _ffi, hostio, transform
+    before = _ffi.kernel_launches()
+    assert lib.drp_transform_points_fwd(None, 5, None, 1, None, None) == 1      # null matrices
+    assert lib.drp_transform_points_fwd(None, 5, None, 0, None, None) == 1      # no views
+    assert lib.drp_transform_points_bwd(None, -1, None, 1, None, None) == 1     # negative count
+    assert lib.drp_transform_points_fwd(None, 0, None, 70000, None, None) == 1  # views above the grid limit
+    assert lib.drp_copy_async(None, None, ctypes.c_size_t(16), None) == 1
+    assert lib.drp_copy_async(None, None, ctypes.c_size_t(0), None) == 0        # nothing to copy
+    dev = ctypes.c_void_p(1)
+    assert lib.drp_host_device_pointer(None, ctypes.byref(dev)) == 1
+    assert _ffi.kernel_launches() == before
+    with pytest.raises(RuntimeError):
+        transform.clip_space(torch.zeros(4, 3), torch.eye(4))
+    with pytest.raises(RuntimeError):
+        transform.clip_space_packed([])
+    with pytest.raises(RuntimeError):
+        hostio.device_view(torch.zeros(4))
