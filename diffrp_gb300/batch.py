@@ -282,13 +282,11 @@ class BatchRenderer:
         ws = self._workspace(0)  # the backward reads no tile list
         stream = _ffi.stream_of(self.device)
         flags = REUSE_AA_RECORDS if gen is not None and gen == self._rec_gen and ws is self._rec_ws else 0
-        aa_grad = None if aa_flags is None else torch.empty(self.image_floats, dtype=torch.float32,
-                                                            device=self.device)
         _ffi.call("drp_batch_backward", ws.data_ptr(), ws.numel(), self._items_dev.data_ptr(), len(self.items),
                   self._pmap.data_ptr(), self.prim_blocks, self._xmap.data_ptr(), self.pixel_blocks,
                   self.total_prims, self.total_tiles, pos.data_ptr(), self.tri.data_ptr(), attr.data_ptr(),
                   self.nbr.data_ptr(), rast.data_ptr(), color.data_ptr(), None if aa_flags is None else aa_flags.data_ptr(),
-                  self.total_pixels, None if aa_grad is None else aa_grad.data_ptr(), grad_out.data_ptr(),
+                  self.total_pixels, None, grad_out.data_ptr(),
                   grad_pos.data_ptr(),
                   grad_attr.data_ptr(), None if grad_scale is None else grad_scale.data_ptr(), flags, stream)
 

@@ -49,7 +49,6 @@ struct BatchArgs {
     unsigned char* aa_flags;
     int* aa_list;
     unsigned* aa_count;
-    float* aa_grad;           // backward scratch: antialiased colour gradient of listed pixels
     bool emit_out;          // the fine raster also writes the colour into out
     bool aa_records;        // the setup pass writes the antialias triangle records
     // fused mean-absolute-error loss (null target: none)
@@ -348,13 +347,16 @@ __device__ __forceinline__ int find_item_by_pixel(const drp_batch_item* items, i
     return lo;
 }
 
-// Antialias backward of the listed pixels (those a blending pair touches,
-// about the silhouettes): edge-vertex gradients (scattered once per pair by
-// its first pixel) and the pixel's antialiased colour gradient into aa_grad.
-// The list is short and each pixel's chain of dependent loads is long, so a
-// quad of lanes takes one pixel: lane q evaluates pair slot q (and scatters
-// its edge gradient when it owns the pair), the quad exchanges the slot terms
-// by shuffles, and the lanes share the channels (c = q, q + 4, ...).
+// Whole backward of the listed pixels (those a blending pair touches, about
+// the silhouettes): edge-vertex gradients (scattered once per pair by its
+// first pixel), the pixel's antialiased colour gradient, and with it the
+// pixel's interpolation backward (attribute atomics) and rasterisation
+// backward (vertex atomics).  batch_bwd_kernel skips these pixels, so the two
+// kernels are independent and run side by side.  The list is short and each
+// pixel's chain of dependent loads is long, so a quad of lanes takes one
+// pixel: lane q evaluates pair slot q (and scatters its edge gradient when it
+// owns the pair), the quad exchanges the slot terms by shuffles, the lanes
+// share the channels (c = q, q + 4, ...) and sum d/du, d/dv by shuffles.
 // Grid-stride over the device-side count, so the launch needs no host sync.
 __global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
     const unsigned n = *a.aa_count;
@@ -406,10 +408,47 @@ __global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
             at.wt[k] = __shfl_sync(0xffffffffu, wt, qbase | k);
             at.any = at.any || at.role[k] != 0;
         }
+        int t = -1, i0 = 0, i1 = 0, i2 = 0;
+        float gu = 0.f, gv = 0.f;
         if (active) {
-            const float* Gd = a.grad_out + itp->image_offset;
-            float* g2 = a.aa_grad + itp->image_offset + (long long)pix * C;
-            for (int c = q; c < C; c += 4) g2[c] = aa_bwd_channel(at, Gd, C, pix, c, gsc);
+            const drp_batch_item& it = *itp;
+            const int* tri = a.tri + 3 * (long long)it.tri_first;
+            const float4 r = reinterpret_cast<const float4*>(a.rast)[it.pixel_offset + pix];
+            t = checked_tri(r.w, tri, it.tri_count, it.num_vertices, i0, i1, i2);
+            if (t >= 0) {
+                const float* Gd = a.grad_out + it.image_offset;
+                const float* A = a.attr + it.attr_offset;
+                float* GA = a.grad_attr + it.attr_offset;
+                const float u = r.x, v = r.y, w = 1.0f - u - v;
+                for (int c = q; c < C; c += 4) {
+                    const float g = aa_bwd_channel(at, Gd, C, pix, c, gsc);
+                    const float x0 = A[(long long)i0 * C + c], x1 = A[(long long)i1 * C + c],
+                                x2 = A[(long long)i2 * C + c];
+                    atomicAdd(GA + (long long)i0 * C + c, g * u);
+                    atomicAdd(GA + (long long)i1 * C + c, g * v);
+                    atomicAdd(GA + (long long)i2 * C + c, g * w);
+                    gu = fmaf(g, x0 - x2, gu);
+                    gv = fmaf(g, x1 - x2, gv);
+                }
+            }
+        }
+        gu += __shfl_xor_sync(0xffffffffu, gu, 1);
+        gv += __shfl_xor_sync(0xffffffffu, gv, 1);
+        gu += __shfl_xor_sync(0xffffffffu, gu, 2);
+        gv += __shfl_xor_sync(0xffffffffu, gv, 2);
+        if (active && t >= 0 && q == 0) {
+            const drp_batch_item& it = *itp;
+            const int W = it.width, H = it.height;
+            const int py = pix / W, px = pix - py * W;
+            const float X = fmaf((float)(2 * px + 1), __frcp_rn((float)W), -1.0f);
+            const float Y = fmaf((float)(2 * py + 1), __frcp_rn((float)H), -1.0f);
+            const float4* P = reinterpret_cast<const float4*>(a.pos) + it.pos_offset;
+            float4* GP = reinterpret_cast<float4*>(a.grad_pos) + it.pos_offset;
+            float4 g3[3];
+            uv_grad_fast(P[i0], P[i1], P[i2], X, Y, gu, gv, g3);
+            atomic_add4(GP + i0, make_float4(g3[0].x, g3[0].y, 0.f, g3[0].w));
+            atomic_add4(GP + i1, make_float4(g3[1].x, g3[1].y, 0.f, g3[1].w));
+            atomic_add4(GP + i2, make_float4(g3[2].x, g3[2].y, 0.f, g3[2].w));
         }
     }
 }
@@ -440,13 +479,14 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
     at.any = false;
     int t = -1, i0 = 0, i1 = 0, i2 = 0;
     float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-    // With the forward's antialias state, the pixels a blend touches were
-    // handled by batch_aa_bwd_kernel: their antialiased colour gradient is in
-    // aa_grad (already scaled).  Without it the terms are evaluated here.
+    // With the forward's antialias state, the pixels a blend touches belong
+    // to batch_aa_bwd_kernel (their whole backward) and are skipped here; the
+    // other pixels have no antialias terms.  Without it the terms are
+    // evaluated here for every pixel.
     const bool flagged = in && a.aa_flags && a.aa_flags[it.pixel_offset + pix];
-    const float* Gsrc = flagged ? a.aa_grad + it.image_offset : Gd;
-    const float gmul = flagged ? 1.0f : gsc;
-    if (in) {
+    const float* Gsrc = Gd;
+    const float gmul = gsc;
+    if (in && !flagged) {
         if (!a.aa_flags) aa_bwd_terms(R, Cc, Gd, rec, it.tri_count, W, H, C, P, tri, GP, 1.0f, pix, at, gsc);
         r = R[pix];
         t = checked_tri(r.w, tri, it.tri_count, it.num_vertices, i0, i1, i2);
@@ -686,22 +726,77 @@ int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream
     return 0;
 }
 
+// A side stream with its fork / join events, one per host thread and device,
+// created on first use outside stream capture (inside a capture, before the
+// first ordinary call, the caller's stream serves alone).  Captured forks
+// and joins become graph edges.
+struct SideStream {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+static bool side_stream(cudaStream_t s, SideStream& out) {
+    constexpr int kMaxDev = 64;
+    thread_local SideStream cache[kMaxDev];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) {
+        cudaGetLastError();
+        return false;
+    }
+    SideStream& c = cache[dev];
+    if (!c.stream) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+            cudaGetLastError();
+            return false;
+        }
+        SideStream n;
+        if (cudaStreamCreateWithFlags(&n.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&n.fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&n.join, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            if (n.stream) cudaStreamDestroy(n.stream);
+            if (n.fork) cudaEventDestroy(n.fork);
+            return false;
+        }
+        c = n;
+    }
+    out = c;
+    return true;
+}
+
 int launch_batch_backward(BatchArgs a, void* ws, const BatchLayout& L, bool reuse_records, cudaStream_t s) {
     carve(a, ws, L);
     if (a.n_prim_blocks > 0 && !reuse_records) {
         batch_aa_setup_kernel<<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
         drp_note_launch();
     }
-    if (a.aa_flags && a.n_pix_blocks > 0) {
-        const int sms = drp_current_sm_count();
-        const long long grid = (long long)(sms > 0 ? sms : 1) * 4;
-        const long long g = a.n_pix_blocks < grid ? a.n_pix_blocks : grid;
-        batch_aa_bwd_kernel<<<(unsigned)g, 256, 0, s>>>(a);
-        drp_note_launch();
-    }
-    if (a.n_pix_blocks > 0) {
+    if (a.n_pix_blocks <= 0) return 0;
+    if (!a.aa_flags) {
         batch_bwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
         drp_note_launch();
+        return 0;
+    }
+    // The listed pixels' kernel (latency-bound, a few percent of the pixels)
+    // and the fused backward of all other pixels are independent: fork the
+    // list kernel onto a side stream so it fills the SMs beside the main
+    // kernel and its tail, then join.  Both only add into the gradients.
+    const int sms = drp_current_sm_count();
+    const long long grid = (long long)(sms > 0 ? sms : 1) * 4;
+    const long long g = a.n_pix_blocks < grid ? a.n_pix_blocks : grid;
+    SideStream side;
+    const bool fork = side_stream(s, side);
+    if (fork) {
+        cudaEventRecord(side.fork, s);
+        cudaStreamWaitEvent(side.stream, side.fork, 0);
+    }
+    batch_bwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+    drp_note_launch();
+    batch_aa_bwd_kernel<<<(unsigned)g, 256, 0, fork ? side.stream : s>>>(a);
+    drp_note_launch();
+    if (fork) {
+        cudaEventRecord(side.join, side.stream);
+        cudaStreamWaitEvent(s, side.join, 0);
     }
     return 0;
 }
@@ -911,10 +1006,10 @@ DRP_API int drp_batch_backward(void* workspace, size_t workspace_bytes, const dr
     a.nbr = nbr;
     a.rast = const_cast<float*>(rast);
     a.color = const_cast<float*>(color);
-    if (aa_state && ((reinterpret_cast<uintptr_t>(aa_state) & 255) || total_pixels <= 0 || !aa_grad))
-        return bfail("batch: aa_state needs 256-byte alignment, total_pixels > 0 and an aa_grad buffer");
+    (void)aa_grad;  // no longer used: the listed pixels' backward is fused into their kernel
+    if (aa_state && ((reinterpret_cast<uintptr_t>(aa_state) & 255) || total_pixels <= 0))
+        return bfail("batch: aa_state needs 256-byte alignment and total_pixels > 0");
     carve_aa_state(a, const_cast<void*>(aa_state), total_pixels);
-    a.aa_grad = aa_grad;
     a.grad_out = grad_out;
     a.grad_pos = grad_pos;
     a.grad_attr = grad_attr;

@@ -389,12 +389,15 @@ int drp_batch_forward_l1(void* workspace, size_t workspace_bytes, const drp_batc
 
 /* Fused backward: grad_out (image floats) -> grad_pos (accumulated, pos
  * layout) and grad_attr (accumulated, attr layout).  aa_state: NULL, or the
- * block the forward filled for this rast; then aa_grad (image floats of
- * scratch) receives the antialiased colour gradient of the listed pixels and
- * the other pixels skip the antialias terms.  grad_scale: NULL, or a device
- * float every grad_out value is multiplied by as it is read (the upstream
- * gradient of drp_batch_forward_l1's loss).  flags: 0 or
- * DRP_BATCH_REUSE_AA_RECORDS. */
+ * block the forward filled for this rast; then the listed pixels get their
+ * whole backward (antialias terms, interpolation, rasterisation) in one
+ * kernel, forked onto a library-owned side stream (one per host thread and
+ * device, joined back before the call's work ends on `stream`; inside a
+ * stream capture the fork and join are graph edges), while the other pixels,
+ * which have no antialias terms, run the fused backward on `stream`.  aa_grad
+ * is ignored (may be NULL).  grad_scale: NULL, or a device float every
+ * grad_out value is multiplied by as it is read (the upstream gradient of
+ * drp_batch_forward_l1's loss).  flags: 0 or DRP_BATCH_REUSE_AA_RECORDS. */
 int drp_batch_backward(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
                        const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
                        long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
