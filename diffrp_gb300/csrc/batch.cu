@@ -729,7 +729,9 @@ int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream
 // A side stream with its fork / join events, one per host thread and device,
 // created on first use outside stream capture (inside a capture, before the
 // first ordinary call, the caller's stream serves alone).  Captured forks
-// and joins become graph edges.
+// and joins become graph edges.  The caller's stream belongs to the current
+// device, as for every launch of this library (a stream query here would
+// invalidate a capture in progress).
 struct SideStream {
     cudaStream_t stream = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
