@@ -2,7 +2,7 @@
 // prediction and target, writes the per-element gradient sign(p - t) * scale
 // and per-block partial sums (compensated float sums over a grid of a few
 // blocks per SM); a second single-block pass adds the partials in a fixed
-// order (reproducible loss).
+// order with compensated float-pair sums (reproducible loss).
 #include "drp_common.cuh"
 #include "drp_internal.h"
 
@@ -63,28 +63,55 @@ __global__ void __launch_bounds__(kLossThreads) l1_partial_kernel(const float* p
     }
 }
 
+// s + x exactly as a float pair: s' = fl(s + x), err = (s + x) - s' (Knuth's
+// TwoSum, no branch).  Sums of pairs carry their rounding errors in c.
+__device__ inline void two_sum(float& s, float& c, float x) {
+    const float t = s + x;
+    const float bp = t - s;
+    const float err = (s - (t - bp)) + (x - bp);
+    s = t;
+    c += err;
+}
+
+// Fixed-order compensated sum of the partials: every thread adds its strided
+// elements (eight loads in flight) in index order, then the (sum, error)
+// pairs are combined by a fixed shuffle tree within warps and across them.
+// Float pairs instead of doubles: FP64 issues at a small fraction of the
+// FP32 rate on this part, and this single block sits on the step's critical
+// path.
 __global__ void __launch_bounds__(1024) l1_final_kernel(const float* partial, long long nblocks, float scale,
                                                         float* loss) {
-    __shared__ double warp_sum[32];
-    double s = 0.0;
-    // eight independent loads in flight per thread, added in index order
+    __shared__ float warp_s[32], warp_c[32];
+    float s = 0.0f, c = 0.0f;
     const long long step = (long long)blockDim.x;
     for (long long i = threadIdx.x; i < nblocks; i += 8 * step) {
         float v[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) v[k] = i + k * step < nblocks ? partial[i + k * step] : 0.0f;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) s += (double)v[k];
+        for (int k = 0; k < 8; ++k) two_sum(s, c, v[k]);
     }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-    if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = s;
+    for (int off = 16; off > 0; off >>= 1) {
+        const float os = __shfl_xor_sync(0xffffffffu, s, off), oc = __shfl_xor_sync(0xffffffffu, c, off);
+        c += oc;
+        two_sum(s, c, os);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        warp_s[threadIdx.x >> 5] = s;
+        warp_c[threadIdx.x >> 5] = c;
+    }
     __syncthreads();
     if (threadIdx.x < 32) {
-        double v = threadIdx.x < (int)(blockDim.x >> 5) ? warp_sum[threadIdx.x] : 0.0;
+        const bool have = threadIdx.x < (int)(blockDim.x >> 5);
+        float v = have ? warp_s[threadIdx.x] : 0.0f, w = have ? warp_c[threadIdx.x] : 0.0f;
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        if (threadIdx.x == 0) *loss = (float)(v * (double)scale);
+        for (int off = 16; off > 0; off >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, v, off), ow = __shfl_xor_sync(0xffffffffu, w, off);
+            w += ow;
+            two_sum(v, w, ov);
+        }
+        if (threadIdx.x == 0) *loss = (v + w) * scale;
     }
 }
 
