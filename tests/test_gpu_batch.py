@@ -208,3 +208,42 @@ def test_batch_cuda_graph_replay(cuda_lib):
     assert torch.allclose(loss, ref_loss)
     scale = ref_gp.abs().max()
     assert float((pos_b.grad - ref_gp).abs().max() / scale) <= 1e-5
+
+
+def test_backward_on_a_side_stream_matches_default_stream(cuda_lib):
+    """The batching form's backward forks its listed-pixel kernel onto a
+    library stream and joins it back into the caller's stream: run on a
+    non-default torch stream (and from a second host thread), the gradients
+    equal the default-stream ones up to atomic summation order."""
+    import threading
+    from diffrp_gb300.batch import BatchRenderer
+    H = W = 256
+    v, f = S.displaced_icosphere(3, 0.8, 0.02, 5)
+    mvp = S.perspective(30.0, H, W, 0.1, 100.0).astype(np.float64) @ \
+        S.view_matrix(S.lookat_pose((0.0, 0.0, 3.2))).astype(np.float64)
+    pos = torch.from_numpy(S.clip_positions(v, mvp)).cuda()
+    attr = torch.from_numpy(np.random.default_rng(5).uniform(0, 1, (len(v), 4)).astype(np.float32)).cuda()
+    tri = torch.from_numpy(f).cuda()
+    target = torch.rand(H * W * 4, device="cuda", generator=torch.Generator(device="cuda").manual_seed(5))
+
+    def run(stream):
+        r = BatchRenderer([(tri, len(v), 4)], [(0, (H, W))], tile_log2=4)
+        p = pos.clone().requires_grad_(True)
+        a = attr.reshape(-1).clone().requires_grad_(True)
+        with torch.cuda.stream(stream):
+            for _ in range(2):  # the second call forks (side stream created by the first)
+                p.grad = a.grad = None
+                loss, _ = r.render_l1(p, a, target)
+                loss.backward()
+        stream.synchronize()
+        return p.grad.clone(), a.grad.clone()
+
+    ref = run(torch.cuda.current_stream())
+    side = run(torch.cuda.Stream())
+    out = {}
+    th = threading.Thread(target=lambda: out.setdefault("g", run(torch.cuda.Stream())))
+    th.start()
+    th.join()
+    for got in (side, out["g"]):
+        for x, y in zip(got, ref):
+            assert torch.allclose(x, y, rtol=1e-5, atol=1e-7)
