@@ -484,8 +484,6 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
     // other pixels have no antialias terms.  Without it the terms are
     // evaluated here for every pixel.
     const bool flagged = in && a.aa_flags && a.aa_flags[it.pixel_offset + pix];
-    const float* Gsrc = Gd;
-    const float gmul = gsc;
     if (in && !flagged) {
         if (!a.aa_flags) aa_bwd_terms(R, Cc, Gd, rec, it.tri_count, W, H, C, P, tri, GP, 1.0f, pix, at, gsc);
         r = R[pix];
@@ -495,17 +493,17 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
     const float u = r.x, v = r.y, w = 1.0f - u - v;
     float gu = 0.f, gv = 0.f;
     const bool vec = (C & 3) == 0 && ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(GA) |
-                                       reinterpret_cast<uintptr_t>(Gsrc)) & 15) == 0;
+                                       reinterpret_cast<uintptr_t>(Gd)) & 15) == 0;
     // Channel groups of 4: the next group's loads are issued before this
     // group's reduction and atomics, which would otherwise hold them back.
     float g[4], x0[4], x1[4], x2[4];
     auto load_group = [&](int c0) {
         if (vec) {
-            const float4 gq = __ldg(reinterpret_cast<const float4*>(Gsrc + (long long)pix * C + c0));
+            const float4 gq = __ldg(reinterpret_cast<const float4*>(Gd + (long long)pix * C + c0));
             const float4 q0 = __ldg(reinterpret_cast<const float4*>(A + (long long)i0 * C + c0));
             const float4 q1 = __ldg(reinterpret_cast<const float4*>(A + (long long)i1 * C + c0));
             const float4 q2 = __ldg(reinterpret_cast<const float4*>(A + (long long)i2 * C + c0));
-            g[0] = gq.x * gmul; g[1] = gq.y * gmul; g[2] = gq.z * gmul; g[3] = gq.w * gmul;
+            g[0] = gq.x * gsc; g[1] = gq.y * gsc; g[2] = gq.z * gsc; g[3] = gq.w * gsc;
             x0[0] = q0.x; x0[1] = q0.y; x0[2] = q0.z; x0[3] = q0.w;
             x1[0] = q1.x; x1[1] = q1.y; x1[2] = q1.z; x1[3] = q1.w;
             x2[0] = q2.x; x2[1] = q2.y; x2[2] = q2.z; x2[3] = q2.w;
@@ -513,7 +511,7 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int c = c0 + k < C ? c0 + k : C - 1;
-                g[k] = c0 + k < C ? Gsrc[(long long)pix * C + c] * gmul : 0.f;
+                g[k] = c0 + k < C ? Gd[(long long)pix * C + c] * gsc : 0.f;
                 x0[k] = A[(long long)i0 * C + c];
                 x1[k] = A[(long long)i1 * C + c];
                 x2[k] = A[(long long)i2 * C + c];
