@@ -121,3 +121,30 @@ def test_camera_conventions():
     pose = S.lookat_pose((0.0, 0.0, 3.2))
     np.testing.assert_allclose(pose, np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 3.2], [0, 0, 0, 1.0]]),
                                atol=1e-12)
+
+
+def test_drop_in_bin_depth_sizing_host_logic():
+    """The drop-in context's choice of fixed-depth bins per call shape and
+    their growth after an overflow (host logic, no device)."""
+    from diffrp_gb300.nvdr import RasterizeCudaContext
+    ctx = RasterizeCudaContext.__new__(RasterizeCudaContext)
+    ctx._depth, ctx._capacity, ctx.last_list_entries = {}, 0, 0
+    shape = (1, 20480, 1024, 1024, 5)  # 1024 tiles of 32 x 32
+    assert ctx._choose_depth(shape, 100, 60000) == 133  # 1.25 x largest + 8
+    assert ctx._choose_depth(shape, 10 ** 6, 60000) == 0  # bins far beyond the exact lists: keep exact
+    ctx._note_stats(shape, 0, 60000, 0, 100)  # an exact-list call: capacity and the shape's depth
+    assert ctx._capacity == int(60000 * 1.25) + 1024 and ctx._depth[shape] == 133
+    ctx._note_stats(shape, 133, 0, 2, 400)  # a bin overflowed: deeper bins for the next call
+    assert ctx._depth[shape] == max(int(133 * 1.5), int(400 * 1.25) + 8)
+    ctx._note_stats(shape, 508, 0, 0, 10)  # no overflow: unchanged
+    assert ctx._depth[shape] == 508
+
+
+def test_batch_bin_depth_choice_host_logic():
+    from diffrp_gb300.batch import BatchRenderer
+    r = BatchRenderer.__new__(BatchRenderer)
+    r.bin_depth_mode, r.total_tiles = None, 4096
+    assert r._choose_depth(50, 100000) == int(50 * 1.25) + 8
+    assert r._choose_depth(5000, 1000) == 0
+    r.bin_depth_mode = 7  # a caller-fixed depth wins
+    assert r._choose_depth(5000, 1000) == 7
