@@ -41,7 +41,8 @@ def device_view(t, device=None):
 
 def copy_(dst, src):
     """dst <- src bytewise with a kernel on the current stream; both CUDA
-    tensors (device memory or device views), contiguous, of equal byte size."""
+    tensors (device memory or device views), contiguous, of equal byte size,
+    not overlapping."""
     if not (dst.is_cuda and src.is_cuda and dst.is_contiguous() and src.is_contiguous()):
         raise RuntimeError("copy_ expects contiguous CUDA tensors")
     n = dst.numel() * dst.element_size()

@@ -290,8 +290,8 @@ int drp_transform_points_bwd(const float* grad_out, long long num_vertices, cons
  * that is not. */
 int drp_host_device_pointer(const void* host, void** device);
 
-/* Copy `bytes` bytes with a kernel (16-byte vectors when both ends are
- * 16-byte aligned), stream-ordered.  Either end may be device memory or the
+/* Copy `bytes` bytes between non-overlapping buffers with a kernel (16-byte
+ * vectors when both ends are 16-byte aligned), stream-ordered.  Either end may be device memory or the
  * device address of mapped pinned host memory: on a coherent host link the
  * SMs move a few hundred kilobytes faster than a copy engine transfer. */
 int drp_copy_async(void* dst, const void* src, size_t bytes, void* stream);
