@@ -315,10 +315,44 @@ static __device__ __align__(256) float4 g_aa_noalloc_scratch[2 * DRP_NOALLOC_AA_
 namespace {
 std::mutex g_noalloc_mutex;
 constexpr int kMaxDevices = 64;
-void* g_noalloc_scratch_addr[kMaxDevices] = {};
+struct NoallocAddr {
+    unsigned long long ctx_id;  // the CUDA context the address belongs to (0: none cached)
+    void* addr;
+};
+NoallocAddr g_noalloc_scratch_addr[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device, looked up once
-// per device (host code may not use the array's name as a device address).
+// Unique id of the calling thread's current CUDA context, through the driver
+// entry points the runtime hands out (no link-time dependency on libcuda).
+// False when there is no current context or the entry points are missing.
+bool current_context_id(unsigned long long* id) {
+    typedef int (*GetCurrentFn)(void**);
+    typedef int (*GetIdFn)(void*, unsigned long long*);
+    static GetCurrentFn get_current = nullptr;
+    static GetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetIdFn>(f);
+    });
+    if (!get_current || !get_id) return false;
+    void* ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx) return false;
+    return get_id(ctx, id) == 0 && *id != 0;
+}
+
+// Device address of the scratch array in the current device's context (host
+// code may not use the array's name as a device address).  Looked up on the
+// first call in each context and cached with that context's id: after a
+// cudaDeviceReset the runtime makes a new primary context, the module is
+// loaded again, and the address is looked up again.  Without context ids
+// (driver entry points unavailable) it is looked up on every call.
 int noalloc_scratch(void** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
@@ -331,16 +365,23 @@ int noalloc_scratch(void** out) {
         return DRP_STATUS_INVALID_ARGUMENT;
     }
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_scratch_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_aa_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            drp_set_last_error("drp_antialias_fwd_noalloc: cudaGetSymbolAddress of the scratch array failed");
-            return DRP_STATUS_CUDA_ERROR;
-        }
-        g_noalloc_scratch_addr[dev] = p;
+    unsigned long long id = 0;
+    const bool have_id = current_context_id(&id);
+    if (have_id && g_noalloc_scratch_addr[dev].ctx_id == id && g_noalloc_scratch_addr[dev].addr) {
+        *out = g_noalloc_scratch_addr[dev].addr;
+        return DRP_STATUS_OK;
     }
-    *out = g_noalloc_scratch_addr[dev];
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_aa_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        drp_set_last_error("drp_antialias_fwd_noalloc: cudaGetSymbolAddress of the scratch array failed");
+        return DRP_STATUS_CUDA_ERROR;
+    }
+    // the lookup made the primary context current if it was not yet
+    unsigned long long id_after = 0;
+    if (current_context_id(&id_after)) g_noalloc_scratch_addr[dev] = NoallocAddr{id_after, p};
+    else g_noalloc_scratch_addr[dev] = NoallocAddr{0, nullptr};
+    *out = p;
     return DRP_STATUS_OK;
 }
 }  // namespace
@@ -355,6 +396,14 @@ extern "C" __attribute__((visibility("default"))) int drp_antialias_fwd_noalloc(
     }
     if (channels <= 0 || num_triangles < 0 || num_vertices < 0 || pos_view_stride < 0 || (pos_view_stride % 4)) {
         drp_set_last_error("drp_antialias_fwd_noalloc: bad channels, sizes or stride");
+        return DRP_STATUS_INVALID_ARGUMENT;
+    }
+    if (num_views > 65535) {
+        drp_set_last_error("drp_antialias_fwd_noalloc: num_views above 65535");
+        return DRP_STATUS_INVALID_ARGUMENT;
+    }
+    if ((long long)num_views * height * width > 0x7fffffffll) {
+        drp_set_last_error("drp_antialias_fwd_noalloc: num_views * height * width above 2^31 - 1");
         return DRP_STATUS_INVALID_ARGUMENT;
     }
     if ((long long)num_views * num_triangles > DRP_NOALLOC_AA_MAX_TRIANGLE_VIEWS) {

@@ -216,7 +216,8 @@ DRP_API int drp_rasterize_bwd(const float* pos, long long pos_view_stride, long 
 static int interp_common(const float* attr, long long attr_view_stride, int channels, const float* rast,
                          const float* rast_db, const int* tri, int num_views, int height, int width,
                          const int* diff_idx, int num_diff) {
-    if (num_views <= 0 || !res_ok(height, width)) return fail(DRP_STATUS_INVALID_ARGUMENT, "bad views / resolution");
+    if (num_views <= 0 || num_views > 65535 || !res_ok(height, width))
+        return fail(DRP_STATUS_INVALID_ARGUMENT, "bad views / resolution");
     if (channels <= 0) return fail(DRP_STATUS_INVALID_ARGUMENT, "channels must be positive");
     if (!attr || !rast || !tri) return fail(DRP_STATUS_INVALID_ARGUMENT, "null pointer");
     if (attr_view_stride < 0) return fail(DRP_STATUS_INVALID_ARGUMENT, "negative stride");
@@ -364,7 +365,8 @@ DRP_API int drp_antialias_topology(void* workspace, size_t workspace_bytes, cons
 
 static int aa_common(const float* color, int channels, const float* rast, const float* pos, long long stride,
                      const int* tri, int num_views, int height, int width) {
-    if (num_views <= 0 || !res_ok(height, width)) return fail(DRP_STATUS_INVALID_ARGUMENT, "bad views / resolution");
+    if (num_views <= 0 || num_views > 65535 || !res_ok(height, width))
+        return fail(DRP_STATUS_INVALID_ARGUMENT, "bad views / resolution");
     if (channels <= 0) return fail(DRP_STATUS_INVALID_ARGUMENT, "channels must be positive");
     if (!color || !rast || !pos || !tri) return fail(DRP_STATUS_INVALID_ARGUMENT, "null pointer");
     if (!aligned(rast, 16) || !aligned(pos, 16) || stride < 0 || (stride % 4) != 0)

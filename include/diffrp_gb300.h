@@ -205,9 +205,13 @@ int drp_antialias_fwd(void* workspace, size_t workspace_bytes, const float* colo
  * library (8 MiB per GPU, held until the process exits), so the call rejects
  * num_views * num_triangles above DRP_NOALLOC_AA_MAX_TRIANGLE_VIEWS with
  * DRP_STATUS_INVALID_ARGUMENT.  Same arguments and output as
- * drp_antialias_fwd.  The first call on each device looks up the array's
- * device address (cudaGetSymbolAddress) -- make that first call before any
- * stream capture.  All calls share the one array: calls whose GPU work
+ * drp_antialias_fwd, except that num_views above 65535 and num_views *
+ * height * width above 2^31 - 1 are rejected the same way.  The first call
+ * on each device looks up the array's device address (cudaGetSymbolAddress)
+ * -- make that first call before any stream capture.  The address is kept
+ * with the id of the CUDA context it was found in; a call in a new context
+ * (after cudaDeviceReset, say) looks it up again, so make the first call
+ * after a reset before any capture too.  All calls share the one array: calls whose GPU work
  * overlaps (different streams, or threads without ordering) race on it.
  * No counterpart in the reference: dr.antialias always allocates its own
  * buffers.

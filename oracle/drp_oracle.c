@@ -888,3 +888,145 @@ ORC_EXPORT int orc_aa_bwd(const real* color, int C, const real* rast, const real
     free(acc);
     return ORC_OK;
 }
+
+/* ---------------------------------------------------------------------- */
+/* Finite-difference support: the L1 loss with visibility held fixed.      */
+/* ---------------------------------------------------------------------- */
+/*
+ * The gradients diffrp gets from dr.antialias (diffrp/rendering/
+ * surface_deferred.py:775) and from the interpolation autograd
+ * (diffrp/rendering/interpolator.py:32-48) are those of the image with every
+ * discrete decision of the forward held: each pixel's triangle, and for each
+ * antialias pair the front triangle, the crossing edge, which pixel is
+ * blended and whether its crossing parameter was clamped.  Central
+ * differences of the loss evaluated that way check the analytic backward
+ * (rasterisation, interpolation, antialias silhouette term) without the
+ * discontinuities of coverage changes.
+ *
+ * orc_aa_plan lists the decisions of one view's antialias forward, evaluated
+ * in this build's precision (use the float build: its decisions are those of
+ * the CUDA forward, bit for bit).  One entry per valid pair, 8 int32 each:
+ *   target pixel, source pixel, front pixel, other pixel, front triangle,
+ *   crossing edge k, branch (+1: w = t - 1/2, -1: w = 1/2 - t, 0: t clamped,
+ *   w = 1/2 fixed), orientation sign of the front triangle (+1 / -1).
+ * Returns the number of entries; writes at most cap of them.
+ */
+ORC_EXPORT long orc_aa_plan(const real* rast, const real* pos, long V, const int32_t* tri, long F,
+                            const int32_t* nbr, int H, int W, int32_t* plan, long cap) {
+    (void)V; (void)F;
+    long n = 0;
+    long npix = (long)H * W;
+    for (long pix = 0; pix < npix; ++pix) {
+        int px = (int)(pix % W), py = (int)(pix / W);
+        long pairs[2][2];
+        int np = 0;
+        if (px < W - 1) { pairs[np][0] = pix; pairs[np][1] = pix + 1; ++np; }
+        if (py < H - 1) { pairs[np][0] = pix; pairs[np][1] = pix + W; ++np; }
+        for (int q = 0; q < np; ++q) {
+            aa_pair_t pr;
+            aa_pair(rast, pos, tri, nbr, W, H, pairs[q][0], pairs[q][1], &pr);
+            if (!pr.valid) continue;
+            if (n < cap) {
+                int32_t* e = plan + n * 8;
+                e[0] = (int32_t)pr.target;
+                e[1] = (int32_t)pr.src;
+                /* front pixel: the pixel holding T */
+                e[2] = rast_tri(rast + pairs[q][0] * 4) == pr.T ? (int32_t)pairs[q][0] : (int32_t)pairs[q][1];
+                e[3] = e[2] == (int32_t)pairs[q][0] ? (int32_t)pairs[q][1] : (int32_t)pairs[q][0];
+                e[4] = pr.T;
+                e[5] = pr.k;
+                e[6] = pr.clamped ? 0 : (int32_t)pr.sign;
+                e[7] = pr.sgn > 0 ? 1 : -1;
+            }
+            ++n;
+        }
+    }
+    return n;
+}
+
+static inline void pixel_color(const real* pos, const int32_t* tri, const real* attr, int C, int t, long pix, int H,
+                               int W, real* col) {
+    const int32_t* ti = tri + (size_t)t * 3;
+    shade_t S;
+    shade_eval(pos + (size_t)ti[0] * 4, pos + (size_t)ti[1] * 4, pos + (size_t)ti[2] * 4, (int)(pix % W),
+               (int)(pix / W), W, H, &S);
+    const real* a0 = attr + (size_t)ti[0] * C;
+    const real* a1 = attr + (size_t)ti[1] * C;
+    const real* a2 = attr + (size_t)ti[2] * C;
+    for (int c = 0; c < C; ++c) col[c] = r_fma(a0[c] - a2[c], S.u, r_fma(a1[c] - a2[c], S.v, a2[c]));
+}
+
+/*
+ * sum over pixels and channels of sign * out, with out the antialiased
+ * interpolation of attr under the fixed decisions: ids (per pixel triangle
+ * or -1) and the plan of orc_aa_plan.  sign is the per (pixel, channel) sign
+ * of (out - target) at the point the gradient is taken (the L1 loss
+ * linearised at its kinks the way its gradient is).  With tri_flag (one
+ * byte per triangle) only the terms that involve a flagged triangle are
+ * summed: the pixels of flagged triangles, and the pairs whose front
+ * triangle or either pixel's triangle is flagged.  Every other term does
+ * not depend on the vertices of the flagged triangles, so differences of
+ * two evaluations equal those of the full sum.  Single view.
+ */
+ORC_EXPORT int orc_l1_fixed_visibility(const real* pos, const int32_t* tri, const real* attr, int C, int H, int W,
+                                       const int32_t* ids, const int8_t* sign, const int32_t* plan, long n_plan,
+                                       const uint8_t* tri_flag, double* result, int nthreads) {
+    if (C > ORC_MAX_AA_CHANNELS) return 2;
+    long npix = (long)H * W;
+    /* per-thread partial sums over static chunks, added in thread order: the
+       same inputs give the same bits (differences of two evaluations that
+       change no term are exactly zero) */
+    int nt = max_threads(nthreads);
+    double* part = (double*)calloc((size_t)nt, sizeof(double));
+    if (!part) return 1;
+#pragma omp parallel num_threads(nt)
+    {
+        real col[ORC_MAX_AA_CHANNELS], cs[ORC_MAX_AA_CHANNELS];
+        double total = 0.0;
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+#pragma omp for schedule(static)
+        for (long pix = 0; pix < npix; ++pix) {
+            int t = ids[pix];
+            if (t < 0 || (tri_flag && !tri_flag[t])) continue;
+            pixel_color(pos, tri, attr, C, t, pix, H, W, col);
+            for (int c = 0; c < C; ++c) total += (double)sign[pix * C + c] * (double)col[c];
+        }
+#pragma omp for schedule(static)
+        for (long e = 0; e < n_plan; ++e) {
+            const int32_t* p = plan + e * 8;
+            long tgt = p[0], src = p[1], Fp = p[2], Op = p[3];
+            int T = p[4], k = p[5], branch = p[6];
+            real sgn = (real)p[7];
+            int tt = ids[tgt], ts = ids[src];
+            if (tri_flag && !tri_flag[T] && !(tt >= 0 && tri_flag[tt]) && !(ts >= 0 && tri_flag[ts])) continue;
+            real w = (real)0.5;
+            if (branch != 0) {
+                const int32_t* ti = tri + (size_t)T * 3;
+                real s[3][2];
+                int ok = 1;
+                for (int i = 0; i < 3; ++i) ok &= project_vertex(pos + (size_t)ti[i] * 4, W, H, s[i]);
+                if (!ok) continue;
+                real cF[2] = {(real)(Fp % W) + (real)0.5, (real)(Fp / W) + (real)0.5};
+                real cO[2] = {(real)(Op % W) + (real)0.5, (real)(Op / W) + (real)0.5};
+                const real* a = s[(k + 1) % 3];
+                const real* b = s[(k + 2) % 3];
+                real eF = sgn * edge_fn(a, b, cF), eO = sgn * edge_fn(a, b, cO);
+                real tc = eF / (eF - eO);
+                w = branch > 0 ? tc - (real)0.5 : (real)0.5 - tc;
+            }
+            for (int c = 0; c < C; ++c) col[c] = 0, cs[c] = 0;
+            if (tt >= 0) pixel_color(pos, tri, attr, C, tt, tgt, H, W, col);
+            if (ts >= 0) pixel_color(pos, tri, attr, C, ts, src, H, W, cs);
+            for (int c = 0; c < C; ++c) total += (double)sign[tgt * C + c] * (double)(w * (cs[c] - col[c]));
+        }
+        part[tid] = total;
+    }
+    double total = 0.0;
+    for (int i = 0; i < nt; ++i) total += part[i];
+    free(part);
+    *result = total;
+    return ORC_OK;
+}

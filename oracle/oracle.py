@@ -26,7 +26,7 @@ from . import build as _build
 __all__ = [
     "load", "triidx_to_float", "float_to_triidx", "raster_ids", "rasterize", "raster_bwd",
     "interpolate", "interpolate_bwd", "interpolate_sparse", "topology", "antialias", "antialias_bwd",
-    "key_tri", "default_threads",
+    "key_tri", "default_threads", "aa_plan", "l1_fixed_visibility",
 ]
 
 _LIBS = {}
@@ -64,6 +64,11 @@ def load(precision="f32"):
                                    _p, _c_int]
         lib.orc_aa_bwd.argtypes = [_p, _c_int, _p, _p, _c_long, _c_long, _p, _c_long, _p, _c_int, _c_int, _c_int,
                                    _p, real, _p, _p, _c_int]
+        lib.orc_aa_plan.argtypes = [_p, _p, _c_long, _p, _c_long, _p, _c_int, _c_int, _p, _c_long]
+        lib.orc_aa_plan.restype = _c_long
+        lib.orc_l1_fixed_visibility.argtypes = [_p, _p, _p, _c_int, _c_int, _c_int, _p, _p, _p, _c_long, _p, _p,
+                                                _c_int]
+        lib.orc_l1_fixed_visibility.restype = _c_int
         for name in ["orc_raster_ids", "orc_shade", "orc_raster_bwd", "orc_interp_fwd", "orc_interp_bwd",
                      "orc_interp_sparse_fwd", "orc_topology", "orc_aa_fwd", "orc_aa_bwd"]:
             getattr(lib, name).restype = _c_int
@@ -294,3 +299,50 @@ def antialias_bwd(color, rast, pos, tri, grad_out, nbr=None, pos_gradient_boost=
                           _ptr(nbr), B, H, W, _ptr(go), float(pos_gradient_boost), _ptr(gc), _ptr(gp),
                           nthreads or default_threads()), "aa_bwd")
     return gc, gp
+
+
+
+def aa_plan(rast, pos, tri, nbr=None):
+    """The decisions of one view's antialias forward, evaluated in float (the
+    CUDA forward's decisions): an (n, 8) int32 array of (target pixel, source
+    pixel, front pixel, other pixel, front triangle, crossing edge, branch,
+    orientation sign); see orc_aa_plan.  rast: (H, W, 4) or (1, H, W, 4)."""
+    rast = np.asarray(rast, dtype=np.float32)
+    H, W = rast.shape[-3], rast.shape[-2]
+    rast = np.ascontiguousarray(rast.reshape(-1, 4))
+    posr = np.ascontiguousarray(pos, dtype=np.float32)
+    tri = np.ascontiguousarray(tri, dtype=np.int32)
+    nbr = np.ascontiguousarray(topology(tri) if nbr is None else nbr, dtype=np.int32)
+    lib = load("f32")
+    cap = max(1024, H * W // 8)
+    while True:
+        plan = np.empty((cap, 8), np.int32)
+        n = lib.orc_aa_plan(_ptr(rast), _ptr(posr), posr.shape[0], _ptr(tri), tri.shape[0], _ptr(nbr), H, W,
+                            _ptr(plan), cap)
+        if n <= cap:
+            return plan[:n].copy()
+        cap = n
+
+
+def l1_fixed_visibility(pos, tri, attr, ids, sign, plan, resolution, tri_flag=None, nthreads=None):
+    """Sum over pixels and channels of sign * antialiased colour, in float64,
+    with every discrete decision of the forward held fixed: ids (H*W
+    triangle indices, -1 background), plan (aa_plan) and sign (H*W*C values
+    in {-1, 0, 1}).  tri_flag (one byte per triangle) restricts the sum to
+    the terms that involve a flagged triangle (see orc_l1_fixed_visibility)."""
+    H, W = resolution
+    posr = np.ascontiguousarray(pos, dtype=np.float64)
+    tri = np.ascontiguousarray(tri, dtype=np.int32)
+    attr = np.ascontiguousarray(attr, dtype=np.float64)
+    ids = np.ascontiguousarray(ids, dtype=np.int32).reshape(-1)
+    sign = np.ascontiguousarray(sign, dtype=np.int8).reshape(-1)
+    plan = np.ascontiguousarray(plan, dtype=np.int32)
+    C = attr.shape[-1]
+    if ids.size != H * W or sign.size != H * W * C:
+        raise ValueError("ids / sign do not match the resolution")
+    flag = None if tri_flag is None else np.ascontiguousarray(tri_flag, dtype=np.uint8)
+    out = np.zeros(1, np.float64)
+    _check(load("f64").orc_l1_fixed_visibility(_ptr(posr), _ptr(tri), _ptr(attr), C, H, W, _ptr(ids), _ptr(sign),
+                                               _ptr(plan), plan.shape[0], _ptr(flag), _ptr(out),
+                                               nthreads or default_threads()), "l1_fixed_visibility")
+    return float(out[0])

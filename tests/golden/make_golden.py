@@ -1,9 +1,10 @@
 """Generate golden vectors by running the reference diffrp session code.
 
 Run from the repository root in a container where the reference tree is
-mounted (default /root/reference, or $DIFFRP_REFERENCE):
+present, naming its root in $DIFFRP_REFERENCE (the directory holding the
+``diffrp`` package):
 
-    python tests/golden/make_golden.py
+    DIFFRP_REFERENCE=<reference root> python tests/golden/make_golden.py [scenario ...]
 
 The reference's own Python -- Scene / MeshObject.preprocess, the vertex
 array object, the stencil-masked and full-screen interpolators, material
@@ -15,7 +16,12 @@ few standard matrix helpers the camera needs (translation, inverse, GL
 perspective, focal length); the rest (loaders, path tracer, image IO) by
 inert stubs that are never called.  ``device='cuda'`` allocations inside
 the reference are redirected to CPU.  Output: ``tests/golden/session_*.npz``
-with the inputs and the reference's outputs and gradients.
+with the inputs and the reference's outputs and gradients.  The config-1
+scenario (``session_c1.npz``: 642-vertex icosphere at 512x512, L2 loss) is
+stored as signatures instead of whole images to keep the file small: the
+triangle-id map, a SHA-256 of the raster buffer's bytes, per-row float64
+sums and a seeded sample of pixels of each image, the loss and the vertex
+gradients.
 """
 import importlib
 import importlib.abc
@@ -30,7 +36,7 @@ import numpy as np
 sys.dont_write_bytecode = True
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("DIFFRP_REFERENCE", "/root/reference")
+REF = os.environ.get("DIFFRP_REFERENCE")
 sys.path.insert(0, ROOT)
 
 import torch  # noqa: E402
@@ -115,6 +121,8 @@ def _install_stubs():
 
 
 def _load_reference():
+    if not REF:
+        raise SystemExit("set DIFFRP_REFERENCE to the reference tree's root (the directory holding diffrp/)")
     if not os.path.isdir(os.path.join(REF, "diffrp")):
         raise SystemExit("reference tree not found at %s" % REF)
     sys.path.insert(0, REF)
@@ -194,7 +202,43 @@ def scenario_inputs():
     sc["objects_masked"] = dict(base, impl="stencil_masked")
     sc["objects_full"] = dict(base, impl="full_screen")
     sc["layers"] = dict(base, impl="stencil_masked", alpha=0.6)
+    # config 1 (the README example at benchmark size): icosphere with 3
+    # subdivisions (642 vertices) of radius 0.8, default camera at
+    # (0, 0, 3.2), fov 30, 512x512, far 100; camera-space normals through
+    # nvdr_antialias; L2 loss to a seeded N(0, 0.1) target
+    v, f = S.icosphere(3, 0.8)
+    sc["c1"] = dict(verts=v, tris=f, h=512, w=512, fov=30.0, near=0.1, far=100.0, target_seed=0)
     return sc
+
+
+def c1_target(seed, h, w):
+    """N(0, 0.1) target image (h, w, 3) float32 by Box-Muller over the
+    PCG64 stream's uniform doubles (stable across numpy versions, unlike
+    Generator.normal's algorithm)."""
+    u = np.random.default_rng(int(seed)).random((2, h, w, 3))
+    z = np.sqrt(-2.0 * np.log1p(-u[0])) * np.cos(2.0 * np.pi * u[1])
+    return (0.1 * z).astype(np.float32)
+
+
+C1_SAMPLES = 4096
+
+
+def c1_signature(out, seed=11):
+    """Small signature of a config-1 render: triangle ids, SHA-256 of the
+    raster bytes, per-row float64 sums and a seeded pixel sample of each
+    image, the loss and the vertex gradient."""
+    import hashlib
+    rast = np.ascontiguousarray(out["rast"], np.float32)
+    H, W = rast.shape[1:3]
+    idx = np.random.default_rng(seed).choice(H * W, C1_SAMPLES, replace=False)
+    sig = {"ids": rast[0, ..., 3].astype(np.int16), "rast_sha256": np.frombuffer(
+        hashlib.sha256(rast.tobytes()).digest(), np.uint8), "sample_idx": idx.astype(np.int64),
+        "clip": out["clip"], "loss": np.float64(out["loss"]), "grad_verts": out["grad_verts"]}
+    for key in ("rast", "normals", "aa"):
+        img = out[key].reshape(H, W, -1) if key != "rast" else rast[0]
+        sig[key + "_rowsum"] = img.astype(np.float64).sum(axis=1)
+        sig[key + "_sample"] = img.reshape(H * W, -1)[idx]
+    return sig
 
 
 def build_scene(api, d, name):
@@ -208,7 +252,7 @@ def build_scene(api, d, name):
     t = lambda a: torch.tensor(np.asarray(a), device=dev)  # noqa: E731
     leaves = {}
     scene = Scene()
-    if name == "normals":
+    if name in ("normals", "c1"):
         verts = t(d["verts"]).requires_grad_(True)
         leaves["verts"] = verts
         scene.add_mesh_object(MeshObject(DefaultMaterial(), verts, t(d["tris"])))
@@ -238,20 +282,31 @@ def build_scene(api, d, name):
     return scene, cam, leaves
 
 
-def render(api, d, name, session_cls, options_cls, ctx=None):
-    """Render a scenario's outputs and gradients with the given session class."""
+def render(api, d, name, session_cls, options_cls, ctx=None, on_session=None):
+    """Render a scenario's outputs and gradients with the given session class.
+    on_session(rp), when given, is called on the new session before anything
+    is rendered (the tests use it to inject the reference's clip space)."""
     scene, cam, leaves = build_scene(api, d, name)
+    hook = on_session if on_session is not None else (lambda rp: None)
     out = {}
-    if name == "normals":
+    if name in ("normals", "c1"):
         rp = session_cls(scene, cam, ctx=ctx)
+        hook(rp)
         n = rp.false_color_camera_space_normal()
         aa = rp.nvdr_antialias(n[..., :3])
-        (aa * torch.as_tensor(d["weight"], device=api["device"])).sum().backward()
+        if name == "normals":
+            (aa * torch.as_tensor(d["weight"], device=api["device"])).sum().backward()
+        else:
+            target = torch.as_tensor(c1_target(d["target_seed"], int(d["h"]), int(d["w"])), device=api["device"])
+            loss = (aa - target).square().mean()
+            loss.backward()
+            out["loss"] = loss
         out.update(normals=n, aa=aa, clip=rp.clip_space(), rast=rp.rasterize()[0])
     else:
         opts = options_cls(interpolator_impl=d["impl"])
         opaque = d.get("alpha") is None
         rp = session_cls(scene, cam, opaque_only=opaque, options=opts, ctx=ctx)
+        hook(rp)
         alb = rp.albedo()
         pos = rp.world_position()
         # depth() goes through transform_point4x3 (addmm), which only takes
@@ -304,10 +359,15 @@ def main():
                PerspectiveCamera=mods["diffrp.rendering.camera"].PerspectiveCamera, device="cpu")
     sd = mods["diffrp.rendering.surface_deferred"]
     from tests.golden import oracle_dr
+    only = set(sys.argv[1:])  # scenario names to (re)generate; all when none are given
     for name, d in scenario_inputs().items():
+        if only and name not in only:
+            continue
         res = render(api, d, name, sd.SurfaceDeferredRenderSession, sd.SurfaceDeferredRenderSessionOptions,
                      ctx=oracle_dr.RasterizeCudaContext())
         payload = {"in_" + k: np.asarray(v) for k, v in d.items() if not isinstance(v, str)}
+        if name == "c1":
+            res = c1_signature(res)
         payload.update({"out_" + k: v for k, v in res.items()})
         path = os.path.join(HERE, "session_%s.npz" % name)
         np.savez_compressed(path, **payload)

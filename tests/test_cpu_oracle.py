@@ -214,3 +214,44 @@ def test_backward_precision_f32_terms_match_f64():
         out[prec] = (gp + O.raster_bwd(pos, tri, rast, gr, precision=prec), ga)
     for a, b in zip(out["f32"], out["f64"]):
         assert np.abs(a - b).max() <= 1e-4 * np.abs(b).max()
+
+
+def test_fixed_visibility_l1_matches_forward_and_backward():
+    """The fixed-decision float64 loss of tests/fd.py equals the float forward
+    at the base point, and its Ridders-refined central differences (from
+    eps 1e-3) reproduce the oracle backward that takes the float forward's
+    decisions: positions (clip and world coordinates) and attributes of 24
+    seeded vertices of a displaced icosphere at 192 x 192, 8 channels."""
+    from diffrp_gb300 import synthetic as S
+    from tests.fd import FixedVisibilityL1
+    H = W = 192
+    v, f = S.displaced_icosphere(3, 0.8, 0.02, 5)
+    rng = np.random.default_rng(6)
+    attr = rng.uniform(0, 1, (len(v), 8)).astype(np.float32)
+    mvp = S.perspective(30.0, H, W, 0.1, 100.0).astype(np.float64) @ \
+        S.view_matrix(S.lookat_pose((0.3, 0.2, 3.1))).astype(np.float64)
+    pos = S.clip_positions(v, mvp)
+    target = rng.uniform(0, 1, (H, W, 8)).astype(np.float32)
+    rast, _, _ = O.rasterize(pos, f, (H, W), grad_db=False)
+    col, _ = O.interpolate(attr, rast, f)
+    nbr = O.topology(f)
+    out = O.antialias(col, rast, pos, f, nbr)
+    fd = FixedVisibilityL1(pos, f, attr, target, rast[0], out[0], nbr)
+    assert len(fd.plan) > 100
+    base = fd.loss_terms()
+    ref = (fd.sign.astype(np.float64) * out.reshape(-1)).sum()
+    assert abs(base - ref) <= 1e-6 * abs(ref)
+
+    g_out = (np.sign(out - target[None]) / np.float32(out.size)).astype(np.float32)
+    g_col, g_pos_aa = O.antialias_bwd(col, rast, pos, f, g_out, nbr, precision="f32")
+    g_attr, g_rast, _ = O.interpolate_bwd(attr, rast, f, g_col, precision="f32")
+    g_pos = g_pos_aa + O.raster_bwd(pos, f, rast, g_rast, precision="f32")
+    pick = fd.pick_vertices(24, seed=3)
+    G = np.array([fd.grad_pos(j)[0] for j in pick])
+    assert np.abs(G - g_pos[pick]).max() <= 1e-4 * np.abs(G).max()
+    assert np.abs(G[:, 2]).max() == 0.0  # clip z carries no gradient with the decisions held
+    Gw = np.array([fd.grad_pos(j, (0, 1, 2), mvp=mvp, verts=v)[0] for j in pick[:8]])
+    gw = g_pos[pick[:8]] @ mvp[:, :3]
+    assert np.abs(Gw - gw).max() <= 1e-4 * np.abs(Gw).max()
+    A = np.array([fd.grad_attr(j) for j in pick])
+    assert np.abs(A - g_attr[pick]).max() <= 1e-5 * np.abs(A).max()
