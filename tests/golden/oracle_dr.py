@@ -4,7 +4,11 @@ session code).
 
 Exposes the names diffrp calls (RasterizeCudaContext, DepthPeeler,
 interpolate, antialias) on CPU tensors, with autograd through the oracle's
-float64 backward.
+backward evaluated like a float32 implementation's: every per-pixel term in
+float32 (so each branch -- antialias edge, blended pixel, clamping -- is the
+one the float32 forward took) and the sums in float64.  A float64 evaluation
+of the terms would resolve a few near-tie antialias pairs the other way than
+the forward did, which changes the position gradients of their vertices.
 """
 import numpy as np
 import torch
@@ -39,8 +43,8 @@ class _Raster(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g_rast, g_db):
         pos, = ctx.saved_tensors
-        g = O.raster_bwd(_np(pos, np.float64), ctx.tri, ctx.rast, _np(g_rast, np.float64),
-                         None if g_db is None else _np(g_db, np.float64))
+        g = O.raster_bwd(_np(pos), ctx.tri, ctx.rast, _np(g_rast), None if g_db is None else _np(g_db),
+                         precision="f32")
         return torch.from_numpy(g).to(pos.dtype), None, None, None, None
 
 
@@ -85,8 +89,7 @@ class _Interp(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g):
         attr, rast, tri = ctx.saved_tensors
-        ga, gr, _ = O.interpolate_bwd(_np(attr, np.float64), _np(rast, np.float64), _np(tri, np.int32),
-                                      _np(g, np.float64))
+        ga, gr, _ = O.interpolate_bwd(_np(attr), _np(rast), _np(tri, np.int32), _np(g), precision="f32")
         return torch.from_numpy(ga).float(), torch.from_numpy(gr).float(), None
 
 
@@ -105,8 +108,7 @@ class _AA(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g):
         color, rast, pos, tri = ctx.saved_tensors
-        gc, gp = O.antialias_bwd(_np(color, np.float64), _np(rast, np.float64), _np(pos, np.float64),
-                                 _np(tri, np.int32), _np(g, np.float64))
+        gc, gp = O.antialias_bwd(_np(color), _np(rast), _np(pos), _np(tri, np.int32), _np(g), precision="f32")
         return torch.from_numpy(gc).float(), None, torch.from_numpy(gp).float(), None
 
 
