@@ -21,6 +21,14 @@ Lines printed (rank 0, one JSON line):
               CUDA-event time vs the measured HBM copy bandwidth;
   cpu_baseline  the CPU oracle (a restatement of the path, all host threads)
               on a bounded sample of the same workload.
+Attached beside the headline (each with ms_per_step, a whole-step roofline
+fraction from the path's byte model and, for the batched ones, the peak
+device memory): batched_views64 (64 views of the 1280-triangle icosphere at
+512x512, batched vs plain per-view), config1_session (the README example at
+512x512 through SurfaceDeferredRenderSession), batched_uneven48 (48 meshes,
+135 items, batched vs plain), batched_large16 (2.09M-triangle heightfield,
+16 views at 2048x2048, recompute in chunks, with the stored-buffer run and
+its peak memory beside it).
 
 ``--impl reference`` times the CPU implementation of the path (the oracle
 port: the reference's own rasteriser is an external CUDA package that does
@@ -191,10 +199,11 @@ class BatchStep:
     """The same step through the batching form (one item): fused raster +
     interpolation, antialias, fused backward (diffrp_gb300.batch)."""
 
-    def __init__(self, dev, f, mvp, target, V, C, tile=(4, 0), fused_loss=True):
+    def __init__(self, dev, f, mvp, target, V, C, tile=(4, 0), fused_loss=True, grads_in_forward=True):
         import torch
         from diffrp_gb300.batch import BatchRenderer
         self.torch = torch
+        self.grads_in_forward = grads_in_forward
         self.tri = torch.from_numpy(f).to(dev)
         self.mvp = torch.from_numpy(mvp).to(dev)
         self.target = torch.from_numpy(target).to(dev).reshape(-1)
@@ -208,7 +217,8 @@ class BatchStep:
         attr.grad = None
         clip = clip_space(verts, self.mvp)
         if self.fused_loss:
-            loss, _ = self.renderer.render_l1(clip, attr.reshape(-1), self.target)
+            loss, _ = self.renderer.render_l1(clip, attr.reshape(-1), self.target,
+                                              grads_in_forward=self.grads_in_forward)
         else:
             loss = l1_loss(self.renderer(clip, attr.reshape(-1)), self.target)
         loss.backward()
@@ -297,11 +307,12 @@ class MultiViewWorkload:
         return clip_space_packed([(v, mv) for v, mv in zip(self.verts, self.mesh_mvps) if mv is not None])
 
     def batched_step(self):
-        """The batching form with the L1 loss fused into its antialias pass."""
+        """The batching form with the L1 loss and its gradient formed in its
+        antialias pass."""
         self._zero()
         pos = self._packed_clip()
         attr = self.torch.cat([a.reshape(-1) for a in self.attrs])
-        loss, _ = self.renderer.render_l1(pos, attr, self.target)
+        loss, _ = self.renderer.render_l1(pos, attr, self.target, grads_in_forward=True)
         loss.backward()
         return loss
 
@@ -375,13 +386,19 @@ def large16_workload(dev, seed=0):
     return [(v, f, 12)], items
 
 
+_WORKLOADS = {}  # generated batched workloads (meshes, items), reused by later runs
+
+
 def run_batched(dev, name, steps, warmup, plain=True, recompute=False, tune=True, tile=None):
     """Mpix/s of the batched form (graph-captured) and of the plain per-item
     drop-in calls (eager, and graph-captured when it fits) on one workload."""
     import torch
     from diffrp_gb300 import autotune
-    meshes, items = {"views64": views64_workload, "uneven48": uneven48_workload,
-                     "large16": large16_workload}[name](dev)
+    if name not in _WORKLOADS:
+        _WORKLOADS[name] = {"views64": views64_workload, "uneven48": uneven48_workload,
+                            "large16": large16_workload}[name](dev)
+    meshes, items = _WORKLOADS[name]
+    torch.cuda.empty_cache()
     torch.cuda.reset_peak_memory_stats(dev)
     wl = MultiViewWorkload(dev, meshes, items, recompute=recompute, tile=tile)
     if tune and tile is None:
@@ -411,11 +428,16 @@ def run_batched(dev, name, steps, warmup, plain=True, recompute=False, tune=True
         return sum(a.elapsed_time(b) for a, b in evs) / n
 
     ms = timed(g.replay, steps)
+    peak, _ = _peaks()
+    nbytes = step_bytes(meshes, items, recompute)
+    res["step_bytes"] = nbytes
     res["batched"] = {"value": wl.pixels / ms / 1e3, "unit": UNIT, "ms_per_step": ms,
-                      "launches_per_step": g.launches_per_step, "path": "batched, one CUDA graph"}
+                      "launches_per_step": g.launches_per_step, "path": "batched, one CUDA graph",
+                      "step_roofline_frac": nbytes / (ms / 1e3) / 1e9 / peak}
     res["peak_memory_gb"] = torch.cuda.max_memory_allocated(dev) / 1e9
+    res["batched"]["recompute"] = bool(recompute)
     if recompute:
-        res["batched"]["recompute"] = True
+        res["batched"]["chunks"] = len(wl.renderer._chunks)
     if plain:
         for _ in range(max(2, warmup)):
             n0 = kernel_launches()
@@ -423,13 +445,112 @@ def run_batched(dev, name, steps, warmup, plain=True, recompute=False, tune=True
             plain_launches = kernel_launches() - n0
         ms_p = timed(wl.plain_step, max(3, steps // 4))
         res["plain_eager"] = {"value": wl.pixels / ms_p / 1e3, "unit": UNIT, "ms_per_step": ms_p,
-                              "launches_per_step": plain_launches}
+                              "launches_per_step": plain_launches,
+                              "step_roofline_frac": step_bytes(meshes, items) / (ms_p / 1e3) / 1e9 / peak}
         try:
             gp = _graph(wl.plain_step, dev, warm=2)
             ms_g = timed(gp.replay, steps)
-            res["plain_graphed"] = {"value": wl.pixels / ms_g / 1e3, "unit": UNIT, "ms_per_step": ms_g}
+            res["plain_graphed"] = {"value": wl.pixels / ms_g / 1e3, "unit": UNIT, "ms_per_step": ms_g,
+                                    "step_roofline_frac": step_bytes(meshes, items) / (ms_g / 1e3) / 1e9 / peak}
         except RuntimeError as e:  # pragma: no cover
             res["plain_graphed"] = {"unavailable": str(e)[:200]}
+    return res
+
+
+def step_bytes(meshes, items, recompute=False):
+    """Algorithmic bytes of one fwd+bwd (the path's byte model): per pixel
+    16 rast write + 16 rast read (dropped when rasterisation is recomputed)
+    + 4C image write + 4C gradient read; per item V (16 clip read + 16 position
+    gradient write) + 24 F; per mesh V * 8C (attribute read + gradient write)."""
+    total = 0
+    for m, (h, w), _ in items:
+        v, f, c = meshes[m]
+        total += h * w * ((0 if recompute else 32) + 8 * c) + len(v) * 32 + 24 * len(f)
+    for v, f, c in meshes:
+        total += len(v) * 8 * c
+    return total
+
+
+WORKLOAD_C1 = ("icosphere3 642 verts / 1280 tris (flat normals: 3840-vertex face soup), 512x512, camera-space "
+               "normals (3 ch), nvdr_antialias, L2 loss to a seeded N(0, 0.1) target, fwd+bwd to the leaf vertices")
+
+
+def c1_target(seed, h, w):
+    """N(0, 0.1) target (h, w, 3) by Box-Muller over PCG64 uniform doubles."""
+    u = np.random.default_rng(int(seed)).random((2, h, w, 3))
+    return (0.1 * np.sqrt(-2.0 * np.log1p(-u[0])) * np.cos(2.0 * np.pi * u[1])).astype(np.float32)
+
+
+def run_config1(dev, steps, warmup):
+    """The README example at benchmark size through the session API
+    (SurfaceDeferredRenderSession): scene, mesh object and session built
+    every step as a training loop does, camera-space normals, nvdr_antialias,
+    L2 loss, backward to the leaf vertices.  Eager with each interpolator
+    implementation, and the full-screen form captured as one CUDA graph."""
+    import torch
+    from diffrp_gb300 import materials, synthetic as S
+    from diffrp_gb300.scene import MeshObject, Scene
+    from diffrp_gb300.rendering.camera import PerspectiveCamera
+    from diffrp_gb300.rendering.surface_deferred import (SurfaceDeferredRenderSession,
+                                                         SurfaceDeferredRenderSessionOptions)
+    h = w = 512
+    v, f = S.icosphere(3, 0.8)
+    verts = torch.from_numpy(v).to(dev).requires_grad_(True)
+    tris = torch.from_numpy(f).to(dev)
+    target = torch.from_numpy(c1_target(0, h, w)).to(dev)
+    cam = PerspectiveCamera(h=h, w=w, far=100.0)
+
+    def make_step(impl):
+        opts = SurfaceDeferredRenderSessionOptions(interpolator_impl=impl)
+
+        def step():
+            verts.grad = None
+            scene = Scene()
+            scene.add_mesh_object(MeshObject(materials.DefaultMaterial(), verts, tris))
+            rp = SurfaceDeferredRenderSession(scene, cam, options=opts)
+            n = rp.false_color_camera_space_normal()
+            aa = rp.nvdr_antialias(n[..., :3])
+            loss = (aa - target).square().mean()
+            loss.backward()
+            return loss
+        return step
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    s = torch.cuda.current_stream(dev)
+
+    def timed(fn, n):
+        for _ in range(max(3, warmup)):
+            fn()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        torch.cuda.synchronize(dev)
+        for i in range(n):
+            flush.fill_(i & 0xff)
+            evs[i][0].record(s)
+            fn()
+            evs[i][1].record(s)
+        torch.cuda.synchronize(dev)
+        return sum(a.elapsed_time(b) for a, b in evs) / n
+
+    px = h * w
+    nbytes = step_bytes([(np.zeros((3 * len(f), 3)), f, 3)], [(0, (h, w), None)])
+    peak, _ = _peaks()
+    res = {"workload": WORKLOAD_C1, "pixels_per_step": px, "step_bytes": nbytes}
+    for impl in ("stencil_masked", "full_screen"):
+        st = make_step(impl)
+        n0 = kernel_launches()
+        st()
+        launches = kernel_launches() - n0
+        ms = timed(st, steps)
+        res["eager_" + impl] = {"value": px / ms / 1e3, "unit": UNIT, "ms_per_step": ms,
+                                "library_launches_per_step": launches}
+    try:
+        g = _graph(make_step("full_screen"), dev, warm=max(2, warmup))
+        ms = timed(g.replay, steps)
+        res["graphed_full_screen"] = {"value": px / ms / 1e3, "unit": UNIT, "ms_per_step": ms,
+                                      "library_launches_per_step": g.launches_per_step,
+                                      "step_roofline_frac": nbytes / (ms / 1e3) / 1e9 / peak}
+    except RuntimeError as e:  # pragma: no cover
+        res["graphed_full_screen"] = {"unavailable": str(e)[:200]}
     return res
 
 
@@ -558,6 +679,16 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None, batc
         # the step's backward reuses the antialias records and slot bits of its forward
         ops["batch_backward"] = lambda: batch._backward_raw(clip, flat_attr, b_rast, b_color, b_g, b_gp, b_ga,
                                                             batch._fwd_gen, aa_flags=b_flags)
+        # the headline step's forward: loss and its gradient in one pass (the
+        # gradient buffers are zeroed inside the timed graph, as in the step)
+        b_gbuf = torch.zeros(clip.numel() + flat_attr.numel(), dtype=torch.float32, device=dev)
+
+        def fwd_l1_grad():
+            b_gbuf.zero_()
+            batch._forward_raw(clip, flat_attr, b_rast, b_color, b_out,
+                               (b_target, 1.0 / b_color.numel(), b_blocks, b_loss, b_gbuf[:clip.numel()].view_as(clip),
+                                b_gbuf[clip.numel():]), flags=b_flags)
+        ops["batch_forward_l1_grad"] = fwd_l1_grad
     P = H * W
     # Algorithmic bytes per launch: every input read once, every output written once.
     algo = {
@@ -575,6 +706,9 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None, batc
         # rast, colour and output gradient read once; vertex / attribute
         # gradients written once
         "batch_backward": P * (16 + 4 * C + 4 * C) + V * (16 + 4 * C) * 2 + F * 12,
+        # rast, colour and output written, target read; vertex / attribute
+        # gradients written (no sign-gradient image)
+        "batch_forward_l1_grad": P * (16 + 4 * C * 3) + V * (16 + 4 * C) * 2 + F * 12,
     }
     times = {}
     for name, fn in ops.items():
@@ -660,7 +794,8 @@ def main():
     ap.add_argument("--workload", default="single", choices=["single", "views64", "uneven48", "large16"],
                     help="single: the headline single-mesh line (with the 64-view batched comparison "
                          "attached); others: one line for that batched workload")
-    ap.add_argument("--no-batched", action="store_true", help="skip the attached 64-view comparison")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the attached lines (64 views, config-1 session, 48 meshes, large heightfield)")
     ap.add_argument("--tile", default=None,
                     help="fixed raster shape 'tile_log2,threads_per_tri' instead of autotuning (profiling runs)")
     args = ap.parse_args()
@@ -741,7 +876,11 @@ def main():
     batched = GraphedStep(bstep, verts_np, attr_np, dev)
     for _ in range(W_):
         batched()
-    # the same batching form with the separate l1_loss op (reported beside)
+    # the same batching form with the loss's gradient from a backward pass,
+    # and with the separate l1_loss op (reported beside)
+    bstep.grads_in_forward = False
+    batched_bwd_pass = None if args.mode == "steps" else GraphedStep(bstep, verts_np, attr_np, dev)
+    bstep.grads_in_forward = True
     bstep.fused_loss = False
     batched_unfused = None if args.mode == "steps" else GraphedStep(bstep, verts_np, attr_np, dev)
     bstep.fused_loss = True
@@ -781,6 +920,7 @@ def main():
             dist.destroy_process_group()
         return 0
     plain_ms = timed(graphed, args.steps)
+    bwd_pass_ms = timed(batched_bwd_pass, args.steps)
     unfused_ms = timed(batched_unfused, args.steps)
     eager_ms = timed(lambda: step(verts, attr), args.steps)
 
@@ -811,7 +951,9 @@ def main():
 
     if rank == 0:
         times, algo = kernel_breakdown(dev, verts_np, f, attr_np, mvp, target, tuned=tuned, batch=bstep.renderer)
-        dom = max(["batch_forward_l1", "batch_backward"], key=times.get)
+        # the headline step is batch_forward_l1_grad and one scaling of the
+        # gradients: that entry point dominates it
+        dom = "batch_forward_l1_grad"
         peak, peak_kind = _peaks()
         achieved = algo[dom] / (times[dom] / 1e3) / 1e9
         traffic = None
@@ -830,8 +972,9 @@ def main():
                        "global_batch": world, "resolution": [H, W], "channels": C,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "flushed between steps (256 MiB write outside the timed events)",
-                       "path": "batching form (diffrp_gb300.batch, one item) with the L1 loss fused into its "
-                               "antialias pass (BatchRenderer.render_l1), whole fwd+bwd step as one CUDA graph",
+                       "path": "batching form (diffrp_gb300.batch, one item) with the L1 loss and its gradient "
+                               "formed in its antialias pass (BatchRenderer.render_l1, grads_in_forward; the "
+                               "backward is one scaling of the gradients), whole fwd+bwd step as one CUDA graph",
                        "raster_tuning": {"tile": 1 << btuned["tile_log2"],
                                          "threads_per_tri": btuned["threads_per_tri"],
                                          "plain_path": {"tile": 1 << tuned["tile_log2"],
@@ -845,6 +988,10 @@ def main():
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                          "algorithmic_bytes": algo[dom], "kernel_ms": times[dom]},
             "kernel_ms": times,
+            "batched_loss_grad_in_backward": {"value": pix / (bwd_pass_ms / 1e3) / 1e6, "unit": UNIT,
+                                              "ms_per_step": bwd_pass_ms / args.steps,
+                                              "note": "batching form, fused L1 loss, its gradient formed by the "
+                                                      "backward pass (drp_batch_backward) instead of in the forward"},
             "batched_unfused_loss": {"value": pix / (unfused_ms / 1e3) / 1e6, "unit": UNIT,
                                      "ms_per_step": unfused_ms / args.steps,
                                      "note": "batching form, loss by the separate l1_loss op (image written, "
@@ -859,14 +1006,25 @@ def main():
             # timed regions: batched graph, its two e2e graphs, the unfused-loss batched graph, drop-in
             # graph, its e2e graph and the eager drop-in step
             "gpu_launches": (batched.launches_per_step + batched_unfused.launches_per_step +
+                             batched_bwd_pass.launches_per_step +
                              graphed.launches_per_step * 2 + sum(gs.launches_per_step for gs in e2e_graphs)) *
                             args.steps,
             "launches_per_step": {"batched": batched.launches_per_step,
+                                  "batched_loss_grad_in_backward": batched_bwd_pass.launches_per_step,
                                   "batched_unfused_loss": batched_unfused.launches_per_step,
                                   "dropin": graphed.launches_per_step},
         }
         if not args.no_batched:
-            line["batched_views64"] = run_batched(dev, "views64", steps=max(5, args.steps // 3), warmup=W_)
+            k_small = max(5, args.steps // 3)
+            k_big = max(3, args.steps // 5)
+            line["batched_views64"] = run_batched(dev, "views64", steps=k_small, warmup=W_)
+            line["config1_session"] = run_config1(dev, steps=k_small, warmup=W_)
+            line["batched_uneven48"] = run_batched(dev, "uneven48", steps=k_big, warmup=W_)
+            big = run_batched(dev, "large16", steps=k_big, warmup=W_, plain=False, recompute=True)
+            stored = run_batched(dev, "large16", steps=k_big, warmup=W_, plain=False, recompute=False,
+                                 tile=(big["tile"].bit_length() - 1, big["threads_per_tri"]))
+            big["stored_buffers"] = {"batched": stored["batched"], "peak_memory_gb": stored["peak_memory_gb"]}
+            line["batched_large16"] = big
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(verts_np, f, attr_np, mvp, target)
         print(json.dumps(line))

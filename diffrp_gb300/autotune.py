@@ -111,7 +111,13 @@ def tune_rasterizer(ctx, pos, tri, resolution, ranges=None, reps=5, candidates=N
 def tune_batch(renderer, pos, attr, reps=5, candidates=None):
     """Time the batched forward (``drp_batch_forward``) of ``renderer`` on
     its own items for every (tile size, threads per primitive) candidate and
-    keep the fastest; returns the choice with the measured times."""
+    keep the fastest; returns the choice with the measured times.  A
+    recompute renderer is timed on its first chunk (the size it renders at),
+    so tuning allocates no more than one chunk's buffers."""
+    top = renderer
+    if renderer.recompute:
+        chunk = renderer._chunks[0]
+        renderer, pos = chunk.renderer, pos[chunk.rows]
     if candidates is None:
         # pixel-parallel, or 1 / 2 / 4 threads per primitive (tiny triangles
         # favour one thread walking each small bounding box)
@@ -134,6 +140,6 @@ def tune_batch(renderer, pos, attr, reps=5, candidates=None):
         times["%d/%d" % (tl, tpt)] = ts[len(ts) // 2]
         if best is None or ts[len(ts) // 2] < best[0]:
             best = (ts[len(ts) // 2], tl, tpt)
-    renderer.set_raster_shape(best[1], best[2])
+    top.set_raster_shape(best[1], best[2])
     renderer.forward_buffers(pos, attr)
     return {"tile_log2": best[1], "threads_per_tri": best[2], "ms": best[0], "times_ms": times}

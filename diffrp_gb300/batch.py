@@ -13,9 +13,13 @@ Packed layouts (see ``drp_batch_item`` in include/diffrp_gb300.h):
   positions   (sum over items of the mesh's V, 4) clip-space rows, item order;
   attributes  (sum over meshes of V * C,) floats, mesh order;
   images      (sum over items of H * W * C,) floats, item order.
-``recompute=True`` keeps no per-pixel buffer between forward and backward:
-the backward re-runs the rasteriser (and the fused interpolation, but not the
-antialias pass) instead.
+``recompute=True`` keeps no per-pixel buffer between forward and backward
+except the returned images: items are rendered in chunks of about
+``chunk_pixels`` pixels through one scratch set and one workspace sized for
+the largest chunk, and the backward re-runs each chunk's forward (raster,
+interpolation, antialias pass with its pixel list and, for the fused loss,
+the sign gradient) into that scratch before the chunk's backward.  Peak
+memory is then the images (and the target), plus one chunk's buffers.
 """
 import ctypes
 
@@ -54,6 +58,8 @@ def _register():
                               P, P, P, P, LL, P],
         "drp_batch_forward_l1": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, I, I, ULL,
                                  ctypes.c_uint, P, P, P, P, LL, P, ctypes.c_float, P, P, P, P],
+        "drp_batch_forward_l1_grad": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, I, I, ULL,
+                                      ctypes.c_uint, P, P, P, P, LL, P, ctypes.c_float, P, P, P, P, P],
         "drp_batch_backward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, P, P, P, LL, P, P, P, P,
                                P, I, P],
     }
@@ -62,6 +68,43 @@ def _register():
         fn.argtypes = args
         fn.restype = ctypes.c_int
     return lib
+
+
+class _SharedWorkspace:
+    """The batch workspace buffer, shared by a renderer and its recompute
+    chunks (one buffer sized for the largest user).  records = (buffer,
+    renderer id, forward generation) of the forward whose antialias records
+    the buffer holds."""
+
+    def __init__(self):
+        self.buf = None
+        self.retired = []  # replaced buffers, kept alive for CUDA graphs captured on them
+        self.records = None
+
+    def get(self, nbytes, device):
+        if self.buf is None or self.buf.numel() < nbytes:
+            if self.buf is not None:
+                self.retired.append(self.buf)
+            self.buf = torch.empty(nbytes, dtype=torch.uint8, device=device)
+            self.records = None
+        return self.buf
+
+
+class _Chunk:
+    """A contiguous run of items [i0, i1) of a recompute renderer: its own
+    plan over those items (sharing the parent's triangles, topology and
+    workspace) and its slices of the packed buffers."""
+
+    def __init__(self, parent, i0, i1):
+        self.i0, self.i1 = i0, i1
+        self.renderer = BatchRenderer(parent.meshes, parent.items[i0:i1], device=parent.device,
+                                      tile_log2=parent.tile_log2, threads_per_tri=parent.threads_per_tri,
+                                      bin_depth=parent.bin_depth_mode,
+                                      _shared=(parent.tri, parent.nbr, parent._wsh))
+        it = parent.item_table
+        self.rows = slice(parent.pos_offsets[i0], parent.pos_offsets[i0] + self.renderer.pos_rows)
+        self.pixels = slice(it[i0].pixel_offset, it[i0].pixel_offset + self.renderer.total_pixels)
+        self.floats = slice(it[i0].image_offset, it[i0].image_offset + self.renderer.image_floats)
 
 
 class BatchRenderer:
@@ -73,9 +116,14 @@ class BatchRenderer:
     bin_depth: None sizes fixed-depth tile bins from the first forward's
     largest tile (one setup pass per forward afterwards); 0 keeps exact tile
     lists (count, scan and fill passes); n > 0 fixes the depth.
+    recompute: keep no per-pixel buffer for the backward but the returned
+    images; render in chunks of consecutive items of about chunk_pixels
+    pixels (at least one item each) and recompute each chunk's forward in
+    the backward.
     """
 
-    def __init__(self, meshes, items, device=None, tile_log2=4, threads_per_tri=0, recompute=False, bin_depth=None):
+    def __init__(self, meshes, items, device=None, tile_log2=4, threads_per_tri=0, recompute=False, bin_depth=None,
+                 chunk_pixels=1 << 23, _shared=None):
         _register()
         self.bin_depth_mode = bin_depth
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -83,19 +131,24 @@ class BatchRenderer:
         self.threads_per_tri = int(threads_per_tri)
         self.recompute = bool(recompute)
         self.meshes = meshes
-        tri_parts, nbr_parts = [], []
+        if _shared is None:
+            tri_parts, nbr_parts = [], []
+            for tri, V, C in meshes:
+                tri = tri.to(self.device, torch.int32).contiguous()
+                tri_parts.append(tri)
+                nbr_parts.append(nvdr.antialias_construct_topology_hash(tri))
+            self.tri = torch.cat(tri_parts).contiguous()
+            self.nbr = torch.cat(nbr_parts).contiguous()
+            self._wsh = _SharedWorkspace()
+        else:
+            self.tri, self.nbr, self._wsh = _shared
         tri_first, attr_off = [], []
         f0 = a0 = 0
         for tri, V, C in meshes:
-            tri = tri.to(self.device, torch.int32).contiguous()
-            tri_parts.append(tri)
-            nbr_parts.append(nvdr.antialias_construct_topology_hash(tri))
             tri_first.append(f0)
             attr_off.append(a0)
-            f0 += tri.shape[0]
+            f0 += int(tri.shape[0])
             a0 += int(V) * int(C)
-        self.tri = torch.cat(tri_parts).contiguous()
-        self.nbr = torch.cat(nbr_parts).contiguous()
         self.attr_floats = a0
         self.attr_offsets = attr_off
         self._item_specs = []
@@ -110,8 +163,10 @@ class BatchRenderer:
         self.pos_rows = p0
         self.items = items
         self._fwd_gen = 0  # bumped by every forward; the workspace's AA records belong to the latest
-        self._retired = []  # replaced workspaces, kept alive for graphs captured on them
         self._plan()
+        self._chunks = None
+        if self.recompute:
+            self._make_chunks(int(chunk_pixels))
 
     def _plan(self):
         """(Re)build the item table and block maps for the current tile size."""
@@ -139,15 +194,12 @@ class BatchRenderer:
         self._xmap = torch.from_numpy(np.frombuffer(bytes(xmap), dtype=np.int32).copy()).to(self.device)
         self._capacity = 0
         self._depth = 0
-        if getattr(self, "_ws", None) is not None:
-            self._retired.append(self._ws)
-        self._ws = None
         self._pending = None
         self._pinned = None
         self.last_list_entries = 0
         self.last_max_tile = 0
-        self._rec_ws = None  # the workspace buffer holding the latest AA records ...
-        self._rec_gen = -1  # ... and the forward generation that wrote them
+        if getattr(self, "_wsh", None) is not None:
+            self._wsh.records = None  # the record offsets depend on the plan
 
     def set_raster_shape(self, tile_log2, threads_per_tri):
         """Change the fine-raster tile size / threads per primitive (re-plans;
@@ -156,6 +208,30 @@ class BatchRenderer:
         if int(tile_log2) != self.tile_log2:
             self.tile_log2 = int(tile_log2)
             self._plan()
+        for c in self._chunks or []:
+            c.renderer.set_raster_shape(tile_log2, threads_per_tri)
+
+    def _make_chunks(self, chunk_pixels):
+        bounds, i0, px = [], 0, 0
+        for i, (_, (H, W)) in enumerate(self.items):
+            if i > i0 and px + H * W > chunk_pixels:
+                bounds.append((i0, i))
+                i0, px = i, 0
+            px += H * W
+        bounds.append((i0, len(self.items)))
+        self._chunks = [_Chunk(self, a, b) for a, b in bounds]
+
+    def _chunk_scratch(self, l1):
+        """One chunk's buffers, sized for the largest chunk: rast, colour,
+        output, sign gradient (l1) and antialias state."""
+        pix = max(c.renderer.total_pixels for c in self._chunks)
+        flt = max(c.renderer.image_floats for c in self._chunks)
+        blocks = max(c.renderer.pixel_blocks for c in self._chunks)
+        rast = torch.empty((pix, 4), dtype=torch.float32, device=self.device)
+        fl = torch.empty((flt + 63) // 64 * 64 * (3 if l1 else 2), dtype=torch.float32, device=self.device)
+        flags = torch.empty(_ffi.size_out("drp_batch_aa_state_size", pix), dtype=torch.uint8, device=self.device)
+        block_loss = torch.empty(max(1, blocks), dtype=torch.float32, device=self.device)
+        return rast, fl, flags, block_loss
 
     # -- layout helpers ---------------------------------------------------------
     def pack_positions(self, per_item):
@@ -184,11 +260,7 @@ class BatchRenderer:
     # -- execution -------------------------------------------------------------------
     def _workspace(self, cap):
         nbytes = _ffi.size_out("drp_batch_workspace_size", self.total_prims, self.total_tiles, cap)
-        if self._ws is None or self._ws.numel() < nbytes:
-            if self._ws is not None:
-                self._retired.append(self._ws)  # a captured CUDA graph may still use it
-            self._ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
-        return self._ws
+        return self._wsh.get(nbytes, self.device)
 
     def _choose_depth(self, max_tile, needed):
         if self.bin_depth_mode is not None:
@@ -223,8 +295,11 @@ class BatchRenderer:
     def _forward_raw(self, pos, attr, rast, color, out, l1=None, flags=None):
         """out=None writes rast and colour only (no antialias pass).  l1 =
         (target, scale, grad, block_loss, loss) fuses the L1 loss into the
-        antialias pass (drp_batch_forward_l1).  flags: an antialias state
-        block (_flags()) the forward fills for its backward, or None."""
+        antialias pass (drp_batch_forward_l1); l1 = (target, scale,
+        block_loss, loss, grad_pos, grad_attr) also forms the loss's gradient
+        there (drp_batch_forward_l1_grad, flags required).  flags: an
+        antialias state block (_flags()) the forward fills for its backward,
+        or None."""
         if not torch.cuda.is_current_stream_capturing():
             self._poll_stats()
         first = not self._capacity
@@ -242,7 +317,14 @@ class BatchRenderer:
         args = (self._items_dev.data_ptr(), len(self.items), self._pmap.data_ptr(), self.prim_blocks,
                 self._xmap.data_ptr(), self.pixel_blocks, self.total_prims, self.total_tiles, pos.data_ptr(),
                 self.tri.data_ptr(), attr.data_ptr(), self.nbr.data_ptr(), self.tile_log2, self.threads_per_tri)
-        if l1 is not None:
+        if l1 is not None and len(l1) == 6:
+            # the loss's gradient formed in the same pass: (target, scale,
+            # block_loss, loss, grad_pos, grad_attr)
+            target, scale, block_loss, loss, gpos, gattr = l1
+            tail = (target.data_ptr(), ctypes.c_float(scale), block_loss.data_ptr(), loss.data_ptr(),
+                    gpos.data_ptr(), gattr.data_ptr(), stream)
+            entry = "drp_batch_forward_l1_grad"
+        elif l1 is not None:
             target, scale, grad, block_loss, loss = l1
             tail = (target.data_ptr(), ctypes.c_float(scale), grad.data_ptr(), block_loss.data_ptr(),
                     loss.data_ptr(), stream)
@@ -270,8 +352,7 @@ class BatchRenderer:
         else:
             self._queue_stats(ws)
         if out is not None or l1 is not None:  # a raster-only forward writes no AA records
-            self._rec_ws = ws
-            self._rec_gen = self._fwd_gen
+            self._wsh.records = (ws, id(self), self._fwd_gen)
 
     def _backward_raw(self, pos, attr, rast, color, grad_out, grad_pos, grad_attr, gen=None, grad_scale=None,
                       aa_flags=None):
@@ -281,7 +362,7 @@ class BatchRenderer:
         aa_flags: the antialias slot bits that forward wrote, or None."""
         ws = self._workspace(0)  # the backward reads no tile list
         stream = _ffi.stream_of(self.device)
-        flags = REUSE_AA_RECORDS if gen is not None and gen == self._rec_gen and ws is self._rec_ws else 0
+        flags = REUSE_AA_RECORDS if gen is not None and self._wsh.records == (ws, id(self), gen) else 0
         _ffi.call("drp_batch_backward", ws.data_ptr(), ws.numel(), self._items_dev.data_ptr(), len(self.items),
                   self._pmap.data_ptr(), self.prim_blocks, self._xmap.data_ptr(), self.pixel_blocks,
                   self.total_prims, self.total_tiles, pos.data_ptr(), self.tri.data_ptr(), attr.data_ptr(),
@@ -309,19 +390,30 @@ class BatchRenderer:
             raise RuntimeError("attr must hold %d float32 values on the GPU" % self.attr_floats)
         return _BatchFn.apply(pos.contiguous(), attr.contiguous().reshape(-1), self)
 
-    def render_l1(self, pos, attr, target):
+    def render_l1(self, pos, attr, target, grads_in_forward=False):
         """Render and score in one pass: returns (loss, images) with loss =
         mean |images - target| over all image floats (target packed like
         the images).  Differentiable w.r.t. pos and attr through both
         outputs; the loss path never materialises a per-pixel gradient
         product (the upstream loss gradient is applied inside the fused
-        backward)."""
+        backward).
+
+        grads_in_forward=True (items of at most 32 channels): the forward
+        also forms d loss / d pos and d loss / d attr, in the pass that forms
+        the loss (drp_batch_forward_l1_grad), so that a backward reaching only
+        the loss is one multiplication by its upstream gradient -- and, with
+        recompute, re-renders nothing.  A backward that also reaches the
+        images runs the full backward instead (the gradients formed in the
+        forward are then not used)."""
         if pos.shape != (self.pos_rows, 4) or pos.dtype != torch.float32 or not pos.is_cuda:
             raise RuntimeError("pos must be a float32 CUDA tensor of shape (%d, 4)" % self.pos_rows)
         if attr.numel() != self.attr_floats or attr.dtype != torch.float32 or not attr.is_cuda:
             raise RuntimeError("attr must hold %d float32 values on the GPU" % self.attr_floats)
         if target.numel() != self.image_floats or target.dtype != torch.float32 or not target.is_cuda:
             raise RuntimeError("target must hold %d float32 values on the GPU" % self.image_floats)
+        if grads_in_forward and max(int(C) for _, _, C in self.meshes) <= 32:
+            return _BatchL1GradFn.apply(pos.contiguous(), attr.contiguous().reshape(-1),
+                                        target.contiguous().reshape(-1), self)
         return _BatchL1Fn.apply(pos.contiguous(), attr.contiguous().reshape(-1), target.contiguous().reshape(-1),
                                 self)
 
@@ -333,41 +425,61 @@ class BatchRenderer:
         return rast, color, out
 
 
-def _zero_grads(pos, attr):
+def _zero_grads(pos, attr, with_buffer=False):
     """Zeroed gradient buffers for pos and attr from one fill (the fused
-    backward accumulates into them); pos rows stay 16-byte aligned."""
+    backward accumulates into them); pos rows stay 16-byte aligned.
+    with_buffer: also return the one buffer both are views of."""
     buf = torch.zeros(pos.numel() + attr.numel(), dtype=torch.float32, device=pos.device)
-    return buf[:pos.numel()].view_as(pos), buf[pos.numel():].view_as(attr)
+    views = buf[:pos.numel()].view_as(pos), buf[pos.numel():].view_as(attr)
+    return views + (buf,) if with_buffer else views
+
+
+def _chunk_views(r, fl, chunk, l1):
+    """A chunk's colour / output (/ sign gradient) views of the float scratch."""
+    stride = (max(c.renderer.image_floats for c in r._chunks) + 63) // 64 * 64
+    n = chunk.renderer.image_floats
+    views = [fl[k * stride:k * stride + n] for k in range(3 if l1 else 2)]
+    return views
 
 
 class _BatchFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, pos, attr, renderer):
+        ctx.renderer = renderer
+        if renderer.recompute:
+            out = torch.empty(renderer.image_floats, dtype=torch.float32, device=pos.device)
+            rast, fl, flags, _ = renderer._chunk_scratch(l1=False)
+            for c in renderer._chunks:
+                color, _ = _chunk_views(renderer, fl, c, False)
+                c.renderer._forward_raw(pos[c.rows], attr, rast, color, out[c.floats], flags=flags)
+            ctx.save_for_backward(pos, attr)
+            return out
         rast, color = renderer._buffers()
         out = torch.empty_like(color)
         flags = renderer._flags()
         renderer._forward_raw(pos, attr, rast, color, out, flags=flags)
-        ctx.renderer = renderer
         ctx.gen = renderer._fwd_gen
-        if renderer.recompute:
-            ctx.save_for_backward(pos, attr, flags)
-        else:
-            ctx.save_for_backward(pos, attr, flags, rast, color)
+        ctx.save_for_backward(pos, attr, flags, rast, color)
         return out
 
     @staticmethod
     def backward(ctx, grad_out):
         r = ctx.renderer
+        grad_out = grad_out.contiguous()
         if r.recompute:
-            pos, attr, flags = ctx.saved_tensors
-            rast, color = r._buffers()
-            r._forward_raw(pos, attr, rast, color, None)
-            gen = ctx.gen  # the raster-only pass wrote no records; the original forward's may remain
-        else:
-            pos, attr, flags, rast, color = ctx.saved_tensors
-            gen = ctx.gen
+            pos, attr = ctx.saved_tensors
+            grad_pos, grad_attr = _zero_grads(pos, attr)
+            rast, fl, flags, _ = r._chunk_scratch(l1=False)
+            for c in r._chunks:
+                cr = c.renderer
+                color, out = _chunk_views(r, fl, c, False)
+                cr._forward_raw(pos[c.rows], attr, rast, color, out, flags=flags)
+                cr._backward_raw(pos[c.rows], attr, rast, color, grad_out[c.floats], grad_pos[c.rows], grad_attr,
+                                 cr._fwd_gen, aa_flags=flags)
+            return grad_pos, grad_attr, None
+        pos, attr, flags, rast, color = ctx.saved_tensors
         grad_pos, grad_attr = _zero_grads(pos, attr)
-        r._backward_raw(pos, attr, rast, color, grad_out.contiguous(), grad_pos, grad_attr, gen, aa_flags=flags)
+        r._backward_raw(pos, attr, rast, color, grad_out, grad_pos, grad_attr, ctx.gen, aa_flags=flags)
         return grad_pos, grad_attr, None
 
 
@@ -375,33 +487,57 @@ class _BatchL1Fn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, pos, attr, target, renderer):
         ctx.set_materialize_grads(False)
+        ctx.renderer = renderer
+        scale = 1.0 / renderer.image_floats
+        if renderer.recompute:
+            out = torch.empty(renderer.image_floats, dtype=torch.float32, device=pos.device)
+            losses = torch.empty(len(renderer._chunks), dtype=torch.float32, device=pos.device)
+            rast, fl, flags, block_loss = renderer._chunk_scratch(l1=True)
+            for k, c in enumerate(renderer._chunks):
+                color, _, grad = _chunk_views(renderer, fl, c, True)
+                c.renderer._forward_raw(pos[c.rows], attr, rast, color, out[c.floats],
+                                        (target[c.floats], scale, grad, block_loss, losses[k]), flags=flags)
+            ctx.save_for_backward(pos, attr, target)
+            return losses.sum(), out
         rast, color = renderer._buffers()
         out = torch.empty_like(color)
         grad = torch.empty_like(color)
         block_loss = torch.empty(max(1, renderer.pixel_blocks), dtype=torch.float32, device=pos.device)
         loss = torch.empty((), dtype=torch.float32, device=pos.device)
         flags = renderer._flags()
-        renderer._forward_raw(pos, attr, rast, color, out,
-                              (target, 1.0 / renderer.image_floats, grad, block_loss, loss), flags=flags)
-        ctx.renderer = renderer
+        renderer._forward_raw(pos, attr, rast, color, out, (target, scale, grad, block_loss, loss), flags=flags)
         ctx.gen = renderer._fwd_gen
-        if renderer.recompute:
-            ctx.save_for_backward(pos, attr, grad, flags)
-        else:
-            ctx.save_for_backward(pos, attr, grad, flags, rast, color)
+        ctx.save_for_backward(pos, attr, grad, flags, rast, color)
         return loss, out
 
     @staticmethod
     def backward(ctx, g_loss, g_out):
         r = ctx.renderer
         if r.recompute:
-            pos, attr, grad, flags = ctx.saved_tensors
-            rast, color = r._buffers()
-            r._forward_raw(pos, attr, rast, color, None)
-            gen = ctx.gen  # the raster-only pass wrote no records; the original forward's may remain
-        else:
-            pos, attr, grad, flags, rast, color = ctx.saved_tensors
-            gen = ctx.gen
+            pos, attr, target = ctx.saved_tensors
+            grad_pos, grad_attr = _zero_grads(pos, attr)
+            if g_loss is None and g_out is None:
+                return grad_pos, grad_attr, None, None
+            scale = None if g_loss is None else g_loss.reshape(1).to(torch.float32).contiguous()
+            g_out = None if g_out is None else g_out.contiguous()
+            rast, fl, flags, block_loss = r._chunk_scratch(l1=True)
+            loss_c = torch.empty((), dtype=torch.float32, device=pos.device)
+            for c in r._chunks:
+                cr = c.renderer
+                color, out, grad = _chunk_views(r, fl, c, True)
+                cr._forward_raw(pos[c.rows], attr, rast, color, out,
+                                (target[c.floats], 1.0 / r.image_floats, grad, block_loss, loss_c), flags=flags)
+                if g_out is None:
+                    gout, gsc = grad, scale  # sign / n, scaled by the loss gradient inside the kernel
+                elif g_loss is None:
+                    gout, gsc = g_out[c.floats], None
+                else:
+                    gout, gsc = grad * g_loss + g_out[c.floats], None
+                cr._backward_raw(pos[c.rows], attr, rast, color, gout, grad_pos[c.rows], grad_attr, cr._fwd_gen,
+                                 gsc, aa_flags=flags)
+            return grad_pos, grad_attr, None, None
+        pos, attr, grad, flags, rast, color = ctx.saved_tensors
+        gen = ctx.gen
         grad_pos, grad_attr = _zero_grads(pos, attr)
         if g_loss is None and g_out is None:
             return grad_pos, grad_attr, None, None
@@ -414,4 +550,64 @@ class _BatchL1Fn(torch.autograd.Function):
         else:
             gout = (grad * g_loss + g_out).contiguous()
         r._backward_raw(pos, attr, rast, color, gout, grad_pos, grad_attr, gen, scale, aa_flags=flags)
+        return grad_pos, grad_attr, None, None
+
+
+class _BatchL1GradFn(torch.autograd.Function):
+    """render_l1 with the loss's gradient formed in the forward pass."""
+
+    @staticmethod
+    def forward(ctx, pos, attr, target, renderer):
+        ctx.set_materialize_grads(False)
+        ctx.renderer = renderer
+        scale = 1.0 / renderer.image_floats
+        gpos, gattr, gbuf = _zero_grads(pos, attr, with_buffer=True)
+        out = torch.empty(renderer.image_floats, dtype=torch.float32, device=pos.device)
+        if renderer.recompute:
+            losses = torch.empty(len(renderer._chunks), dtype=torch.float32, device=pos.device)
+            rast, fl, flags, block_loss = renderer._chunk_scratch(l1=False)
+            for k, c in enumerate(renderer._chunks):
+                color, _ = _chunk_views(renderer, fl, c, False)
+                c.renderer._forward_raw(pos[c.rows], attr, rast, color, out[c.floats],
+                                        (target[c.floats], scale, block_loss, losses[k], gpos[c.rows], gattr),
+                                        flags=flags)
+            ctx.save_for_backward(pos, attr, target, out, gbuf)
+            return losses.sum(), out
+        rast, color = renderer._buffers()
+        block_loss = torch.empty(max(1, renderer.pixel_blocks), dtype=torch.float32, device=pos.device)
+        loss = torch.empty((), dtype=torch.float32, device=pos.device)
+        flags = renderer._flags()
+        renderer._forward_raw(pos, attr, rast, color, out, (target, scale, block_loss, loss, gpos, gattr),
+                              flags=flags)
+        ctx.gen = renderer._fwd_gen
+        ctx.save_for_backward(pos, attr, target, out, gbuf, flags, rast, color)
+        return loss, out
+
+    @staticmethod
+    def backward(ctx, g_loss, g_out):
+        r = ctx.renderer
+        saved = ctx.saved_tensors
+        pos, attr, target, out, gbuf = saved[:5]
+        if g_out is None:
+            if g_loss is None:
+                return torch.zeros_like(pos), torch.zeros_like(attr), None, None
+            g = gbuf * g_loss.to(torch.float32)
+            return g[:pos.numel()].view_as(pos), g[pos.numel():].view_as(attr), None, None
+        # the images reach the objective too: the full backward of
+        # g_loss * loss + <g_out, images>
+        gout = g_out.contiguous()
+        if g_loss is not None:
+            gout = gout + torch.sign(out - target) * (g_loss.to(torch.float32) / r.image_floats)
+        grad_pos, grad_attr = _zero_grads(pos, attr)
+        if r.recompute:
+            rast, fl, flags, _ = r._chunk_scratch(l1=False)
+            for c in r._chunks:
+                cr = c.renderer
+                color, outc = _chunk_views(r, fl, c, False)
+                cr._forward_raw(pos[c.rows], attr, rast, color, outc, flags=flags)
+                cr._backward_raw(pos[c.rows], attr, rast, color, gout[c.floats], grad_pos[c.rows], grad_attr,
+                                 cr._fwd_gen, aa_flags=flags)
+            return grad_pos, grad_attr, None, None
+        flags, rast, color = saved[5:]
+        r._backward_raw(pos, attr, rast, color, gout, grad_pos, grad_attr, ctx.gen, aa_flags=flags)
         return grad_pos, grad_attr, None, None

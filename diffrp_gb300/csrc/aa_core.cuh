@@ -249,19 +249,24 @@ __device__ __forceinline__ float l1_sign(float d, float scale) {
 
 // Forward of one pixel with the mean-absolute-error loss fused: the output
 // value of every channel as aa_fwd_pixel computes it (written to o when o is
-// not null), g = sign(out - target) * scale, and the return value is the
-// pixel's sum of |out - target| in channel order.  tg, o, g: this pixel's
-// target, output and gradient rows; pair_bits: as aa_fwd_terms.
+// not null), g = sign(out - target) * scale (written when g is not null),
+// and the return value is the pixel's sum of |out - target| in channel
+// order.  tg, o, g: this pixel's target, output and gradient rows;
+// pair_bits: as aa_fwd_terms.  sign_nz / sign_pos (may be null; at most 32
+// channels): bit c set when out - target of channel c is nonzero / positive,
+// which is g without the buffer.
 __device__ __forceinline__ float aa_fwd_pixel_l1(const float4* R, const float* Cc, const float4* rec, long long F,
                                                  int W, int H, int C, int pix, const float* tg, float scale, float* o,
-                                                 float* g, unsigned* pair_bits = nullptr) {
+                                                 float* g, unsigned* pair_bits = nullptr, unsigned* sign_nz = nullptr,
+                                                 unsigned* sign_pos = nullptr) {
     const float* cs = Cc + (long long)pix * C;
     int src[4];
     float wt[4];
     const bool any = aa_fwd_terms(R, rec, F, W, H, pix, src, wt, pair_bits);
     float s = 0.0f;
-    const bool vec = (C & 3) == 0 &&
-                     (((uintptr_t)cs | (uintptr_t)tg | (uintptr_t)g | (uintptr_t)(o ? o : g)) & 15) == 0;
+    unsigned nz = 0u, ps = 0u;
+    const bool vec = (C & 3) == 0 && (((uintptr_t)cs | (uintptr_t)tg | (uintptr_t)(g ? g : cs) |
+                                       (uintptr_t)(o ? o : cs)) & 15) == 0;
     if (vec) {
         for (int c = 0; c < C; c += 4) {
             const float4 b4 = *reinterpret_cast<const float4*>(cs + c);
@@ -286,8 +291,10 @@ __device__ __forceinline__ float aa_fwd_pixel_l1(const float4* R, const float* C
                 const float d = v[k] - tv[k];
                 s += fabsf(d);
                 gv[k] = l1_sign(d, scale);
+                if (d > 0.0f || d < 0.0f) nz |= 1u << ((c + k) & 31);
+                if (d > 0.0f) ps |= 1u << ((c + k) & 31);
             }
-            *reinterpret_cast<float4*>(g + c) = make_float4(gv[0], gv[1], gv[2], gv[3]);
+            if (g) *reinterpret_cast<float4*>(g + c) = make_float4(gv[0], gv[1], gv[2], gv[3]);
         }
     } else {
         for (int c = 0; c < C; ++c) {
@@ -301,11 +308,33 @@ __device__ __forceinline__ float aa_fwd_pixel_l1(const float4* R, const float* C
             if (o) o[c] = v;
             const float d = v - tg[c];
             s += fabsf(d);
-            g[c] = l1_sign(d, scale);
+            if (g) g[c] = l1_sign(d, scale);
+            if (d > 0.0f || d < 0.0f) nz |= 1u << (c & 31);
+            if (d > 0.0f) ps |= 1u << (c & 31);
         }
     }
+    if (sign_nz) *sign_nz = nz;
+    if (sign_pos) *sign_pos = ps;
     return s;
 }
+
+// The incoming image gradient at flat index i (pixel * C + channel), as the
+// backward reads it.  GradBuffer: a gradient buffer times a scale (a loss's
+// upstream gradient applied on the fly; 1 leaves the values unchanged).
+// GradL1: the gradient of the mean-absolute-error loss, sign(out - target) *
+// scale, formed from the output and the target instead of a stored buffer.
+struct GradBuffer {
+    const float* g;
+    float s;
+    __device__ __forceinline__ float operator()(long long i) const { return g[i] * s; }
+};
+
+struct GradL1 {
+    const float* out;
+    const float* tgt;
+    float scale;
+    __device__ __forceinline__ float operator()(long long i) const { return l1_sign(out[i] - tgt[i], scale); }
+};
 
 // Backward pair terms of one pixel.  For every pair slot: role (0 none, 1 this
 // pixel is the blend target, 2 the source), the target pixel and the weight;
@@ -314,12 +343,13 @@ __device__ __forceinline__ float aa_fwd_pixel_l1(const float4* R, const float* C
 // Edge-vertex gradient of one valid, unclamped pair (scattered by the pair's
 // first pixel): dL/dt through the blend weight, then t through the exit
 // edge's two screen vertices to their clip coordinates.
-__device__ __forceinline__ void aa_edge_grad(const AAPair& p, const float* Cc, const float* Gd, int C,
-                                             const float4* P, const int* tri, float4* GP, float boost, float gscale,
-                                             int W, int H) {
+template <class G>
+__device__ __forceinline__ void aa_edge_grad_g(const AAPair& p, const float* Cc, const G& grad, int C,
+                                               const float4* P, const int* tri, float4* GP, float boost, int W,
+                                               int H) {
     float dLdw = 0.f;
     for (int c = 0; c < C; ++c)
-        dLdw = fmaf(Gd[(long long)p.target * C + c] * gscale,
+        dLdw = fmaf(grad((long long)p.target * C + c),
                     Cc[(long long)p.src * C + c] - Cc[(long long)p.target * C + c], dLdw);
     const float dLdt = dLdw * p.sign * boost;
     const float den = p.eF - p.eO;
@@ -339,6 +369,12 @@ __device__ __forceinline__ void aa_edge_grad(const AAPair& p, const float* Cc, c
                                      -(gA0 * hx * pA.x + gA1 * hy * pA.y) * iwA * iwA));
     atomic_add4(GP + vB, make_float4(gB0 * hx * iwB, gB1 * hy * iwB, 0.f,
                                      -(gB0 * hx * pB.x + gB1 * hy * pB.y) * iwB * iwB));
+}
+
+__device__ __forceinline__ void aa_edge_grad(const AAPair& p, const float* Cc, const float* Gd, int C,
+                                             const float4* P, const int* tri, float4* GP, float boost, float gscale,
+                                             int W, int H) {
+    aa_edge_grad_g(p, Cc, GradBuffer{Gd, gscale}, C, P, tri, GP, boost, W, H);
 }
 
 struct AATerms {
@@ -385,16 +421,21 @@ __device__ __forceinline__ void aa_bwd_terms(const float4* R, const float* Cc, c
 // Colour gradient of channel c of a pixel from its terms (slot order).
 // gscale multiplies every incoming gradient as it is read (a loss gradient
 // applied on the fly; 1 leaves them unchanged).
-__device__ __forceinline__ float aa_bwd_channel(const AATerms& at, const float* Gd, int C, int pix, int c,
-                                                float gscale = 1.0f) {
-    const float gs = Gd[(long long)pix * C + c] * gscale;
+template <class G>
+__device__ __forceinline__ float aa_bwd_channel_g(const AATerms& at, const G& grad, int C, int pix, int c) {
+    const float gs = grad((long long)pix * C + c);
     float v = gs;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         if (at.role[q] == 1) v = fmaf(-at.wt[q], gs, v);
-        else if (at.role[q] == 2) v = fmaf(at.wt[q], Gd[(long long)at.tgt[q] * C + c] * gscale, v);
+        else if (at.role[q] == 2) v = fmaf(at.wt[q], grad((long long)at.tgt[q] * C + c), v);
     }
     return v;
+}
+
+__device__ __forceinline__ float aa_bwd_channel(const AATerms& at, const float* Gd, int C, int pix, int c,
+                                                float gscale = 1.0f) {
+    return aa_bwd_channel_g(at, GradBuffer{Gd, gscale}, C, pix, c);
 }
 
 }  // namespace drp

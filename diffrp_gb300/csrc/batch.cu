@@ -57,6 +57,7 @@ struct BatchArgs {
     float* l1_grad;
     float* block_loss;      // one partial per pixel block
     float* loss;
+    bool l1_grads;          // the loss pass also forms the loss's gradient (drp_batch_forward_l1_grad)
     const float* grad_scale;  // backward: device scalar multiplying grad_out, or null
     const float* grad_out;
     float* grad_pos;
@@ -258,7 +259,7 @@ batch_fine_kernel(BatchArgs a) {
         e.out = a.emit_out ? a.out + it.image_offset : nullptr;
         e.vec = (it.channels & 3) == 0 && ((reinterpret_cast<uintptr_t>(e.A) | reinterpret_cast<uintptr_t>(e.color) |
                                             reinterpret_cast<uintptr_t>(e.out)) & 15) == 0;
-        fine_tile<TILE_LOG2, TPT>(ft, e);
+        fine_tile<TILE_LOG2, TPT, false>(ft, e);
     }
 }
 
@@ -358,9 +359,28 @@ __device__ __forceinline__ int find_item_by_pixel(const drp_batch_item* items, i
 // owns the pair), the quad exchanges the slot terms by shuffles, the lanes
 // share the channels (c = q, q + 4, ...) and sum d/du, d/dv by shuffles.
 // Grid-stride over the device-side count, so the launch needs no host sync.
+// The incoming image gradient of one item: the gradient buffer times the
+// upstream scale, or (L1G, the forward that forms the loss's gradient) the
+// L1 sign gradient from the output and the target.
+template <bool L1G>
+struct ItemGrad;
+template <>
+struct ItemGrad<false> {
+    static __device__ __forceinline__ GradBuffer of(const BatchArgs& a, const drp_batch_item& it, float gsc) {
+        return GradBuffer{a.grad_out + it.image_offset, gsc};
+    }
+};
+template <>
+struct ItemGrad<true> {
+    static __device__ __forceinline__ GradL1 of(const BatchArgs& a, const drp_batch_item& it, float) {
+        return GradL1{a.out + it.image_offset, a.target + it.image_offset, a.l1_scale};
+    }
+};
+
+template <bool L1G>
 __global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
     const unsigned n = *a.aa_count;
-    const float gsc = a.grad_scale ? *a.grad_scale : 1.0f;
+    const float gsc = (!L1G && a.grad_scale) ? *a.grad_scale : 1.0f;
     const int lane = threadIdx.x & 31, q = lane & 3, qbase = lane & ~3;
     const long long quads = ((long long)gridDim.x * blockDim.x) >> 2;
     for (long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 2;; i += quads) {
@@ -391,10 +411,10 @@ __global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
                         tgt = p.target;
                         wt = p.w;
                         if (A == pix && !p.clamped)
-                            aa_edge_grad(p, a.color + it.image_offset, a.grad_out + it.image_offset, C,
-                                         reinterpret_cast<const float4*>(a.pos) + it.pos_offset,
-                                         a.tri + 3 * (long long)it.tri_first,
-                                         reinterpret_cast<float4*>(a.grad_pos) + it.pos_offset, 1.0f, gsc, W, H);
+                            aa_edge_grad_g(p, a.color + it.image_offset, ItemGrad<L1G>::of(a, it, gsc), C,
+                                           reinterpret_cast<const float4*>(a.pos) + it.pos_offset,
+                                           a.tri + 3 * (long long)it.tri_first,
+                                           reinterpret_cast<float4*>(a.grad_pos) + it.pos_offset, 1.0f, W, H);
                     }
                 }
             }
@@ -416,12 +436,12 @@ __global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
             const float4 r = reinterpret_cast<const float4*>(a.rast)[it.pixel_offset + pix];
             t = checked_tri(r.w, tri, it.tri_count, it.num_vertices, i0, i1, i2);
             if (t >= 0) {
-                const float* Gd = a.grad_out + it.image_offset;
+                const auto grad = ItemGrad<L1G>::of(a, it, gsc);
                 const float* A = a.attr + it.attr_offset;
                 float* GA = a.grad_attr + it.attr_offset;
                 const float u = r.x, v = r.y, w = 1.0f - u - v;
                 for (int c = q; c < C; c += 4) {
-                    const float g = aa_bwd_channel(at, Gd, C, pix, c, gsc);
+                    const float g = aa_bwd_channel_g(at, grad, C, pix, c);
                     const float x0 = A[(long long)i0 * C + c], x1 = A[(long long)i1 * C + c],
                                 x2 = A[(long long)i2 * C + c];
                     atomicAdd(GA + (long long)i0 * C + c, g * u);
@@ -583,6 +603,143 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
     }
 }
 
+// Antialias + L1 loss with the loss's gradient formed in the same pass
+// (drp_batch_forward_l1_grad).  Every pixel: its output and |error| partial
+// as batch_aa_l1_kernel computes them.  Then, for the pixels no blending pair
+// touches (the listed ones belong to batch_aa_bwd_kernel<true>, which forms
+// the sign from the output and the target), the pixel's whole backward with
+// the upstream gradient sign(out - target) * scale: interpolation backward
+// (attribute gradients) and rasterisation backward (vertex gradients),
+// reduced over runs of one triangle in the warp and scattered with float4
+// atomics -- the work batch_bwd_kernel does for those pixels, done while
+// the pixel's rast row and signs are at hand, with no gradient image written
+// or read back.  The signs pass between the two phases as two bit masks, so
+// an item may have at most 32 channels (more: DRP_DEVERR_CHANNELS, and the
+// item gets no gradient here).  Warps never straddle items (256-pixel blocks).
+__global__ void __launch_bounds__(256, 4) batch_aa_l1_grad_kernel(BatchArgs a) {
+    __shared__ float warp_sum[8];
+    const int2 blk = a.pix_blocks[blockIdx.x];
+    const drp_batch_item& it = a.items[blk.x];
+    const int pix = blk.y * 256 + threadIdx.x;
+    const int W = it.width, H = it.height, C = it.channels;
+    const bool in = pix < W * H;
+    const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
+    float s = 0.0f;
+    unsigned bits = 0u, nz = 0u, ps = 0u;
+    if (in) {
+        const long long row = it.image_offset + (long long)pix * C;
+        s = aa_fwd_pixel_l1(R, a.color + it.image_offset, a.aa_rec + it.prim_offset * 2, it.tri_count, W, H, C, pix,
+                            a.target + row, a.l1_scale, a.out + row, nullptr, &bits, &nz, &ps);
+    }
+    aa_note_pixel(a, it.pixel_offset + pix, in, bits);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.0f;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) t += warp_sum[w];
+        a.block_loss[blockIdx.x] = t;
+    }
+    if (C > 32) {
+        if (threadIdx.x == 0) atomicOr(a.stats + 2, DRP_DEVERR_CHANNELS);
+        return;
+    }
+    const int* tri = a.tri + 3 * (long long)it.tri_first;
+    const float* A = a.attr + it.attr_offset;
+    float* GA = a.grad_attr + it.attr_offset;
+    const float4* P = reinterpret_cast<const float4*>(a.pos) + it.pos_offset;
+    float4* GP = reinterpret_cast<float4*>(a.grad_pos) + it.pos_offset;
+    int t = -1, i0 = 0, i1 = 0, i2 = 0;
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (in && bits == 0u) {
+        r = R[pix];
+        t = checked_tri(r.w, tri, it.tri_count, it.num_vertices, i0, i1, i2);
+    }
+    const Seg seg = seg_setup(t >= 0 ? (long long)t : (long long)(-1 - lane_id()));
+    const float u = r.x, v = r.y, w = 1.0f - u - v;
+    const float sc = a.l1_scale;
+    float gu = 0.f, gv = 0.f;
+    const bool vec = (C & 3) == 0 && ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(GA)) & 15) == 0;
+    for (int c0 = 0; c0 < C; c0 += 4) {
+        float val[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) val[k] = 0.f;
+        if (t >= 0) {
+            float g[4], x0[4], x1[4], x2[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int c = c0 + k;
+                g[k] = (c < C && ((nz >> c) & 1u)) ? (((ps >> c) & 1u) ? sc : -sc) : 0.f;
+            }
+            if (vec) {
+                const float4 q0 = __ldg(reinterpret_cast<const float4*>(A + (long long)i0 * C + c0));
+                const float4 q1 = __ldg(reinterpret_cast<const float4*>(A + (long long)i1 * C + c0));
+                const float4 q2 = __ldg(reinterpret_cast<const float4*>(A + (long long)i2 * C + c0));
+                x0[0] = q0.x; x0[1] = q0.y; x0[2] = q0.z; x0[3] = q0.w;
+                x1[0] = q1.x; x1[1] = q1.y; x1[2] = q1.z; x1[3] = q1.w;
+                x2[0] = q2.x; x2[1] = q2.y; x2[2] = q2.z; x2[3] = q2.w;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int c = c0 + k < C ? c0 + k : C - 1;
+                    x0[k] = A[(long long)i0 * C + c];
+                    x1[k] = A[(long long)i1 * C + c];
+                    x2[k] = A[(long long)i2 * C + c];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                val[k] = g[k] * u;
+                val[4 + k] = g[k] * v;
+                val[8 + k] = g[k] * w;
+                gu = fmaf(g[k], x0[k] - x2[k], gu);
+                gv = fmaf(g[k], x1[k] - x2[k], gv);
+            }
+        }
+        seg_reduce<12>(seg, val);
+        if (t >= 0 && seg.head) {
+            if (vec) {
+                atomic_add4(reinterpret_cast<float4*>(GA + (long long)i0 * C + c0),
+                            make_float4(val[0], val[1], val[2], val[3]));
+                atomic_add4(reinterpret_cast<float4*>(GA + (long long)i1 * C + c0),
+                            make_float4(val[4], val[5], val[6], val[7]));
+                atomic_add4(reinterpret_cast<float4*>(GA + (long long)i2 * C + c0),
+                            make_float4(val[8], val[9], val[10], val[11]));
+            } else {
+                for (int k = 0; k < 4 && c0 + k < C; ++k) {
+                    atomicAdd(GA + (long long)i0 * C + c0 + k, val[k]);
+                    atomicAdd(GA + (long long)i1 * C + c0 + k, val[4 + k]);
+                    atomicAdd(GA + (long long)i2 * C + c0 + k, val[8 + k]);
+                }
+            }
+        }
+    }
+    float pv[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) pv[k] = 0.f;
+    if (t >= 0) {
+        const int py = pix / W, px = pix - py * W;
+        const float X = fmaf((float)(2 * px + 1), __frcp_rn((float)W), -1.0f);
+        const float Y = fmaf((float)(2 * py + 1), __frcp_rn((float)H), -1.0f);
+        float4 g3[3];
+        uv_grad_fast(P[i0], P[i1], P[i2], X, Y, gu, gv, g3);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            pv[3 * k] = g3[k].x;
+            pv[3 * k + 1] = g3[k].y;
+            pv[3 * k + 2] = g3[k].w;
+        }
+    }
+    seg_reduce<9>(seg, pv);
+    if (t >= 0 && seg.head) {
+        atomic_add4(GP + i0, make_float4(pv[0], pv[1], 0.f, pv[2]));
+        atomic_add4(GP + i1, make_float4(pv[3], pv[4], 0.f, pv[5]));
+        atomic_add4(GP + i2, make_float4(pv[6], pv[7], 0.f, pv[8]));
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Host side.
 // ---------------------------------------------------------------------------
@@ -697,33 +854,6 @@ static void launch_batch_raster(const BatchArgs& a, cudaStream_t s) {
     }
 }
 
-int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream_t s) {
-    carve(a, ws, L);
-    cudaMemsetAsync(a.stats, 0, 256, s);  // stats and work queue
-    if (a.aa_count) cudaMemsetAsync(a.aa_count, 0, sizeof(unsigned), s);
-    cudaMemsetAsync(a.tile_count, 0, sizeof(uint32_t) * a.total_tiles, s);
-    switch (a.tile_log2) {
-    case 3: launch_batch_raster<3>(a, s); break;
-    case 5: launch_batch_raster<5>(a, s); break;
-    default: launch_batch_raster<4>(a, s); break;
-    }
-    // (the antialias triangle records were written by the setup / count pass)
-    if (a.target) {
-        if (a.n_pix_blocks > 0) {
-            batch_aa_l1_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
-            drp_note_launch();
-        }
-        launch_l1_final(a.block_loss, a.n_pix_blocks, a.l1_scale, a.loss, s);
-        return 0;
-    }
-    if (!a.out) return 0;  // raster + interpolation only (recomputing them for the backward)
-    if (a.n_pix_blocks > 0) {
-        batch_aa_fwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
-        drp_note_launch();
-    }
-    return 0;
-}
-
 // A side stream with its fork / join events, one per host thread and device,
 // created on first use outside stream capture (inside a capture, before the
 // first ordinary call, the caller's stream serves alone).  Captured forks
@@ -765,6 +895,60 @@ static bool side_stream(cudaStream_t s, SideStream& out) {
     return true;
 }
 
+int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream_t s) {
+    carve(a, ws, L);
+    cudaMemsetAsync(a.stats, 0, 256, s);  // stats and work queue
+    if (a.aa_count) cudaMemsetAsync(a.aa_count, 0, sizeof(unsigned), s);
+    cudaMemsetAsync(a.tile_count, 0, sizeof(uint32_t) * a.total_tiles, s);
+    switch (a.tile_log2) {
+    case 3: launch_batch_raster<3>(a, s); break;
+    case 5: launch_batch_raster<5>(a, s); break;
+    default: launch_batch_raster<4>(a, s); break;
+    }
+    // (the antialias triangle records were written by the setup / count pass)
+    if (a.target && a.l1_grads) {
+        if (a.n_pix_blocks > 0) {
+            batch_aa_l1_grad_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+            drp_note_launch();
+            // the listed pixels' whole backward beside the final loss sum
+            // (both read only what the loss pass wrote)
+            const int sms = drp_current_sm_count();
+            const long long grid = (long long)(sms > 0 ? sms : 1) * 4;
+            const long long g = a.n_pix_blocks < grid ? a.n_pix_blocks : grid;
+            SideStream side;
+            const bool fork = side_stream(s, side);
+            if (fork) {
+                cudaEventRecord(side.fork, s);
+                cudaStreamWaitEvent(side.stream, side.fork, 0);
+            }
+            batch_aa_bwd_kernel<true><<<(unsigned)g, 256, 0, fork ? side.stream : s>>>(a);
+            drp_note_launch();
+            launch_l1_final(a.block_loss, a.n_pix_blocks, a.l1_scale, a.loss, s);
+            if (fork) {
+                cudaEventRecord(side.join, side.stream);
+                cudaStreamWaitEvent(s, side.join, 0);
+            }
+        } else {
+            launch_l1_final(a.block_loss, a.n_pix_blocks, a.l1_scale, a.loss, s);
+        }
+        return 0;
+    }
+    if (a.target) {
+        if (a.n_pix_blocks > 0) {
+            batch_aa_l1_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+            drp_note_launch();
+        }
+        launch_l1_final(a.block_loss, a.n_pix_blocks, a.l1_scale, a.loss, s);
+        return 0;
+    }
+    if (!a.out) return 0;  // raster + interpolation only (recomputing them for the backward)
+    if (a.n_pix_blocks > 0) {
+        batch_aa_fwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+        drp_note_launch();
+    }
+    return 0;
+}
+
 int launch_batch_backward(BatchArgs a, void* ws, const BatchLayout& L, bool reuse_records, cudaStream_t s) {
     carve(a, ws, L);
     if (a.n_prim_blocks > 0 && !reuse_records) {
@@ -792,7 +976,7 @@ int launch_batch_backward(BatchArgs a, void* ws, const BatchLayout& L, bool reus
     }
     batch_bwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
     drp_note_launch();
-    batch_aa_bwd_kernel<<<(unsigned)g, 256, 0, fork ? side.stream : s>>>(a);
+    batch_aa_bwd_kernel<false><<<(unsigned)g, 256, 0, fork ? side.stream : s>>>(a);
     drp_note_launch();
     if (fork) {
         cudaEventRecord(side.join, side.stream);
@@ -986,6 +1170,54 @@ DRP_API int drp_batch_forward_l1(void* workspace, size_t workspace_bytes, const 
     a.loss = loss;
     drp::launch_batch_forward(a, workspace, L, static_cast<cudaStream_t>(stream));
     return drp_check_launch("drp_batch_forward_l1");
+}
+
+DRP_API int drp_batch_forward_l1_grad(void* workspace, size_t workspace_bytes, const drp_batch_item* items,
+                                      int num_items, const int* prim_block_map, long long prim_blocks,
+                                      const int* pixel_block_map, long long pixel_blocks, long long total_prims,
+                                      long long total_tiles, const float* pos, const int* tri, const float* attr,
+                                      const int* nbr, int tile_log2, int threads_per_tri,
+                                      unsigned long long list_capacity, unsigned bin_depth, float* rast, float* color,
+                                      float* out, void* aa_state, long long total_pixels, const float* target,
+                                      float scale, float* block_loss, float* loss, float* grad_pos, float* grad_attr,
+                                      void* stream) {
+    drp::BatchArgs a;
+    drp::BatchLayout L;
+    int st = batch_common(workspace, workspace_bytes, items, num_items, prim_block_map, prim_blocks, pixel_block_map,
+                          pixel_blocks, total_prims, total_tiles, list_capacity, pos, tri, attr, a, L);
+    if (st) return st;
+    if (tile_log2 < 3 || tile_log2 > 5) return bfail("batch: tile_log2 must be 3, 4 or 5");
+    if (threads_per_tri < 0 || threads_per_tri > 32 || (threads_per_tri & (threads_per_tri - 1)))
+        return bfail("batch: threads_per_tri must be 0 or a power of two <= 32");
+    if (!rast || !color || !out || !target || !loss || (pixel_blocks > 0 && !block_loss) ||
+        (reinterpret_cast<uintptr_t>(rast) & 15))
+        return bfail("batch: bad outputs");
+    if (!grad_pos || !grad_attr || (reinterpret_cast<uintptr_t>(grad_pos) & 15))
+        return bfail("batch: bad gradient buffers");
+    if (!aa_state || (reinterpret_cast<uintptr_t>(aa_state) & 255) || total_pixels <= 0)
+        return bfail("batch: the gradient pass needs the antialias state (256-byte aligned, total_pixels > 0)");
+    if (bin_depth && (unsigned long long)total_tiles * bin_depth > list_capacity)
+        return bfail("batch: list_capacity below total_tiles * bin_depth");
+    a.nbr = nbr;
+    a.tile_log2 = tile_log2;
+    a.tpt = threads_per_tri;
+    a.bin_depth = bin_depth;
+    a.rast = rast;
+    a.color = color;
+    a.out = out;
+    carve_aa_state(a, aa_state, total_pixels);
+    a.emit_out = false;  // the fused antialias + loss pass writes every output pixel
+    a.aa_records = true;
+    a.target = target;
+    a.l1_scale = scale;
+    a.l1_grad = nullptr;
+    a.block_loss = block_loss;
+    a.loss = loss;
+    a.l1_grads = true;
+    a.grad_pos = grad_pos;
+    a.grad_attr = grad_attr;
+    drp::launch_batch_forward(a, workspace, L, static_cast<cudaStream_t>(stream));
+    return drp_check_launch("drp_batch_forward_l1_grad");
 }
 
 DRP_API int drp_batch_backward(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,

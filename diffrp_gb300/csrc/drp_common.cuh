@@ -19,6 +19,7 @@
 // Device-side error bits (stats word 2).
 #define DRP_DEVERR_BAD_INDEX 1u
 #define DRP_DEVERR_LIST_OVERFLOW 2u
+#define DRP_DEVERR_CHANNELS 4u
 
 namespace drp {
 

@@ -118,7 +118,9 @@ struct RastEmit {
     }
 };
 
-template <int TILE_LOG2, int TPT>
+// PEEL: a previous layer's keys are given (depth peeling).  Only the
+// pixel-parallel shape (TPT = 0) has a separate instantiation without them.
+template <int TILE_LOG2, int TPT, bool PEEL>
 __global__ void __launch_bounds__((1 << (2 * TILE_LOG2)) < 256 ? (1 << (2 * TILE_LOG2)) : 256,
                                   TILE_LOG2 == 3 ? 12 : 4)
 fine_raster_kernel(RasterArgs a) {
@@ -158,7 +160,7 @@ fine_raster_kernel(RasterArgs a) {
     e.rast = reinterpret_cast<float4*>(a.rast) + b * npix;
     e.db = a.rast_db ? reinterpret_cast<float4*>(a.rast_db) + b * npix : nullptr;
     e.key = a.out_key ? a.out_key + b * npix : nullptr;
-    fine_tile<TILE_LOG2, TPT>(ft, e);
+    fine_tile<TILE_LOG2, TPT, PEEL>(ft, e);
 }
 
 // ---------------------------------------------------------------------------
@@ -235,13 +237,17 @@ static void launch_fine(const RasterArgs& args, int tpt, cudaStream_t s) {
         a.tile_order = a.ws.tile_cursor;
     }
     switch (tpt) {
-    case 0: fine_raster_kernel<TL, 0><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
-    case 1: fine_raster_kernel<TL, 1><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
-    case 2: fine_raster_kernel<TL, 2><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
-    case 4: fine_raster_kernel<TL, 4><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
-    case 8: fine_raster_kernel<TL, 8><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
-    case 16: fine_raster_kernel<TL, 16><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
-    default: fine_raster_kernel<TL, 32><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
+    case 0:
+        if (a.prev_key) fine_raster_kernel<TL, 0, true><<<grid, NT, 0, s>>>(a);
+        else fine_raster_kernel<TL, 0, false><<<grid, NT, 0, s>>>(a);
+        drp_note_launch();
+        break;
+    case 1: fine_raster_kernel<TL, 1, true><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
+    case 2: fine_raster_kernel<TL, 2, true><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
+    case 4: fine_raster_kernel<TL, 4, true><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
+    case 8: fine_raster_kernel<TL, 8, true><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
+    case 16: fine_raster_kernel<TL, 16, true><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
+    default: fine_raster_kernel<TL, 32, true><<<grid, NT, 0, s>>>(a); drp_note_launch(); break;
     }
 }
 

@@ -328,6 +328,9 @@ __device__ __forceinline__ unsigned long long tile_prim_key(const float4& z4, in
 // tiles, 256 threads) warp w owns the 2x2 blocks of the 16x8 region at
 // ((w & 1) * 16, (w >> 1) * 8), q walking them row-major.  A warp can then
 // skip a primitive whose block mask misses its blocks with one uniform test.
+// (Spreading a warp's four blocks over the tile instead -- one per pair of
+// block rows -- balanced the warps better but made every primitive hit more
+// warps: the fine raster took 13 us longer on the single-mesh step.)
 template <int TILE_LOG2, int NTHREADS>
 __device__ __forceinline__ int tile_block(int tid, int q) {
     constexpr int T = 1 << TILE_LOG2;
@@ -380,7 +383,9 @@ struct FineTile {
 //             registers, no atomics);
 //   TPT  > 0: groups of TPT threads walk one primitive's bbox within the tile
 //             and resolve keys with shared-memory atomicMin.
-template <int TILE_LOG2, int TPT, class Emit>
+//   PEEL = false: ft.prev is ignored (no previous layer); the compiler then
+//             keeps no per-pixel previous-layer keys in registers.
+template <int TILE_LOG2, int TPT, bool PEEL, class Emit>
 __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
     constexpr int T = 1 << TILE_LOG2;
     constexpr int NPIX = T * T;
@@ -397,7 +402,7 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
 
     const int tx0 = ft.tx0, ty0 = ft.ty0, W = ft.W, H = ft.H;
     const int tid = threadIdx.x;
-    const unsigned long long* prev_g = ft.prev;
+    const unsigned long long* prev_g = PEEL ? ft.prev : nullptr;
 
     unsigned long long best[PPT], prevk[PPT];
 #pragma unroll

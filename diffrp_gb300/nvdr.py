@@ -16,8 +16,11 @@ follow nvdiffrast's documented interface; the arithmetic is this project's own
 CUDA (``libdiffrp_gb300.so`` through ``_ffi``).  There is no CPU path: every op
 requires CUDA tensors and the built library.
 """
+import collections
 import numbers
 import threading
+
+import numpy as np
 
 import torch
 
@@ -74,6 +77,32 @@ def _check_tensor(name, t, dtype, ndims, device=None, last=None):
 # ---------------------------------------------------------------------------
 # Context
 # ---------------------------------------------------------------------------
+
+_CONSTANTS = collections.OrderedDict()  # (device, dtype, shape, bytes) -> device tensor
+_CONSTANTS_MAX = 256
+
+
+def _device_constant(values, dtype, device):
+    """A small host array (call ranges, attribute indices, lookup tables) as
+    a device tensor, copied once and kept for later calls with the same
+    values: repeated calls copy nothing from the host, so they neither wait
+    for the GPU nor break CUDA-graph capture.  The returned tensor is shared
+    and must not be modified."""
+    a = np.ascontiguousarray(values)
+    dev = torch.device(device)
+    if dev.type == "cuda" and dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    key = (str(dev), str(dtype), a.shape, a.dtype.str, a.tobytes())
+    hit = _CONSTANTS.get(key)
+    if hit is not None:
+        _CONSTANTS.move_to_end(key)
+        return hit
+    t = torch.from_numpy(a.copy()).to(device=dev, dtype=dtype)
+    _CONSTANTS[key] = t
+    if len(_CONSTANTS) > _CONSTANTS_MAX:
+        _CONSTANTS.popitem(last=False)
+    return t
+
 class RasterizeCudaContext:
     """Per-device rasterisation state: the scratch workspace and its sizing.
 
@@ -285,7 +314,7 @@ def _raster_setup(glctx, pos, tri, resolution, ranges):
                 raise ValueError("ranges out of bounds for %d triangles" % F)
             B = r.shape[0]
             max_view_tris = int(r[:, 1].max()) if B else 0
-            ranges_dev = ranges.to(pos.device, non_blocking=False)
+            ranges_dev = _device_constant(r, torch.int32, pos.device)
     return pos.contiguous(), tri.contiguous(), H, W, B, stride, ranges_dev, max_view_tris
 
 
@@ -387,7 +416,7 @@ def _diff_indices(diff_attrs, C, device):
                 raise ValueError("diff_attrs index %d out of range for %d attributes" % (i, C))
     if not idx:
         return None
-    return torch.tensor(idx, dtype=torch.int32, device=device)
+    return _device_constant(np.asarray(idx, np.int32), torch.int32, device)
 
 
 class _InterpolateFn(torch.autograd.Function):

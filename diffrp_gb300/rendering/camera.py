@@ -17,6 +17,22 @@ def _translation(t):
     return m
 
 
+def _device_matrix(cam, name, m):
+    """The GPU copy of a camera matrix, kept on the camera while its value
+    stays the same: a render step then copies nothing from the host once the
+    camera has been used (which also lets the step be captured in a CUDA
+    graph).  The returned tensor is shared; do not modify it in place."""
+    m = numpy.ascontiguousarray(m, dtype=numpy.float32)
+    cache = cam.__dict__.setdefault("_matrix_cache", {})
+    hit = cache.get(name)
+    dev = torch.cuda.current_device()
+    if hit is not None and hit[0] == dev and numpy.array_equal(hit[1], m):
+        return hit[2]
+    t = gpu_f32(m)
+    cache[name] = (dev, m, t)
+    return t
+
+
 class Camera:
     """Abstract camera: ``V()`` (GL view, inverse pose), ``P()`` (GL
     projection) and ``resolution()`` (h, w).  The default pose sits at
@@ -26,7 +42,7 @@ class Camera:
         self.t = _translation([0.0, 0.0, 3.2])
 
     def V(self):
-        return gpu_f32(numpy.linalg.inv(self.t).astype(numpy.float32))
+        return _device_matrix(self, "V", numpy.linalg.inv(numpy.asarray(self.t)).astype(numpy.float32))
 
     def P(self):
         raise NotImplementedError
@@ -59,7 +75,7 @@ class PerspectiveCamera(Camera):
         self.fov, self.h, self.w, self.near, self.far = fov, h, w, near, far
 
     def P(self):
-        return gpu_f32(synthetic.perspective(self.fov, self.h, self.w, self.near, self.far))
+        return _device_matrix(self, "P", synthetic.perspective(self.fov, self.h, self.w, self.near, self.far))
 
     def resolution(self):
         return self.h, self.w

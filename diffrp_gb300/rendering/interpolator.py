@@ -98,11 +98,31 @@ class MaskedSparseInterpolator(Interpolator):
     """Interpolates only the pixels selected by ``mask`` (one material's
     stencil); results are (N, C) rows in ``mask.nonzero`` order."""
 
-    def __init__(self, vi_data, tris, mask):
+    def __init__(self, vi_data, tris, mask, indices=None):
         self.tris = tris
-        self.indices = mask.nonzero(as_tuple=True)
+        # indices: the mask's nonzero index tuple when the caller already has it
+        self.indices = mask.nonzero(as_tuple=True) if indices is None else indices
         self.vi_data = vi_data[self.indices]
         self.tri_idx = tris[float_to_triidx(self.vi_data[..., -1]) - 1].long()
 
     def interpolate(self, vertex_buffer):
         return polyfill_interpolate(vertex_buffer, self.vi_data, self.tri_idx)
+
+
+def stencil_groups(stencil, n_objects):
+    """For each object id k = 1..n_objects, the index tuple of
+    ``(stencil == k).nonzero(as_tuple=True)`` (row-major order), computed for
+    all objects at once: one stable sort of the pixels by stencil value and
+    one read-back of the per-value counts, instead of one nonzero (each a
+    host wait) per object."""
+    if n_objects <= 2:
+        return [(stencil == k + 1).nonzero(as_tuple=True) for k in range(n_objects)]
+    flat = stencil.reshape(-1).long()
+    order = torch.sort(flat, stable=True).indices
+    counts = torch.bincount(flat, minlength=n_objects + 1)[:n_objects + 1].cpu().tolist()
+    groups, off = [], counts[0]
+    for k in range(n_objects):
+        idx = order[off:off + counts[k + 1]]
+        off += counts[k + 1]
+        groups.append(torch.unravel_index(idx, stencil.shape))
+    return groups

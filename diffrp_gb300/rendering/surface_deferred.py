@@ -13,6 +13,7 @@ import warnings
 from dataclasses import dataclass
 from typing import Callable, List, Optional, Tuple, Union
 
+import numpy
 import torch
 
 from .. import nvdr as dr
@@ -20,10 +21,10 @@ from ..transform import clip_space
 from ..materials.base_material import SurfaceInput, SurfaceOutputStandard, SurfaceUniform
 from ..utils.cache import cached
 from ..utils.composite import alpha_additive, alpha_blend
-from ..utils.shader_ops import (float3, float4, floatx, gpu_f32, length, normalized, ones_like_vec,
+from ..utils.shader_ops import (float3, float4, floatx, length, normalized, ones_like_vec,
                                 transform_point4x3, transform_vector3x3)
 from .camera import Camera
-from .interpolator import FullScreenInterpolator, MaskedSparseInterpolator, float_to_triidx
+from .interpolator import FullScreenInterpolator, MaskedSparseInterpolator, float_to_triidx, stencil_groups
 from .mixin import RenderSessionMixin
 
 __all__ = ["SurfaceDeferredRenderSession", "SurfaceDeferredRenderSessionOptions"]
@@ -64,6 +65,16 @@ class SurfaceDeferredRenderSessionOptions:
     def intepolator_impl(self, value):
         warnings.warn("`intepolator_impl` is deprecated, please use `interpolator_impl` instead.")
         self.interpolator_impl = value
+
+
+def _constant(values, dtype):
+    """A list of numbers (or a tensor) as a device tensor on the current
+    device; lists are copied from the host once and reused by later calls
+    with the same values (no host wait, CUDA-graph capturable)."""
+    if isinstance(values, torch.Tensor):
+        return values.to(device=torch.device("cuda", torch.cuda.current_device()), dtype=dtype)
+    return dr._device_constant(numpy.asarray(values, dtype=numpy.float64 if dtype.is_floating_point else numpy.int64),
+                               dtype, "cuda")
 
 
 def _thread_context():
@@ -132,12 +143,13 @@ class SurfaceDeferredRenderSession(RenderSessionMixin):
             mats = []
             if impl == "stencil_masked":
                 stencil = vao.stencils[float_to_triidx(rast[..., -1])]
+                groups = stencil_groups(stencil, len(self.scene.objects))
             for pi, obj in enumerate(self.scene.objects):
                 su = SurfaceUniform(obj.M, cam_v, cam_p)
                 if impl == "full_screen":
                     si = SurfaceInput(su, vao, FullScreenInterpolator(rast, vao.tris))
                 elif impl == "stencil_masked":
-                    si = SurfaceInput(su, vao, MaskedSparseInterpolator(rast, vao.tris, stencil == pi + 1))
+                    si = SurfaceInput(su, vao, MaskedSparseInterpolator(rast, vao.tris, None, indices=groups[pi]))
                     if len(si.interpolator.indices[0]) == 0:
                         mats.append((si, SurfaceOutputStandard()))
                         continue
@@ -158,14 +170,14 @@ class SurfaceDeferredRenderSession(RenderSessionMixin):
             if all(d == default[0] for d in default):
                 base = torch.full([1, h, w, C], float(default[0]), dtype=torch.float32, device="cuda")
             else:
-                base = gpu_f32(default).expand(1, h, w, C)
+                base = _constant(default, torch.float32).expand(1, h, w, C)
             return [self._gbuffer_collect_layer_impl_stencil_masked(mats, operator, base)
                     for mats in self.layer_material()]
         if self.options.interpolator_impl != "full_screen":
             raise ValueError("Unrecognized `interpolator_impl` '%s'" % self.options.interpolator_impl)
         result = []
         for rast, mats in zip(self.rasterize(), self.layer_material()):
-            buffers = [gpu_f32(default).expand(1, h, w, C)]
+            buffers = [_constant(default, torch.float32).expand(1, h, w, C)]
             lookup = [0]
             for si, so in mats:
                 val = operator(si, so)
@@ -174,7 +186,7 @@ class SurfaceDeferredRenderSession(RenderSessionMixin):
                 else:
                     lookup.append(len(buffers))
                     buffers.append(val)
-            lookup = vao.stencils.new_tensor(lookup)
+            lookup = _constant(lookup, vao.stencils.dtype)
             which = lookup[vao.stencils][float_to_triidx(rast[..., 3:4])]
             result.append(torch.gather(torch.cat(buffers), 0, which.repeat_interleave(C, dim=-1).long()))
         return result

@@ -48,6 +48,8 @@ extern "C" {
 /* Device error bits in the rasterisation workspace's stats block. */
 #define DRP_DEVERR_BAD_INDEX 1u
 #define DRP_DEVERR_LIST_OVERFLOW 2u
+/* drp_batch_forward_l1_grad: an item has more than 32 channels (its gradient was not formed). */
+#define DRP_DEVERR_CHANNELS 4u
 
 int drp_abi_version(void);
 const char* drp_status_string(int status);
@@ -385,6 +387,30 @@ int drp_batch_forward_l1(void* workspace, size_t workspace_bytes, const drp_batc
                          unsigned long long list_capacity, unsigned bin_depth, float* rast, float* color, float* out,
                          void* aa_state, long long total_pixels, const float* target, float scale, float* grad,
                          float* block_loss, float* loss, void* stream);
+
+/*
+ * drp_batch_forward_l1 that also forms the gradient of the loss in the same
+ * pass: grad_pos (pos layout) and grad_attr (attr layout), both accumulated
+ * (caller zeroes), receive d loss / d pos and d loss / d attr -- the
+ * gradients drp_batch_backward gives for grad_out = sign(out - target) *
+ * scale.  The pixels no blending pair touches get their backward inside the
+ * antialias + loss kernel (their rast row and signs at hand, no gradient
+ * image written); the listed ones in a second kernel that forms the sign from
+ * out and target, forked onto the side stream drp_batch_backward uses, beside
+ * the final loss sum.  out and aa_state are required; no sign-gradient image
+ * is written.  At most 32 channels per item (an item with more sets
+ * DRP_DEVERR_CHANNELS in the stats block and gets no gradient).  A caller
+ * whose loss is the only consumer of the images can then skip the backward
+ * pass entirely: multiply the two gradients by the loss's upstream gradient.
+ * No counterpart in the reference.
+ */
+int drp_batch_forward_l1_grad(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
+                              const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
+                              long long pixel_blocks, long long total_prims, long long total_tiles, const float* pos,
+                              const int* tri, const float* attr, const int* nbr, int tile_log2, int threads_per_tri,
+                              unsigned long long list_capacity, unsigned bin_depth, float* rast, float* color,
+                              float* out, void* aa_state, long long total_pixels, const float* target, float scale,
+                              float* block_loss, float* loss, float* grad_pos, float* grad_attr, void* stream);
 
 /* drp_batch_backward flag: the workspace still holds the antialias triangle
  * records of the last drp_batch_forward, which ran on the same positions

@@ -4,6 +4,7 @@ stored in the golden vectors; cache / swizzle / options semantics."""
 import os
 
 import numpy as np
+import pytest
 import torch
 
 from diffrp_gb300 import synthetic as S
@@ -148,3 +149,38 @@ def test_batch_bin_depth_choice_host_logic():
     assert r._choose_depth(5000, 1000) == 0
     r.bin_depth_mode = 7  # a caller-fixed depth wins
     assert r._choose_depth(5000, 1000) == 7
+
+
+@pytest.mark.parametrize("n_objects", [1, 2, 5, 9])
+def test_stencil_groups_match_per_object_nonzero(n_objects):
+    """The per-layer grouping of pixels by stencil (one sort, one count
+    read-back) gives each object exactly mask.nonzero's index tuple."""
+    import torch
+    from diffrp_gb300.rendering.interpolator import stencil_groups
+    g = torch.Generator().manual_seed(n_objects)
+    st = torch.randint(0, n_objects + 2, (1, 41, 67), generator=g, dtype=torch.int32)
+    st[st == 3] = 0  # an object with no pixels
+    groups = stencil_groups(st, n_objects)
+    assert len(groups) == n_objects
+    for k in range(n_objects):
+        ref = (st == k + 1).nonzero(as_tuple=True)
+        assert len(groups[k]) == 3
+        for a, b in zip(groups[k], ref):
+            assert a.dtype == b.dtype and torch.equal(a, b)
+
+
+def test_masked_sparse_interpolator_from_mask_and_from_indices():
+    """The stencil-masked interpolator built from a mask and from the
+    precomputed index tuple holds the same pixels, rows and triangles."""
+    from diffrp_gb300.rendering.interpolator import MaskedSparseInterpolator, stencil_groups
+    g = torch.Generator().manual_seed(3)
+    rast = torch.rand(1, 9, 11, 4, generator=g)
+    ids = torch.randint(0, 5, (1, 9, 11), generator=g)
+    rast[..., 3] = ids.float()
+    tris = torch.arange(12, dtype=torch.int32).reshape(4, 3)
+    stencil = (ids > 2).int() * 2 + (ids > 0).int()
+    a = MaskedSparseInterpolator(rast, tris, stencil == 1)
+    b = MaskedSparseInterpolator(rast, tris, None, indices=stencil_groups(stencil, 3)[0])
+    for x, y in zip(a.indices, b.indices):
+        assert torch.equal(x, y)
+    assert torch.equal(a.vi_data, b.vi_data) and torch.equal(a.tri_idx, b.tri_idx)

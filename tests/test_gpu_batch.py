@@ -36,12 +36,19 @@ def _scene(items=SMALL_ITEMS):
     return meshes_np, chans, attrs, items, views
 
 
+# recompute modes: stored buffers, recompute in one chunk, recompute in
+# chunks of at most 3000 pixels (one or two items each)
+RECOMPUTE = [False, True, "chunked"]
+
+
 def _renderer(recompute=False, tile_log2=4, tpt=0, items=SMALL_ITEMS, bin_depth=None):
     from diffrp_gb300.batch import BatchRenderer
     meshes_np, chans, attrs, items, views = _scene(items)
     meshes = [(torch.from_numpy(f).cuda(), len(v), c) for (v, f), c in zip(meshes_np, chans)]
-    r = BatchRenderer(meshes, items, tile_log2=tile_log2, threads_per_tri=tpt, recompute=recompute,
-                      bin_depth=bin_depth)
+    r = BatchRenderer(meshes, items, tile_log2=tile_log2, threads_per_tri=tpt, recompute=bool(recompute),
+                      bin_depth=bin_depth, chunk_pixels=3000 if recompute == "chunked" else 1 << 23)
+    if recompute == "chunked":
+        assert len(r._chunks) >= 3
     pos = r.pack_positions([torch.from_numpy(p).cuda() for p in views])
     attr = r.pack_attributes([torch.from_numpy(a).cuda() for a in attrs])
     return r, pos, attr, (meshes_np, chans, attrs, items, views)
@@ -68,7 +75,7 @@ def test_batch_forward_matches_per_item_calls(cuda_lib, tile_log2, tpt, items):
         assert torch.equal(ov[k], oo[0]), "antialiased image differs for item %d" % k
 
 
-@pytest.mark.parametrize("recompute", [False, True])
+@pytest.mark.parametrize("recompute", RECOMPUTE)
 def test_batch_gradients_match_per_item_autograd(cuda_lib, recompute):
     from diffrp_gb300 import nvdr as dr
     r, pos, attr, (meshes_np, chans, attrs, items, views) = _renderer(recompute=recompute)
@@ -136,7 +143,7 @@ def test_batch_fixed_depth_bins_exact(cuda_lib, depth):
         assert r._depth > 2
 
 
-@pytest.mark.parametrize("recompute", [False, True])
+@pytest.mark.parametrize("recompute", RECOMPUTE)
 @pytest.mark.parametrize("use_images", [False, True])
 def test_batch_render_l1_matches_unfused(cuda_lib, recompute, use_images):
     """render_l1 gives the images of the plain forward bit for bit, the loss
@@ -247,3 +254,113 @@ def test_backward_on_a_side_stream_matches_default_stream(cuda_lib):
     for got in (side, out["g"]):
         for x, y in zip(got, ref):
             assert torch.allclose(x, y, rtol=1e-5, atol=1e-7)
+
+
+def test_batch_recompute_chunks_match_stored(cuda_lib):
+    """Recompute in chunks (each chunk's forward re-run in the backward) gives
+    the stored-buffer path's images bit for bit and its gradients to 1e-5,
+    eagerly and replayed from a CUDA graph, with the fused L1 loss."""
+    r0, pos, attr, _ = _renderer(recompute=False)
+    r1, _, _, _ = _renderer(recompute="chunked")
+    g = torch.Generator(device="cuda").manual_seed(7)
+    target = torch.rand(r0.image_floats, device="cuda", generator=g)
+
+    def run(r):
+        p = pos.clone().requires_grad_(True)
+        a = attr.clone().requires_grad_(True)
+
+        def step():
+            p.grad = None
+            a.grad = None
+            loss, img = r.render_l1(p, a, target)
+            loss.backward()
+            return loss, img
+        loss, img = step()
+        return step, p, a, loss.detach().clone(), img.detach().clone(), p.grad.clone(), a.grad.clone()
+
+    _, _, _, l0, im0, gp0, ga0 = run(r0)
+    step, p1, a1, l1, im1, gp1, ga1 = run(r1)
+    assert torch.equal(im0, im1)
+    assert torch.allclose(l0, l1, rtol=2e-6, atol=0)
+    for got, ref in [(gp1, gp0), (ga1, ga0)]:
+        assert float((got - ref).abs().max() / ref.abs().max()) <= 1e-5
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(2):
+            step()
+    torch.cuda.current_stream().wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        gl, gimg = step()
+    p1.grad.zero_()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(gimg, im1)
+    for got, ref in [(p1.grad, gp0), (a1.grad, ga0)]:
+        assert float((got - ref).abs().max() / ref.abs().max()) <= 1e-5
+
+
+@pytest.mark.parametrize("recompute", RECOMPUTE)
+@pytest.mark.parametrize("use_images", [False, True])
+def test_batch_render_l1_grads_in_forward(cuda_lib, recompute, use_images):
+    """render_l1 with the loss's gradient formed in the forward pass gives
+    the images bit for bit, the same loss and the gradients of the ordinary
+    backward (to 1e-5), with a non-unit upstream loss gradient; when the
+    images reach the objective too, the full backward runs instead."""
+    r, pos, attr, _ = _renderer(recompute=recompute)
+    g = torch.Generator(device="cuda").manual_seed(11)
+    target = torch.rand(r.image_floats, device="cuda", generator=g)
+    w = torch.linspace(-1, 1, r.image_floats, device="cuda")
+
+    def run(eager):
+        p = pos.clone().requires_grad_(True)
+        a = attr.clone().requires_grad_(True)
+        loss, img = r.render_l1(p, a, target, grads_in_forward=eager)
+        total = 3.0 * loss + ((img * w).sum() if use_images else 0.0)
+        total.backward()
+        return loss.detach(), img.detach(), p.grad, a.grad
+
+    le, ime, gpe, gae = run(True)
+    lr, imr, gpr, gar = run(False)
+    assert torch.equal(ime, imr)
+    assert torch.allclose(le, lr, rtol=2e-6, atol=0)
+    for got, ref in [(gpe, gpr), (gae, gar)]:
+        assert float((got - ref).abs().max() / ref.abs().max()) <= 1e-5
+
+
+def test_batch_render_l1_grads_in_forward_graph_replay(cuda_lib):
+    """The forward that forms the gradient, captured with its backward in a
+    CUDA graph and replayed, matches an eager step.  (Every step before the
+    capture runs on a side stream: a leaf first differentiated on the legacy
+    default stream keeps that stream for its gradient accumulation, which
+    a capture cannot wait on.)"""
+    r, pos, attr, _ = _renderer()
+    g = torch.Generator(device="cuda").manual_seed(12)
+    target = torch.rand(r.image_floats, device="cuda", generator=g)
+    p = pos.clone().requires_grad_(True)
+    a = attr.clone().requires_grad_(True)
+
+    def step():
+        p.grad = None
+        a.grad = None
+        loss, img = r.render_l1(p, a, target, grads_in_forward=True)
+        loss.backward()
+        return loss, img
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        l0, im0 = step()
+        ref = (l0.detach().clone(), im0.detach().clone(), p.grad.clone(), a.grad.clone())
+        for _ in range(2):
+            step()
+    torch.cuda.current_stream().wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        gl, gimg = step()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(gimg, ref[1])
+    assert torch.allclose(gl, ref[0], rtol=0, atol=0)
+    for got, want in [(p.grad, ref[2]), (a.grad, ref[3])]:
+        assert float((got - want).abs().max() / want.abs().max()) <= 1e-6

@@ -60,9 +60,12 @@ def _gate(got, fd_vals, what, per_vertex=False):
     return err
 
 
-def test_benchmark_step_gradients_match_finite_differences(cuda_lib):
-    """Clip transform kernel + batching form with the fused L1: world-space
-    vertex and attribute gradients against central differences."""
+@pytest.mark.parametrize("grads_in_forward", [False, True], ids=["backward_pass", "grads_in_forward"])
+def test_benchmark_step_gradients_match_finite_differences(cuda_lib, grads_in_forward):
+    """Clip transform kernel + batching form with the fused L1 (gradient
+    from the backward pass, or formed in the forward pass as the benchmark
+    step does): world-space vertex and attribute gradients against central
+    differences."""
     from diffrp_gb300.batch import BatchRenderer
     from diffrp_gb300.transform import clip_space
     v, f, attr, mvp, target = _workload()
@@ -73,7 +76,8 @@ def test_benchmark_step_gradients_match_finite_differences(cuda_lib):
     clip_t = clip_space(verts_t, torch.from_numpy(mvp).to(dev))
     r = BatchRenderer([(torch.from_numpy(f).to(dev), len(v), C)], [(0, (H, W))], device=dev, tile_log2=5)
     rast, _, _ = r.forward_buffers(clip_t.detach(), attr_t.detach())
-    loss, out = r.render_l1(clip_t, attr_t, torch.from_numpy(target).to(dev).reshape(-1))
+    loss, out = r.render_l1(clip_t, attr_t, torch.from_numpy(target).to(dev).reshape(-1),
+                            grads_in_forward=grads_in_forward)
     loss.backward()
     torch.cuda.synchronize()
     clip = clip_t.detach().cpu().numpy()
