@@ -603,60 +603,23 @@ __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
     }
 }
 
-// Antialias + L1 loss with the loss's gradient formed in the same pass
-// (drp_batch_forward_l1_grad).  Every pixel: its output and |error| partial
-// as batch_aa_l1_kernel computes them.  Then, for the pixels no blending pair
-// touches (the listed ones belong to batch_aa_bwd_kernel<true>, which forms
-// the sign from the output and the target), the pixel's whole backward with
-// the upstream gradient sign(out - target) * scale: interpolation backward
-// (attribute gradients) and rasterisation backward (vertex gradients),
-// reduced over runs of one triangle in the warp and scattered with float4
-// atomics -- the work batch_bwd_kernel does for those pixels, done while
-// the pixel's rast row and signs are at hand, with no gradient image written
-// or read back.  The signs pass between the two phases as two bit masks, so
-// an item may have at most 32 channels (more: DRP_DEVERR_CHANNELS, and the
-// item gets no gradient here).  Warps never straddle items (256-pixel blocks).
-__global__ void __launch_bounds__(256, 4) batch_aa_l1_grad_kernel(BatchArgs a) {
-    __shared__ float warp_sum[8];
-    const int2 blk = a.pix_blocks[blockIdx.x];
-    const drp_batch_item& it = a.items[blk.x];
-    const int pix = blk.y * 256 + threadIdx.x;
+// The backward of one pixel no blending pair touches, with the upstream
+// gradient sign(out - target) * scale given by the sign masks (bit c:
+// nonzero / positive): interpolation backward (attribute gradients) and
+// rasterisation backward (vertex gradients), reduced over runs of one
+// triangle in the warp and scattered with float4 atomics.  All 32 lanes call
+// it (active = false for the others); a warp without an active lane on a
+// triangle returns at once.
+// r, t, i0..i2: the pixel's rast row, triangle (-1: none, or not active)
+// and vertex indices, loaded by the caller before its antialias work.
+__device__ __forceinline__ void pixel_backward_l1(const BatchArgs& a, const drp_batch_item& it, int pix, float4 r,
+                                                  int t, int i0, int i1, int i2, unsigned nz, unsigned ps) {
     const int W = it.width, H = it.height, C = it.channels;
-    const bool in = pix < W * H;
-    const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
-    float s = 0.0f;
-    unsigned bits = 0u, nz = 0u, ps = 0u;
-    if (in) {
-        const long long row = it.image_offset + (long long)pix * C;
-        s = aa_fwd_pixel_l1(R, a.color + it.image_offset, a.aa_rec + it.prim_offset * 2, it.tri_count, W, H, C, pix,
-                            a.target + row, a.l1_scale, a.out + row, nullptr, &bits, &nz, &ps);
-    }
-    aa_note_pixel(a, it.pixel_offset + pix, in, bits);
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-    if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float t = 0.0f;
-#pragma unroll
-        for (int w = 0; w < 8; ++w) t += warp_sum[w];
-        a.block_loss[blockIdx.x] = t;
-    }
-    if (C > 32) {
-        if (threadIdx.x == 0) atomicOr(a.stats + 2, DRP_DEVERR_CHANNELS);
-        return;
-    }
-    const int* tri = a.tri + 3 * (long long)it.tri_first;
     const float* A = a.attr + it.attr_offset;
     float* GA = a.grad_attr + it.attr_offset;
     const float4* P = reinterpret_cast<const float4*>(a.pos) + it.pos_offset;
     float4* GP = reinterpret_cast<float4*>(a.grad_pos) + it.pos_offset;
-    int t = -1, i0 = 0, i1 = 0, i2 = 0;
-    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (in && bits == 0u) {
-        r = R[pix];
-        t = checked_tri(r.w, tri, it.tri_count, it.num_vertices, i0, i1, i2);
-    }
+    if (!__any_sync(0xffffffffu, t >= 0)) return;  // background or listed pixels only: nothing to add
     const Seg seg = seg_setup(t >= 0 ? (long long)t : (long long)(-1 - lane_id()));
     const float u = r.x, v = r.y, w = 1.0f - u - v;
     const float sc = a.l1_scale;
@@ -737,6 +700,59 @@ __global__ void __launch_bounds__(256, 4) batch_aa_l1_grad_kernel(BatchArgs a) {
         atomic_add4(GP + i0, make_float4(pv[0], pv[1], 0.f, pv[2]));
         atomic_add4(GP + i1, make_float4(pv[3], pv[4], 0.f, pv[5]));
         atomic_add4(GP + i2, make_float4(pv[6], pv[7], 0.f, pv[8]));
+    }
+}
+
+// Antialias + L1 loss with the loss's gradient formed in the same pass
+// (drp_batch_forward_l1_grad).  Every pixel: its output and |error| partial
+// as batch_aa_l1_kernel computes them.  Then, for the pixels no blending pair
+// touches (the listed ones belong to batch_aa_bwd_kernel<true>, which forms
+// the sign from the output and the target), the pixel's whole backward with
+// the upstream gradient sign(out - target) * scale: interpolation backward
+// (attribute gradients) and rasterisation backward (vertex gradients),
+// reduced over runs of one triangle in the warp and scattered with float4
+// atomics -- the work batch_bwd_kernel does for those pixels, done while
+// the pixel's rast row and signs are at hand, with no gradient image written
+// or read back.  The signs pass between the two phases as two bit masks, so
+// an item may have at most 32 channels (more: DRP_DEVERR_CHANNELS, and the
+// item gets no gradient here).  Warps never straddle items (256-pixel blocks).
+__global__ void __launch_bounds__(256, 4) batch_aa_l1_grad_kernel(BatchArgs a) {
+    __shared__ float warp_sum[8];
+    const int2 blk = a.pix_blocks[blockIdx.x];
+    const drp_batch_item& it = a.items[blk.x];
+    const int pix = blk.y * 256 + threadIdx.x;
+    const int W = it.width, H = it.height, C = it.channels;
+    const bool in = pix < W * H;
+    const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
+    // the backward's rast row and vertex indices, loaded first so that their
+    // latency overlaps the antialias work
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    int t = -1, i0 = 0, i1 = 0, i2 = 0;
+    if (in) {
+        r = R[pix];
+        t = checked_tri(r.w, a.tri + 3 * (long long)it.tri_first, it.tri_count, it.num_vertices, i0, i1, i2);
+    }
+    float s = 0.0f;
+    unsigned bits = 0u, nz = 0u, ps = 0u;
+    if (in) {
+        const long long row = it.image_offset + (long long)pix * C;
+        s = aa_fwd_pixel_l1(R, a.color + it.image_offset, a.aa_rec + it.prim_offset * 2, it.tri_count, W, H, C, pix,
+                            a.target + row, a.l1_scale, a.out + row, nullptr, &bits, &nz, &ps);
+    }
+    aa_note_pixel(a, it.pixel_offset + pix, in, bits);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = s;
+    // the block's loss partial is added at the end: a barrier here would hold
+    // every warp's backward until the slowest antialias pixel of the block
+    pixel_backward_l1(a, it, pix, r, (bits == 0u && C <= 32) ? t : -1, i0, i1, i2, nz, ps);
+    if (C > 32 && threadIdx.x == 0) atomicOr(a.stats + 2, DRP_DEVERR_CHANNELS);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.0f;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) t += warp_sum[w];
+        a.block_loss[blockIdx.x] = t;
     }
 }
 

@@ -376,21 +376,30 @@ struct FineTile {
     uint32_t* stats;            // device error bits or null
 };
 
-// Fine raster of one tile by one CTA, then emit(px, py, local index, key,
-// ndc x, ndc y) for every pixel of the tile inside the viewport.
-//   TPT == 0: every thread owns T*T/NTHREADS pixels (8x4 blocks per warp)
-//             and tests them against each primitive of the tile (keys in
-//             registers, no atomics);
+// Fine raster of one tile by one CTA, then emit(px, py, key, ndc x, ndc y)
+// for every pixel of the tile inside the viewport.
+//   TPT == 0: pixel-parallel.  The tile's 8x4 pixel blocks are handed to the
+//             warps one at a time from a shared counter; a warp tests its
+//             block's 32 pixels (one per lane, keys in registers) against
+//             every primitive whose bounding box meets the block, nearer
+//             facing class first, then the other class with the blocks'
+//             depth bound, and emits the block at once when the keys are
+//             final.  A warp that drew light blocks takes more of them, so
+//             the warps of a CTA reach the tile's barriers together (fixed
+//             16x8 regions per warp left half of them waiting at the
+//             barriers for the busiest one).  Keys go through shared memory
+//             only when a tile needs more than one chunk of primitives or
+//             has clipped (complex) primitives.
 //   TPT  > 0: groups of TPT threads walk one primitive's bbox within the tile
 //             and resolve keys with shared-memory atomicMin.
-//   PEEL = false: ft.prev is ignored (no previous layer); the compiler then
-//             keeps no per-pixel previous-layer keys in registers.
+//   PEEL = false: ft.prev is ignored (no previous layer).
 template <int TILE_LOG2, int TPT, bool PEEL, class Emit>
 __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
     constexpr int T = 1 << TILE_LOG2;
     constexpr int NPIX = T * T;
     constexpr int NTHREADS = NPIX < 256 ? NPIX : 256;
     constexpr int PPT = NPIX / NTHREADS;
+    constexpr int NBLK = NPIX / 32;  // 8x4 blocks
     constexpr int CHUNK = NTHREADS;  // primitives prepared per pass: one per thread
     constexpr int GROUPS = TPT > 0 ? NTHREADS / TPT : 1;
     __shared__ unsigned long long keys[NPIX];
@@ -398,22 +407,21 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
     __shared__ uint32_t pmask[CHUNK];  // 8x4 blocks each prepared primitive's bbox overlaps
     __shared__ uint32_t pzlo[CHUNK];   // depth_order of a lower bound of the primitive's fragment depths
     __shared__ int n_complex;
+    __shared__ int blk_next;           // next 8x4 block a warp takes (TPT == 0)
     __shared__ float col_ndc[T], row_ndc[T];
 
     const int tx0 = ft.tx0, ty0 = ft.ty0, W = ft.W, H = ft.H;
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
     const unsigned long long* prev_g = PEEL ? ft.prev : nullptr;
 
-    unsigned long long best[PPT], prevk[PPT];
+    if (TPT > 0) {
 #pragma unroll
-    for (int q = 0; q < PPT; ++q) {
-        int dx, dy, bx, by;
-        tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
-        const int px = tx0 + dx, py = ty0 + dy;
-        best[q] = ~0ull;
-        prevk[q] = 0;
-        if (prev_g) prevk[q] = (px < W && py < H) ? prev_g[py * W + px] : ~0ull;
-        if (TPT > 0) keys[(dy << TILE_LOG2) + dx] = ~0ull;
+        for (int q = 0; q < PPT; ++q) {
+            int dx, dy, bx, by;
+            tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+            keys[(dy << TILE_LOG2) + dx] = ~0ull;
+        }
     }
     if (tid == 0) n_complex = 0;
     if (tid < T) col_ndc[tid] = pixel_ndc(tx0 + tid, W);
@@ -426,8 +434,21 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
     if (overflow && tid == 0 && ft.stats) atomicOr(ft.stats + 2, DRP_DEVERR_LIST_OVERFLOW);
     __syncthreads();
 
+    if (TPT == 0 && total == 0) {
+        // no primitive meets the tile: every pixel is background
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            int dx, dy, bx, by;
+            tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
+            const int px = tx0 + dx, py = ty0 + dy;
+            if (px < W && py < H) emit(px, py, ~0ull, col_ndc[dx], row_ndc[dy]);
+        }
+        return;
+    }
+
     for (long long base = 0; base < total; base += CHUNK) {
         const int n = (int)min((long long)CHUNK, total - base);
+        const bool last_chunk = base + CHUNK >= total;
         if (tid < n && tid < CHUNK) {
             const long long pidx = overflow ? pbase + base + tid : (long long)ft.list[base + tid];
             TilePrim& tp = prims[tid];
@@ -439,18 +460,11 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
                                           : 0u;
             if (TPT == 0 && (fl & TP_ACTIVE)) pzlo[tid] = depth_order(prim_depth_lower_bound(tp));
         }
+        if (tid == 0) blk_next = 0;
         __syncthreads();
         if (TPT == 0) {
-            // Each warp ballots the primitives whose block mask meets its own
-            // blocks, then walks only those (warp-uniform loop).  The facing
-            // class holding the nearest primitive goes first; the other class
-            // is then skipped per 8x4 block wherever its depth lower bound lies
-            // behind every key the block already holds (such a primitive
-            // cannot win any of the block's pixels, so the result is exact).
-            const int lane = tid & 31;
-            uint32_t wbits = 0;
-#pragma unroll
-            for (int q = 0; q < PPT; ++q) wbits |= 1u << tile_block<TILE_LOG2, NTHREADS>(tid, q);
+            // Facing class holding the nearest primitive (every warp computes
+            // the same answer).
             uint32_t zmin0 = 0xffffffffu, zmin1 = 0xffffffffu;
             for (int j = lane; j < n; j += 32) {
                 const int f = prims[j].e2.y;
@@ -459,38 +473,51 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
                 else zmin0 = min(zmin0, pzlo[j]);
             }
             const int first = __reduce_min_sync(0xffffffffu, zmin0) <= __reduce_min_sync(0xffffffffu, zmin1) ? 0 : 1;
-            for (int pass = 0; pass < 2; ++pass) {
-                const int want = pass == 0 ? first : 1 - first;
-                uint32_t bmax[PPT];
-#pragma unroll
-                for (int q = 0; q < PPT; ++q)
-                    bmax[q] = pass == 0 ? 0xffffffffu : __reduce_max_sync(0xffffffffu, (uint32_t)(best[q] >> 32));
-                for (int j0 = 0; j0 < n; j0 += 32) {
-                    const int j = j0 + lane;
-                    const uint32_t pm =
-                        (j < n && ((prims[j].e2.y & TP_NEG) ? 1 : 0) == want) ? pmask[j] : 0u;
-                    uint32_t hits = __ballot_sync(0xffffffffu, (pm & wbits) != 0u);
-                    while (hits) {
-                        const int b = __ffs(hits) - 1;
-                        hits &= hits - 1;
-                        const uint32_t mj = __shfl_sync(0xffffffffu, pm, b);
-                        const uint32_t zj = pzlo[j0 + b];
-                        const TilePrim& tp = prims[j0 + b];
-                        const int4 e0 = tp.e0, e1 = tp.e1, e2 = tp.e2;
-#pragma unroll
-                        for (int q = 0; q < PPT; ++q) {
-                            if (!((mj >> tile_block<TILE_LOG2, NTHREADS>(tid, q)) & 1u)) continue;  // warp-uniform
-                            if (zj > bmax[q]) continue;  // behind the whole block: warp-uniform
-                            int dx, dy, bx, by;
-                            tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
-                            const int sx = (tx0 + dx) * DRP_SUBPIX + DRP_HALF_SUBPIX;
-                            const int sy = (ty0 + dy) * DRP_SUBPIX + DRP_HALF_SUBPIX;
+            // keys are final at the end of this chunk unless a clipped
+            // primitive still has to be rasterised (second pass below)
+            const bool final_keys = last_chunk && n_complex == 0;
+            for (;;) {
+                int b = 0;
+                if (lane == 0) b = atomicAdd(&blk_next, 1);
+                b = __shfl_sync(0xffffffffu, b, 0);
+                if (b >= NBLK) break;
+                const int dx = (b % (T / 8)) * 8 + (lane & 7);
+                const int dy = (b / (T / 8)) * 4 + (lane >> 3);
+                const int px = tx0 + dx, py = ty0 + dy;
+                const int sx = px * DRP_SUBPIX + DRP_HALF_SUBPIX, sy = py * DRP_SUBPIX + DRP_HALF_SUBPIX;
+                const int li = (dy << TILE_LOG2) + dx;
+                unsigned long long best = base == 0 ? ~0ull : keys[li];
+                unsigned long long pk = 0;
+                if (prev_g) pk = (px < W && py < H) ? prev_g[py * W + px] : ~0ull;
+                const uint32_t bit = 1u << b;
+                for (int pass = 0; pass < 2; ++pass) {
+                    const int want = pass == 0 ? first : 1 - first;
+                    // The other class is skipped wherever its depth lower
+                    // bound lies behind every key the block already holds
+                    // (such a primitive cannot win a pixel: exact).
+                    const uint32_t bmax =
+                        pass == 0 ? 0xffffffffu : __reduce_max_sync(0xffffffffu, (uint32_t)(best >> 32));
+                    for (int j0 = 0; j0 < n; j0 += 32) {
+                        const int j = j0 + lane;
+                        const bool meets = j < n && (pmask[j] & bit) && ((prims[j].e2.y & TP_NEG) ? 1 : 0) == want;
+                        uint32_t hits = __ballot_sync(0xffffffffu, meets);
+                        while (hits) {
+                            const int h = __ffs(hits) - 1;
+                            hits &= hits - 1;
+                            if (pzlo[j0 + h] > bmax) continue;  // warp-uniform
+                            const TilePrim& tp = prims[j0 + h];
+                            const int4 e0 = tp.e0, e1 = tp.e1, e2 = tp.e2;
                             if (!tile_prim_covers(tp, e0, e1, e2, dx, dy, sx, sy)) continue;
                             bool ok;
                             const unsigned long long k = tile_prim_key(tp.z, e2.z, e2.w, sx, sy, ok);
-                            if (ok && k < best[q] && (!prev_g || k > prevk[q])) best[q] = k;
+                            if (ok && k < best && (!prev_g || k > pk)) best = k;
                         }
                     }
+                }
+                if (final_keys) {
+                    if (px < W && py < H) emit(px, py, best, col_ndc[dx], row_ndc[dy]);
+                } else {
+                    keys[li] = best;
                 }
             }
         } else {
@@ -519,27 +546,7 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
         }
         __syncthreads();
     }
-    if (TPT == 0) {
-        if (n_complex == 0) {
-            // Every key is final and in this thread's registers: emit at once.
-#pragma unroll
-            for (int q = 0; q < PPT; ++q) {
-                int dx, dy, bx, by;
-                tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
-                const int px = tx0 + dx, py = ty0 + dy;
-                if (px >= W || py >= H) continue;
-                emit(px, py, best[q], col_ndc[dx], row_ndc[dy]);
-            }
-            return;
-        }
-#pragma unroll
-        for (int q = 0; q < PPT; ++q) {
-            int dx, dy, bx, by;
-            tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
-            keys[(dy << TILE_LOG2) + dx] = best[q];
-        }
-    }
-    __syncthreads();
+    if (TPT == 0 && n_complex == 0) return;  // every block was emitted in the last chunk
     if (n_complex > 0) {
         // Clipped polygons (rare): second pass over the list, group-parallel.
         __shared__ unsigned long long prev_s[NPIX];
@@ -548,7 +555,8 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
             for (int q = 0; q < PPT; ++q) {
                 int dx, dy, bx, by;
                 tile_pixel<TILE_LOG2, NTHREADS>(tid, q, dx, dy, bx, by);
-                prev_s[(dy << TILE_LOG2) + dx] = prevk[q];
+                const int px = tx0 + dx, py = ty0 + dy;
+                prev_s[(dy << TILE_LOG2) + dx] = (px < W && py < H) ? prev_g[py * W + px] : ~0ull;
             }
         }
         __syncthreads();
