@@ -33,8 +33,10 @@ its peak memory beside it).
 ``--impl reference`` times the CPU implementation of the path (the oracle
 port: the reference's own rasteriser is an external CUDA package that does
 not exist on this machine) with all host threads on the same workload.
-``--gpus N`` under torchrun runs N replicas (weak scaling; no collective on
-the data path).
+``--gpus N`` under torchrun runs N replicas of the headline step (weak
+scaling; no collective on the data path) and attaches ``sharded_views64``:
+the 64 views sharded across the ranks with one all-reduce of the shared
+mesh's gradients per step (strong scaling).
 """
 import argparse
 import ctypes
@@ -558,6 +560,46 @@ def run_config1(dev, steps, warmup):
     return res
 
 
+def run_sharded_views64(dev, steps, warmup, rank, world):
+    """The 64-view workload sharded across ranks (strong scaling): each rank
+    renders its share of the views (diffrp_gb300.replicas.shard_items) as one
+    batched CUDA graph and the shared mesh's vertex and attribute gradients
+    are summed with one all-reduce per step.  value = all 64 views' pixels /
+    the slowest rank's step time."""
+    import torch
+    import torch.distributed as dist
+    from diffrp_gb300.replicas import allreduce_gradients, shard_items
+    meshes, items = views64_workload(dev)
+    mine = shard_items([(m, hw) for m, hw, _ in items], rank, world)
+    wl = MultiViewWorkload(dev, meshes, [items[i] for i in mine], tile=(5, 0))
+    g = _graph(wl.batched_step, dev, warm=max(2, warmup))
+    params = wl.verts + wl.attrs
+
+    def step():
+        g.replay()
+        allreduce_gradients(params)
+
+    for _ in range(max(3, warmup)):
+        step()
+    s = torch.cuda.current_stream(dev)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    dist.barrier()
+    torch.cuda.synchronize(dev)
+    for i in range(steps):
+        evs[i][0].record(s)
+        step()
+        evs[i][1].record(s)
+    torch.cuda.synchronize(dev)
+    ms = sum(a.elapsed_time(b) for a, b in evs) / steps
+    t = torch.tensor([ms], device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_px = sum(h * w for _, (h, w), _ in items)
+    return {"value": total_px / float(t[0]) / 1e3, "unit": UNIT, "ms_per_step": float(t[0]), "scaling": "strong",
+            "items_per_rank": len(mine), "pixels_per_step": total_px,
+            "path": "views sharded across ranks, batched CUDA graph per rank, one all-reduce of the shared "
+                    "mesh's gradients per step"}
+
+
 def _clock_sampler():
     f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
     try:
@@ -950,6 +992,11 @@ def main():
     pix = H * W * args.steps * world
     value = pix / (total_ms / 1e3) / 1e6
     e2e_value = pix / (e2e_ms / 1e3) / 1e6
+    # the 64 views sharded across the ranks (every rank takes part in its
+    # all-reduce; before the attached lines, which rank 0 runs alone)
+    sharded = None
+    if world > 1 and not args.no_batched:
+        sharded = run_sharded_views64(dev, max(5, args.steps // 3), W_, rank, world)
     h2d = h_in.numel() * 4
     d2h = h_out.numel() * 4
 
@@ -1031,6 +1078,8 @@ def main():
             line["batched_large16"] = big
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(verts_np, f, attr_np, mvp, target)
+        if sharded is not None:
+            line["sharded_views64"] = sharded
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()

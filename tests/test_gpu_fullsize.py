@@ -8,7 +8,10 @@ the CPU oracle at full size; the position / attribute gradients agree within
 CUDA path (float32 terms, float64 sums), and at the 99.9th percentile with
 the all-float64 backward.
 One view of the 2.09M-triangle heightfield at 2048x2048 (the large
-workload's shape) is compared the same way for the forward.
+workload's shape) is compared the same way for the forward, two views for the
+forward and backward with recompute in chunks; seven items of the 48-mesh
+workload (its meshes, resolutions and channel counts) for the forward and
+the gradients formed in the forward pass.
 """
 import numpy as np
 import pytest
@@ -110,3 +113,106 @@ def test_heightfield_2048_view_forward(cuda_lib):
     # a second forward bins in one pass (fixed-depth bins) and must agree too
     rast2, _, out2 = r.forward_buffers(torch.from_numpy(pos).cuda(), torch.from_numpy(attr).cuda().reshape(-1))
     assert torch.equal(rast2, rast) and torch.equal(out2, out)
+
+
+def _oracle_item_grads(pos, f, attr, target, H, W, scale, nbr):
+    """Forward images and the L1 loss gradients of one item by the oracle
+    (float32 terms, float64 sums): (rast, colour, out, d/dclip (V, 4),
+    d/dattr (V, C))."""
+    rast, _, _ = O.rasterize(pos, f, (H, W), grad_db=False)
+    col, _ = O.interpolate(attr, rast, f)
+    out = O.antialias(col, rast, pos, f, nbr)
+    g_out = (np.sign(out - target.reshape(out.shape)) * np.float32(scale)).astype(np.float32)
+    g_col, g_pos_aa = O.antialias_bwd(col, rast, pos, f, g_out, nbr, precision="f32")
+    g_attr, g_rast, _ = O.interpolate_bwd(attr, rast, f, g_col, precision="f32")
+    g_pos = g_pos_aa + O.raster_bwd(pos, f, rast, g_rast, precision="f32")
+    return rast, col, out, g_pos, g_attr
+
+
+def test_uneven_items_forward_and_gradients(cuda_lib):
+    """Items 0-5 and 7 of the 48-mesh workload (two icospheres of 81920 and
+    20480 triangles with 9 and 16 channels, a displaced grid of 88200
+    triangles with 8; 256 to 1024 pixels square) through one batched forward
+    with the fused L1 loss and its gradient formed in the forward: every
+    item's rast, colour and image bit-identical to the oracle, position and
+    attribute gradients within 1e-4 of the largest."""
+    import bench
+    from diffrp_gb300.batch import BatchRenderer
+    meshes_all, items_all = bench.uneven48_workload(None, seed=0)
+    items_sel = items_all[:6] + items_all[7:8]
+    used = sorted({m for m, _, _ in items_sel})
+    remap = {m: k for k, m in enumerate(used)}
+    meshes = [meshes_all[m] for m in used]
+    rng = np.random.default_rng(21)
+    attrs = [rng.uniform(0, 1, (len(v), c)).astype(np.float32) for v, _, c in meshes]
+    views = [S.clip_positions(meshes[remap[m]][0], mvp) for m, _, mvp in items_sel]
+    r = BatchRenderer([(torch.from_numpy(f).cuda(), len(v), c) for v, f, c in meshes],
+                      [(remap[m], hw) for m, hw, _ in items_sel], tile_log2=3)
+    pos_t = r.pack_positions([torch.from_numpy(p).cuda() for p in views]).requires_grad_(True)
+    attr_t = r.pack_attributes([torch.from_numpy(a).cuda() for a in attrs]).requires_grad_(True)
+    target = rng.uniform(0, 1, r.image_floats).astype(np.float32)
+    rast_b, col_b, _ = r.forward_buffers(pos_t.detach(), attr_t.detach())
+    loss, out = r.render_l1(pos_t, attr_t, torch.from_numpy(target).cuda(), grads_in_forward=True)
+    loss.backward()
+    torch.cuda.synchronize()
+    rv, cv, ov = r.rast_views(rast_b), r.images(col_b), r.images(out.detach())
+    tv = r.images(torch.from_numpy(target))
+    scale = 1.0 / r.image_floats
+    g_pos_ref = np.zeros((r.pos_rows, 4))
+    g_attr_ref = [np.zeros(a.shape) for a in attrs]
+    for k, (m, (H, W), _) in enumerate(items_sel):
+        v, f, c = meshes[remap[m]]
+        nbr = O.topology(f)
+        rast, col, o, gp, ga = _oracle_item_grads(views[k], f, attrs[remap[m]], tv[k].numpy(), H, W, scale, nbr)
+        np.testing.assert_array_equal(rv[k].cpu().numpy(), rast[0])
+        np.testing.assert_array_equal(cv[k].cpu().numpy(), col[0])
+        np.testing.assert_array_equal(ov[k].cpu().numpy(), o[0])
+        g_pos_ref[r.pos_offsets[k]:r.pos_offsets[k] + len(v)] = gp
+        g_attr_ref[remap[m]] += ga
+    _grad_close(pos_t.grad.cpu().numpy(), g_pos_ref)
+    _grad_close(attr_t.grad.cpu().numpy(), np.concatenate([g.reshape(-1) for g in g_attr_ref]))
+
+
+@pytest.mark.parametrize("grads_in_forward", [False, True], ids=["backward_recompute", "grads_in_forward"])
+def test_heightfield_two_views_recompute_gradients(cuda_lib, grads_in_forward):
+    """Two oblique 2048x2048 views of the 2.09M-triangle heightfield (the
+    large workload's shape, 12 channels) with recompute in chunks of one view:
+    images bit-identical to the oracle and gradients within 1e-4 of the
+    largest, with the backward re-rendering each chunk or with the gradient
+    formed in the forward."""
+    from diffrp_gb300.batch import BatchRenderer
+    H = W = 2048
+    v, f = S.heightfield(1024, 0.3, 6, 0)
+    rng = np.random.default_rng(5)
+    C = 12
+    attr = rng.uniform(0, 1, (len(v), C)).astype(np.float32)
+    views = []
+    for az in (0.7, 2.9):
+        el = np.radians(40.0)
+        eye = 2.6 * np.array([np.cos(az) * np.cos(el), np.sin(az) * np.cos(el), np.sin(el)])
+        mvp = S.perspective(40.0, H, W, 0.1, 20.0).astype(np.float64) @ \
+            S.view_matrix(S.lookat_pose(eye, up=(0.0, 0.0, 1.0))).astype(np.float64)
+        views.append(S.clip_positions(v, mvp))
+    tri = torch.from_numpy(f).cuda()
+    r = BatchRenderer([(tri, len(v), C)], [(0, (H, W)), (0, (H, W))], tile_log2=5, threads_per_tri=1,
+                      recompute=True, chunk_pixels=H * W)
+    assert len(r._chunks) == 2
+    pos_t = r.pack_positions([torch.from_numpy(p).cuda() for p in views]).requires_grad_(True)
+    attr_t = torch.from_numpy(attr).cuda().reshape(-1).requires_grad_(True)
+    target = rng.uniform(0, 1, r.image_floats).astype(np.float32)
+    loss, out = r.render_l1(pos_t, attr_t, torch.from_numpy(target).cuda(), grads_in_forward=grads_in_forward)
+    loss.backward()
+    torch.cuda.synchronize()
+    ov = r.images(out.detach())
+    tv = r.images(torch.from_numpy(target))
+    nbr = O.topology(f)
+    scale = 1.0 / r.image_floats
+    g_pos_ref = np.zeros((r.pos_rows, 4))
+    g_attr_ref = np.zeros(attr.shape)
+    for k in range(2):
+        _, _, o, gp, ga = _oracle_item_grads(views[k], f, attr, tv[k].numpy(), H, W, scale, nbr)
+        np.testing.assert_array_equal(ov[k].cpu().numpy(), o[0])
+        g_pos_ref[r.pos_offsets[k]:r.pos_offsets[k] + len(v)] = gp
+        g_attr_ref += ga
+    _grad_close(pos_t.grad.cpu().numpy(), g_pos_ref)
+    _grad_close(attr_t.grad.view(-1, C).cpu().numpy(), g_attr_ref)
