@@ -79,6 +79,8 @@ constexpr int kSetupCount = 0, kSetupFill = 1, kSetupBins = 2;
 
 template <int TILE_LOG2, int MODE>
 __global__ void __launch_bounds__(512) batch_setup_bin_kernel(BatchArgs a) {
+    pdl_wait();
+    pdl_launch_dependents();
     constexpr bool FILL = MODE == kSetupFill;
     const int2 blk = a.prim_blocks[blockIdx.x];
     const drp_batch_item& it = a.items[blk.x];
@@ -212,6 +214,8 @@ __global__ void __launch_bounds__((1 << (2 * TILE_LOG2)) < 256 ? (1 << (2 * TILE
 batch_fine_kernel(BatchArgs a) {
     __shared__ long long job;
     __shared__ int job_item;
+    pdl_wait();
+    pdl_launch_dependents();
     for (;;) {
         if (threadIdx.x == 0) {
             const long long j = (long long)atomicAdd(a.queue, 1u);
@@ -264,6 +268,8 @@ batch_fine_kernel(BatchArgs a) {
 }
 
 __global__ void __launch_bounds__(256) batch_aa_setup_kernel(BatchArgs a) {
+    pdl_wait();
+    pdl_launch_dependents();
     const int2 blk = a.prim_blocks[blockIdx.x];
     const drp_batch_item& it = a.items[blk.x];
     const long long j = (long long)blk.y * 256 + threadIdx.x;
@@ -291,6 +297,8 @@ __device__ __forceinline__ void aa_note_pixel(const BatchArgs& a, long long gpix
 }
 
 __global__ void __launch_bounds__(256) batch_aa_fwd_kernel(BatchArgs a) {
+    pdl_wait();
+    pdl_launch_dependents();
     const int2 blk = a.pix_blocks[blockIdx.x];
     const drp_batch_item& it = a.items[blk.x];
     const int pix = blk.y * 256 + threadIdx.x;
@@ -312,6 +320,8 @@ __global__ void __launch_bounds__(256) batch_aa_fwd_kernel(BatchArgs a) {
 // (reproducible loss).
 __global__ void __launch_bounds__(256, 5) batch_aa_l1_kernel(BatchArgs a) {
     __shared__ float warp_sum[8];
+    pdl_wait();
+    pdl_launch_dependents();
     const int2 blk = a.pix_blocks[blockIdx.x];
     const drp_batch_item& it = a.items[blk.x];
     const int pix = blk.y * 256 + threadIdx.x;
@@ -477,6 +487,8 @@ __global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
 // backward (attribute gradients, d/du, d/dv) -> rasterisation backward
 // (vertex gradients).  Warps never straddle items (256-pixel blocks).
 __global__ void __launch_bounds__(256, 4) batch_bwd_kernel(BatchArgs a) {
+    pdl_wait();
+    pdl_launch_dependents();
     const int2 blk = a.pix_blocks[blockIdx.x];
     const drp_batch_item& it = a.items[blk.x];
     const int pix = blk.y * 256 + threadIdx.x;
@@ -718,6 +730,8 @@ __device__ __forceinline__ void pixel_backward_l1(const BatchArgs& a, const drp_
 // item gets no gradient here).  Warps never straddle items (256-pixel blocks).
 __global__ void __launch_bounds__(256, 4) batch_aa_l1_grad_kernel(BatchArgs a) {
     __shared__ float warp_sum[8];
+    pdl_wait();
+    pdl_launch_dependents();
     const int2 blk = a.pix_blocks[blockIdx.x];
     const drp_batch_item& it = a.items[blk.x];
     const int pix = blk.y * 256 + threadIdx.x;
@@ -816,6 +830,19 @@ static void carve(BatchArgs& a, void* ws, const BatchLayout& L) {
 // Up to this many tiles per resident fine CTA the work order is sorted.
 constexpr long long kOrderTilesPerCTA = 8;
 
+// Zeroes the stats / work-queue block (256 bytes), the antialias pixel-list
+// count and the per-tile counts that a forward accumulates into: one kernel
+// in the forward's launch chain instead of three memsets.
+__global__ void __launch_bounds__(256) batch_clear_kernel(uint32_t* stats, unsigned* aa_count,
+                                                          uint32_t* tile_count, long long tiles) {
+    pdl_wait();
+    pdl_launch_dependents();
+    const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i0 < 64) stats[i0] = 0u;
+    if (i0 == 0 && aa_count) *aa_count = 0u;
+    for (long long i = i0; i < tiles; i += (long long)gridDim.x * blockDim.x) tile_count[i] = 0u;
+}
+
 template <int TL, int TPT>
 static void launch_batch_fine(const BatchArgs& a, cudaStream_t s) {
     constexpr int NT = (1 << (2 * TL)) < 256 ? (1 << (2 * TL)) : 256;
@@ -840,17 +867,19 @@ static void launch_batch_fine(const BatchArgs& a, cudaStream_t s) {
         launch_tile_order(a.tile_count, a.total_tiles, a.tile_cursor, s);
         b.tile_order = a.tile_cursor;
     }
-    batch_fine_kernel<TL, TPT><<<(unsigned)g, NT, 0, s>>>(b);
+    launch_pdl(batch_fine_kernel<TL, TPT>, dim3((unsigned)g), dim3(NT), s, b);
     drp_note_launch();
 }
 
 template <int TL>
 static void launch_batch_raster(const BatchArgs& a, cudaStream_t s) {
     if (a.n_prim_blocks > 0 && a.bin_depth) {
-        batch_setup_bin_kernel<TL, kSetupBins><<<(unsigned)a.n_prim_blocks, a.aa_records ? 512 : 256, 0, s>>>(a);
+        launch_pdl(batch_setup_bin_kernel<TL, kSetupBins>, dim3((unsigned)a.n_prim_blocks),
+                   dim3(a.aa_records ? 512 : 256), s, a);
         drp_note_launch();
     } else if (a.n_prim_blocks > 0) {
-        batch_setup_bin_kernel<TL, kSetupCount><<<(unsigned)a.n_prim_blocks, a.aa_records ? 512 : 256, 0, s>>>(a);
+        launch_pdl(batch_setup_bin_kernel<TL, kSetupCount>, dim3((unsigned)a.n_prim_blocks),
+                   dim3(a.aa_records ? 512 : 256), s, a);
         drp_note_launch();
         launch_tile_scan(a.tile_count, a.tile_offset, a.tile_cursor, a.total_tiles, a.chunk_sums,
                          reinterpret_cast<unsigned long long*>(a.stats), s);
@@ -913,9 +942,17 @@ static bool side_stream(cudaStream_t s, SideStream& out) {
 
 int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream_t s) {
     carve(a, ws, L);
-    cudaMemsetAsync(a.stats, 0, 256, s);  // stats and work queue
-    if (a.aa_count) cudaMemsetAsync(a.aa_count, 0, sizeof(unsigned), s);
-    cudaMemsetAsync(a.tile_count, 0, sizeof(uint32_t) * a.total_tiles, s);
+    {
+        // stats and work queue, list count, tile counts
+        const long long need = a.total_tiles > 64 ? a.total_tiles : 64;
+        const int sms = drp_current_sm_count();
+        long long blocks = (need + 255) / 256;
+        const long long cap = (long long)(sms > 0 ? sms : 1) * 4;
+        if (blocks > cap) blocks = cap;
+        launch_pdl(batch_clear_kernel, dim3((unsigned)blocks), dim3(256), s, a.stats, a.aa_count, a.tile_count,
+                   (long long)a.total_tiles);
+        drp_note_launch();
+    }
     switch (a.tile_log2) {
     case 3: launch_batch_raster<3>(a, s); break;
     case 5: launch_batch_raster<5>(a, s); break;
@@ -924,7 +961,7 @@ int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream
     // (the antialias triangle records were written by the setup / count pass)
     if (a.target && a.l1_grads) {
         if (a.n_pix_blocks > 0) {
-            batch_aa_l1_grad_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+            launch_pdl(batch_aa_l1_grad_kernel, dim3((unsigned)a.n_pix_blocks), dim3(256), s, a);
             drp_note_launch();
             // the listed pixels' whole backward beside the final loss sum
             // (both read only what the loss pass wrote)
@@ -951,7 +988,7 @@ int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream
     }
     if (a.target) {
         if (a.n_pix_blocks > 0) {
-            batch_aa_l1_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+            launch_pdl(batch_aa_l1_kernel, dim3((unsigned)a.n_pix_blocks), dim3(256), s, a);
             drp_note_launch();
         }
         launch_l1_final(a.block_loss, a.n_pix_blocks, a.l1_scale, a.loss, s);
@@ -959,7 +996,7 @@ int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream
     }
     if (!a.out) return 0;  // raster + interpolation only (recomputing them for the backward)
     if (a.n_pix_blocks > 0) {
-        batch_aa_fwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
+        launch_pdl(batch_aa_fwd_kernel, dim3((unsigned)a.n_pix_blocks), dim3(256), s, a);
         drp_note_launch();
     }
     return 0;
@@ -968,7 +1005,7 @@ int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream
 int launch_batch_backward(BatchArgs a, void* ws, const BatchLayout& L, bool reuse_records, cudaStream_t s) {
     carve(a, ws, L);
     if (a.n_prim_blocks > 0 && !reuse_records) {
-        batch_aa_setup_kernel<<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+        launch_pdl(batch_aa_setup_kernel, dim3((unsigned)a.n_prim_blocks), dim3(256), s, a);
         drp_note_launch();
     }
     if (a.n_pix_blocks <= 0) return 0;

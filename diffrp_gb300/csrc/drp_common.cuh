@@ -23,6 +23,20 @@
 
 namespace drp {
 
+// Programmatic dependent launch (Hopper and later).  A kernel launched with
+// launch_pdl() (drp_internal.h) may be scheduled before the kernel ahead of
+// it in the stream has finished, which hides the launch gap between the
+// dependent kernels of one pass.  pdl_wait() (griddepcontrol.wait) blocks
+// until the kernel ahead has completed and its memory writes are visible:
+// every kernel launched with launch_pdl() calls it before its first global
+// memory access.  pdl_launch_dependents() (griddepcontrol.launch_dependents)
+// lets the next kernel's CTAs be scheduled once every CTA of this grid has
+// issued it or exited.  Both are no-ops in a kernel launched without the
+// attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
+
 // ---------------------------------------------------------------------------
 // Triangle id <-> float encoding of the rast w channel
 // (diffrp/rendering/interpolator.py:24-29): ids up to 2^24 are stored as exact

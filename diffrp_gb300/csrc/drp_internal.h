@@ -7,6 +7,26 @@
 
 namespace drp {
 
+// Launch `kernel` on `s` with programmatic stream serialisation allowed: it
+// may start before the previous kernel in the stream ends, and waits for it
+// with pdl_wait() (drp_common.cuh) before touching memory.  Only for kernels
+// that call pdl_wait() first.  After a non-kernel operation (memset, event,
+// copy) the launch serialises as usual.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Tile-count scan: chunks of kScanChunk tiles, one block of kScanThreads each.
 constexpr int kScanThreads = 256;
 constexpr int kScanPerThread = 16;

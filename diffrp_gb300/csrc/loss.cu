@@ -82,6 +82,8 @@ __device__ inline void two_sum(float& s, float& c, float x) {
 __global__ void __launch_bounds__(1024) l1_final_kernel(const float* partial, long long nblocks, float scale,
                                                         float* loss) {
     __shared__ float warp_s[32], warp_c[32];
+    pdl_wait();
+    pdl_launch_dependents();
     float s = 0.0f, c = 0.0f;
     const long long step = (long long)blockDim.x;
     for (long long i = threadIdx.x; i < nblocks; i += 8 * step) {
@@ -116,7 +118,7 @@ __global__ void __launch_bounds__(1024) l1_final_kernel(const float* partial, lo
 }
 
 void launch_l1_final(const float* partial, long long nblocks, float scale, float* loss, cudaStream_t s) {
-    l1_final_kernel<<<1, 1024, 0, s>>>(partial, nblocks, scale, loss);
+    launch_pdl(l1_final_kernel, dim3(1), dim3(1024), s, partial, nblocks, scale, loss);
     drp_note_launch();
 }
 

@@ -745,6 +745,8 @@ static __global__ void __launch_bounds__(kOrderThreads) tile_order_kernel(const 
                                                                           uint32_t* __restrict__ order) {
     __shared__ uint32_t start[kOrderThreads];  // bucket k holds tiles of count 1023 - k (1023: or more)
     __shared__ uint32_t warp_tot[kOrderThreads / 32];
+    pdl_wait();
+    pdl_launch_dependents();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     start[tid] = 0;
     __syncthreads();
@@ -776,7 +778,7 @@ static __global__ void __launch_bounds__(kOrderThreads) tile_order_kernel(const 
 }
 
 static inline void launch_tile_order(const uint32_t* counts, long long n, uint32_t* order, cudaStream_t s) {
-    tile_order_kernel<<<1, kOrderThreads, 0, s>>>(counts, n, order);
+    launch_pdl(tile_order_kernel, dim3(1), dim3(kOrderThreads), s, counts, n, order);
     drp_note_launch();
 }
 
