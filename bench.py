@@ -725,15 +725,14 @@ def kernel_breakdown(dev, verts, f, attr, mvp, target, reps=10, tuned=None, batc
         # the step's backward reuses the antialias records and slot bits of its forward
         ops["batch_backward"] = lambda: batch._backward_raw(clip, flat_attr, b_rast, b_color, b_g, b_gp, b_ga,
                                                             batch._fwd_gen, aa_flags=b_flags)
-        # the headline step's forward: loss and its gradient in one pass (the
-        # gradient buffers are zeroed inside the timed graph, as in the step)
+        # the headline step's forward: loss and its gradient in one pass (its
+        # first kernel zeroes the gradient buffers, as in the step)
         b_gbuf = torch.zeros(clip.numel() + flat_attr.numel(), dtype=torch.float32, device=dev)
 
         def fwd_l1_grad():
-            b_gbuf.zero_()
             batch._forward_raw(clip, flat_attr, b_rast, b_color, b_out,
                                (b_target, 1.0 / b_color.numel(), b_blocks, b_loss, b_gbuf[:clip.numel()].view_as(clip),
-                                b_gbuf[clip.numel():]), flags=b_flags)
+                                b_gbuf[clip.numel():], b_gbuf), flags=b_flags)
         ops["batch_forward_l1_grad"] = fwd_l1_grad
     P = H * W
     # Algorithmic bytes per launch: every input read once, every output written once.

@@ -59,7 +59,8 @@ def _register():
         "drp_batch_forward_l1": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, I, I, ULL,
                                  ctypes.c_uint, P, P, P, P, LL, P, ctypes.c_float, P, P, P, P],
         "drp_batch_forward_l1_grad": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, I, I, ULL,
-                                      ctypes.c_uint, P, P, P, P, LL, P, ctypes.c_float, P, P, P, P, P],
+                                      ctypes.c_uint, P, P, P, P, LL, P, ctypes.c_float, P, P, P, P, P, LL, P],
+        "drp_scale_floats": [P, P, LL, P, P],
         "drp_batch_backward": [P, ctypes.c_size_t, P, I, P, LL, P, LL, LL, LL, P, P, P, P, P, P, P, LL, P, P, P, P,
                                P, I, P],
     }
@@ -297,7 +298,9 @@ class BatchRenderer:
         (target, scale, grad, block_loss, loss) fuses the L1 loss into the
         antialias pass (drp_batch_forward_l1); l1 = (target, scale,
         block_loss, loss, grad_pos, grad_attr) also forms the loss's gradient
-        there (drp_batch_forward_l1_grad, flags required).  flags: an
+        there (drp_batch_forward_l1_grad, flags required; grad_attr and
+        grad_pos are accumulated, after the call zeroes the buffer given
+        last, when it is not None).  flags: an
         antialias state block (_flags()) the forward fills for its backward,
         or None."""
         if not torch.cuda.is_current_stream_capturing():
@@ -317,12 +320,14 @@ class BatchRenderer:
         args = (self._items_dev.data_ptr(), len(self.items), self._pmap.data_ptr(), self.prim_blocks,
                 self._xmap.data_ptr(), self.pixel_blocks, self.total_prims, self.total_tiles, pos.data_ptr(),
                 self.tri.data_ptr(), attr.data_ptr(), self.nbr.data_ptr(), self.tile_log2, self.threads_per_tri)
-        if l1 is not None and len(l1) == 6:
+        if l1 is not None and len(l1) == 7:
             # the loss's gradient formed in the same pass: (target, scale,
-            # block_loss, loss, grad_pos, grad_attr)
-            target, scale, block_loss, loss, gpos, gattr = l1
+            # block_loss, loss, grad_pos, grad_attr, buffer the call zeroes
+            # first or None)
+            target, scale, block_loss, loss, gpos, gattr, zero = l1
             tail = (target.data_ptr(), ctypes.c_float(scale), block_loss.data_ptr(), loss.data_ptr(),
-                    gpos.data_ptr(), gattr.data_ptr(), stream)
+                    gpos.data_ptr(), gattr.data_ptr(), None if zero is None else zero.data_ptr(),
+                    0 if zero is None else zero.numel(), stream)
             entry = "drp_batch_forward_l1_grad"
         elif l1 is not None:
             target, scale, grad, block_loss, loss = l1
@@ -425,13 +430,11 @@ class BatchRenderer:
         return rast, color, out
 
 
-def _zero_grads(pos, attr, with_buffer=False):
+def _zero_grads(pos, attr):
     """Zeroed gradient buffers for pos and attr from one fill (the fused
-    backward accumulates into them); pos rows stay 16-byte aligned.
-    with_buffer: also return the one buffer both are views of."""
+    backward accumulates into them); pos rows stay 16-byte aligned."""
     buf = torch.zeros(pos.numel() + attr.numel(), dtype=torch.float32, device=pos.device)
-    views = buf[:pos.numel()].view_as(pos), buf[pos.numel():].view_as(attr)
-    return views + (buf,) if with_buffer else views
+    return buf[:pos.numel()].view_as(pos), buf[pos.numel():].view_as(attr)
 
 
 def _chunk_views(r, fl, chunk, l1):
@@ -561,7 +564,9 @@ class _BatchL1GradFn(torch.autograd.Function):
         ctx.set_materialize_grads(False)
         ctx.renderer = renderer
         scale = 1.0 / renderer.image_floats
-        gpos, gattr, gbuf = _zero_grads(pos, attr, with_buffer=True)
+        # one buffer for both gradients, zeroed by the first forward kernel
+        gbuf = torch.empty(pos.numel() + attr.numel(), dtype=torch.float32, device=pos.device)
+        gpos, gattr = gbuf[:pos.numel()].view_as(pos), gbuf[pos.numel():].view_as(attr)
         out = torch.empty(renderer.image_floats, dtype=torch.float32, device=pos.device)
         if renderer.recompute:
             losses = torch.empty(len(renderer._chunks), dtype=torch.float32, device=pos.device)
@@ -569,15 +574,15 @@ class _BatchL1GradFn(torch.autograd.Function):
             for k, c in enumerate(renderer._chunks):
                 color, _ = _chunk_views(renderer, fl, c, False)
                 c.renderer._forward_raw(pos[c.rows], attr, rast, color, out[c.floats],
-                                        (target[c.floats], scale, block_loss, losses[k], gpos[c.rows], gattr),
-                                        flags=flags)
+                                        (target[c.floats], scale, block_loss, losses[k], gpos[c.rows], gattr,
+                                         gbuf if k == 0 else None), flags=flags)
             ctx.save_for_backward(pos, attr, target, out, gbuf)
             return losses.sum(), out
         rast, color = renderer._buffers()
         block_loss = torch.empty(max(1, renderer.pixel_blocks), dtype=torch.float32, device=pos.device)
         loss = torch.empty((), dtype=torch.float32, device=pos.device)
         flags = renderer._flags()
-        renderer._forward_raw(pos, attr, rast, color, out, (target, scale, block_loss, loss, gpos, gattr),
+        renderer._forward_raw(pos, attr, rast, color, out, (target, scale, block_loss, loss, gpos, gattr, gbuf),
                               flags=flags)
         ctx.gen = renderer._fwd_gen
         ctx.save_for_backward(pos, attr, target, out, gbuf, flags, rast, color)
@@ -591,7 +596,10 @@ class _BatchL1GradFn(torch.autograd.Function):
         if g_out is None:
             if g_loss is None:
                 return torch.zeros_like(pos), torch.zeros_like(attr), None, None
-            g = gbuf * g_loss.to(torch.float32)
+            g = torch.empty_like(gbuf)
+            gl = g_loss.reshape(1).to(torch.float32).contiguous()
+            _ffi.call("drp_scale_floats", g.data_ptr(), gbuf.data_ptr(), gbuf.numel(), gl.data_ptr(),
+                      _ffi.stream_of(gbuf.device))
             return g[:pos.numel()].view_as(pos), g[pos.numel():].view_as(attr), None, None
         # the images reach the objective too: the full backward of
         # g_loss * loss + <g_out, images>

@@ -58,6 +58,8 @@ struct BatchArgs {
     float* block_loss;      // one partial per pixel block
     float* loss;
     bool l1_grads;          // the loss pass also forms the loss's gradient (drp_batch_forward_l1_grad)
+    float* zero_first;      // floats zeroed by the forward's first kernel (null: none)
+    long long zero_floats;
     const float* grad_scale;  // backward: device scalar multiplying grad_out, or null
     const float* grad_out;
     float* grad_pos;
@@ -833,14 +835,30 @@ constexpr long long kOrderTilesPerCTA = 8;
 // Zeroes the stats / work-queue block (256 bytes), the antialias pixel-list
 // count and the per-tile counts that a forward accumulates into: one kernel
 // in the forward's launch chain instead of three memsets.
+// Also zeroes `zero_n` floats at `zero` (the gradient buffers of
+// drp_batch_forward_l1_grad, when the call is asked to start them at zero).
 __global__ void __launch_bounds__(256) batch_clear_kernel(uint32_t* stats, unsigned* aa_count,
-                                                          uint32_t* tile_count, long long tiles) {
+                                                          uint32_t* tile_count, long long tiles, float* zero,
+                                                          long long zero_n) {
     pdl_wait();
     pdl_launch_dependents();
     const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
     if (i0 < 64) stats[i0] = 0u;
     if (i0 == 0 && aa_count) *aa_count = 0u;
-    for (long long i = i0; i < tiles; i += (long long)gridDim.x * blockDim.x) tile_count[i] = 0u;
+    for (long long i = i0; i < tiles; i += stride) tile_count[i] = 0u;
+    if (zero) {
+        // 16-byte groups from the first aligned float (the buffer start is
+        // at least 4-byte aligned), scalar head and tail
+        const long long head = (long long)(((16 - (reinterpret_cast<uintptr_t>(zero) & 15)) & 15) >> 2);
+        const long long h = head < zero_n ? head : zero_n;
+        if (i0 < h) zero[i0] = 0.f;
+        float4* z4 = reinterpret_cast<float4*>(zero + h);
+        const long long n4 = (zero_n - h) >> 2;
+        for (long long i = i0; i < n4; i += stride) z4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        const long long t0 = h + 4 * n4;
+        if (i0 < zero_n - t0) zero[t0 + i0] = 0.f;
+    }
 }
 
 template <int TL, int TPT>
@@ -943,14 +961,16 @@ static bool side_stream(cudaStream_t s, SideStream& out) {
 int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream_t s) {
     carve(a, ws, L);
     {
-        // stats and work queue, list count, tile counts
-        const long long need = a.total_tiles > 64 ? a.total_tiles : 64;
+        // stats and work queue, list count, tile counts (and the buffers a
+        // gradient-forming forward is asked to zero)
+        long long need = a.total_tiles > 64 ? a.total_tiles : 64;
+        if (a.zero_first && a.zero_floats / 4 > need) need = a.zero_floats / 4;
         const int sms = drp_current_sm_count();
         long long blocks = (need + 255) / 256;
         const long long cap = (long long)(sms > 0 ? sms : 1) * 4;
         if (blocks > cap) blocks = cap;
         launch_pdl(batch_clear_kernel, dim3((unsigned)blocks), dim3(256), s, a.stats, a.aa_count, a.tile_count,
-                   (long long)a.total_tiles);
+                   (long long)a.total_tiles, a.zero_first, a.zero_floats);
         drp_note_launch();
     }
     switch (a.tile_log2) {
@@ -1233,7 +1253,7 @@ DRP_API int drp_batch_forward_l1_grad(void* workspace, size_t workspace_bytes, c
                                       unsigned long long list_capacity, unsigned bin_depth, float* rast, float* color,
                                       float* out, void* aa_state, long long total_pixels, const float* target,
                                       float scale, float* block_loss, float* loss, float* grad_pos, float* grad_attr,
-                                      void* stream) {
+                                      float* zero_first, long long zero_floats, void* stream) {
     drp::BatchArgs a;
     drp::BatchLayout L;
     int st = batch_common(workspace, workspace_bytes, items, num_items, prim_block_map, prim_blocks, pixel_block_map,
@@ -1269,6 +1289,10 @@ DRP_API int drp_batch_forward_l1_grad(void* workspace, size_t workspace_bytes, c
     a.l1_grads = true;
     a.grad_pos = grad_pos;
     a.grad_attr = grad_attr;
+    if (zero_floats < 0 || (zero_floats > 0 && !zero_first) || (reinterpret_cast<uintptr_t>(zero_first) & 3))
+        return bfail("batch: bad zero region");
+    a.zero_first = zero_floats > 0 ? zero_first : nullptr;
+    a.zero_floats = zero_floats;
     drp::launch_batch_forward(a, workspace, L, static_cast<cudaStream_t>(stream));
     return drp_check_launch("drp_batch_forward_l1_grad");
 }

@@ -122,6 +122,30 @@ void launch_l1_final(const float* partial, long long nblocks, float scale, float
     drp_note_launch();
 }
 
+// dst = src * scale[0]: 16-byte groups from the first aligned float, scalar
+// head and tail (grid-stride).
+__global__ void __launch_bounds__(256) scale_floats_kernel(float* dst, const float* src, long long n,
+                                                           const float* scale) {
+    pdl_wait();
+    pdl_launch_dependents();
+    const float k = *scale;
+    const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const bool same_phase = ((reinterpret_cast<uintptr_t>(dst) ^ reinterpret_cast<uintptr_t>(src)) & 15) == 0;
+    long long h = same_phase ? (long long)(((16 - (reinterpret_cast<uintptr_t>(dst) & 15)) & 15) >> 2) : n;
+    if (h > n) h = n;
+    for (long long i = i0; i < h; i += stride) dst[i] = src[i] * k;
+    const long long n4 = (n - h) >> 2;
+    float4* d4 = reinterpret_cast<float4*>(dst + h);
+    const float4* s4 = reinterpret_cast<const float4*>(src + h);
+    for (long long i = i0; i < n4; i += stride) {
+        const float4 v = s4[i];
+        d4[i] = make_float4(v.x * k, v.y * k, v.z * k, v.w * k);
+    }
+    const long long t0 = h + 4 * n4;
+    if (i0 < n - t0) dst[t0 + i0] = src[t0 + i0] * k;
+}
+
 // Blocks for n elements: enough to fill every SM, never more than one
 // float4 group per thread.
 static long long l1_blocks(long long n) {
@@ -163,4 +187,23 @@ extern "C" __attribute__((visibility("default"))) int drp_l1_loss_fwd(void* work
     drp::l1_final_kernel<<<1, 1024, 0, s>>>(partial, nblocks, scale, loss);
     drp_note_launch();
     return drp_check_launch("drp_l1_loss_fwd");
+}
+
+extern "C" __attribute__((visibility("default"))) int drp_scale_floats(float* dst, const float* src, long long n,
+                                                                      const float* scale, void* stream) {
+    if (n < 0 || (n > 0 && (!dst || !src || !scale)) || ((reinterpret_cast<uintptr_t>(dst) |
+                                                        reinterpret_cast<uintptr_t>(src)) & 3)) {
+        drp_set_last_error("drp_scale_floats: bad arguments");
+        return 1;
+    }
+    if (n == 0) return 0;
+    const int sms = drp_current_sm_count();
+    long long blocks = (n / 4 + 255) / 256;
+    const long long cap = (long long)(sms > 0 ? sms : 1) * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    drp::launch_pdl(drp::scale_floats_kernel, dim3((unsigned)blocks), dim3(256), static_cast<cudaStream_t>(stream),
+                    dst, src, n, scale);
+    drp_note_launch();
+    return drp_check_launch("drp_scale_floats");
 }

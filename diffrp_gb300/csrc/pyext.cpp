@@ -151,6 +151,7 @@ DRP_FAST(drp_copy_async)
 DRP_FAST(drp_batch_forward)
 DRP_FAST(drp_batch_forward_l1)
 DRP_FAST(drp_batch_forward_l1_grad)
+DRP_FAST(drp_scale_floats)
 DRP_FAST(drp_batch_backward)
 
 PyMethodDef methods[] = {
@@ -158,7 +159,7 @@ PyMethodDef methods[] = {
     DRP_ENTRY(drp_interpolate_bwd),   DRP_ENTRY(drp_interpolate_sparse_fwd), DRP_ENTRY(drp_interpolate_sparse_bwd),
     DRP_ENTRY(drp_antialias_topology), DRP_ENTRY(drp_antialias_fwd),      DRP_ENTRY(drp_antialias_bwd),
     DRP_ENTRY(drp_edge_gradient_bwd), DRP_ENTRY(drp_l1_loss_fwd),         DRP_ENTRY(drp_batch_forward),
-    DRP_ENTRY(drp_batch_forward_l1),  DRP_ENTRY(drp_batch_forward_l1_grad),  DRP_ENTRY(drp_batch_backward),      DRP_ENTRY(drp_transform_points_fwd),
+    DRP_ENTRY(drp_batch_forward_l1),  DRP_ENTRY(drp_batch_forward_l1_grad),  DRP_ENTRY(drp_scale_floats),  DRP_ENTRY(drp_batch_backward),      DRP_ENTRY(drp_transform_points_fwd),
     DRP_ENTRY(drp_transform_points_bwd), DRP_ENTRY(drp_copy_async), {nullptr, nullptr, 0, nullptr}};
 
 PyModuleDef module = {PyModuleDef_HEAD_INIT, "_drp_fast", "CPython fast path onto libdiffrp_gb300", -1, methods,

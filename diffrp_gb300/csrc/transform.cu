@@ -15,6 +15,8 @@ __global__ void __launch_bounds__(256) transform_fwd_kernel(const float* __restr
                                                             const float* __restrict__ M, int B,
                                                             float4* __restrict__ out) {
     __shared__ float m[16];
+    pdl_wait();
+    pdl_launch_dependents();
     const int b = blockIdx.y;
     if (threadIdx.x < 16) m[threadIdx.x] = M[16 * b + threadIdx.x];
     __syncthreads();
@@ -31,6 +33,8 @@ __global__ void __launch_bounds__(256) transform_fwd_kernel(const float* __restr
 __global__ void __launch_bounds__(256) transform_bwd_kernel(const float4* __restrict__ grad_out, long long V,
                                                             const float* __restrict__ M, int B,
                                                             float* __restrict__ grad_verts) {
+    pdl_wait();
+    pdl_launch_dependents();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     float gx = 0.f, gy = 0.f, gz = 0.f;
@@ -59,8 +63,8 @@ DRP_API int drp_transform_points_fwd(const float* verts, long long num_vertices,
     }
     if (num_vertices == 0) return DRP_STATUS_OK;
     const dim3 grid((unsigned)((num_vertices + 255) / 256), (unsigned)num_views);
-    drp::transform_fwd_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        verts, num_vertices, mats, num_views, reinterpret_cast<float4*>(out));
+    drp::launch_pdl(drp::transform_fwd_kernel, grid, dim3(256), static_cast<cudaStream_t>(stream), verts,
+                    num_vertices, mats, num_views, reinterpret_cast<float4*>(out));
     drp_note_launch();
     return drp_check_launch("drp_transform_points_fwd");
 }
@@ -73,8 +77,9 @@ DRP_API int drp_transform_points_bwd(const float* grad_out, long long num_vertic
         return DRP_STATUS_INVALID_ARGUMENT;
     }
     if (num_vertices == 0) return DRP_STATUS_OK;
-    drp::transform_bwd_kernel<<<(unsigned)((num_vertices + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        reinterpret_cast<const float4*>(grad_out), num_vertices, mats, num_views, grad_verts);
+    drp::launch_pdl(drp::transform_bwd_kernel, dim3((unsigned)((num_vertices + 255) / 256)), dim3(256),
+                    static_cast<cudaStream_t>(stream), reinterpret_cast<const float4*>(grad_out), num_vertices, mats,
+                    num_views, grad_verts);
     drp_note_launch();
     return drp_check_launch("drp_transform_points_bwd");
 }

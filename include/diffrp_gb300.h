@@ -401,8 +401,11 @@ int drp_batch_forward_l1(void* workspace, size_t workspace_bytes, const drp_batc
  * is written.  At most 32 channels per item (an item with more sets
  * DRP_DEVERR_CHANNELS in the stats block and gets no gradient).  A caller
  * whose loss is the only consumer of the images can then skip the backward
- * pass entirely: multiply the two gradients by the loss's upstream gradient.
- * No counterpart in the reference.
+ * pass entirely: multiply the two gradients by the loss's upstream gradient
+ * (drp_scale_floats).  zero_first / zero_floats (may be NULL / 0): floats
+ * the call zeroes before anything is accumulated -- the gradient buffers,
+ * when the caller wants them started at zero (in its first kernel, instead
+ * of a separate fill).  No counterpart in the reference.
  */
 int drp_batch_forward_l1_grad(void* workspace, size_t workspace_bytes, const drp_batch_item* items, int num_items,
                               const int* prim_block_map, long long prim_blocks, const int* pixel_block_map,
@@ -410,7 +413,16 @@ int drp_batch_forward_l1_grad(void* workspace, size_t workspace_bytes, const drp
                               const int* tri, const float* attr, const int* nbr, int tile_log2, int threads_per_tri,
                               unsigned long long list_capacity, unsigned bin_depth, float* rast, float* color,
                               float* out, void* aa_state, long long total_pixels, const float* target, float scale,
-                              float* block_loss, float* loss, float* grad_pos, float* grad_attr, void* stream);
+                              float* block_loss, float* loss, float* grad_pos, float* grad_attr, float* zero_first,
+                              long long zero_floats, void* stream);
+
+/*
+ * dst[i] = src[i] * scale[0] for n floats (scale: one device float), dst and
+ * src 4-byte aligned, the same buffer or disjoint: the backward of a loss
+ * whose gradient drp_batch_forward_l1_grad formed, scaled by the loss's
+ * upstream gradient without a host read.  No counterpart in the reference.
+ */
+int drp_scale_floats(float* dst, const float* src, long long n, const float* scale, void* stream);
 
 /* drp_batch_backward flag: the workspace still holds the antialias triangle
  * records of the last drp_batch_forward, which ran on the same positions
