@@ -366,11 +366,13 @@ __device__ __forceinline__ int find_item_by_pixel(const drp_batch_item* items, i
 // pixel's interpolation backward (attribute atomics) and rasterisation
 // backward (vertex atomics).  batch_bwd_kernel skips these pixels, so the two
 // kernels are independent and run side by side.  The list is short and each
-// pixel's chain of dependent loads is long, so a quad of lanes takes one
-// pixel: lane q evaluates pair slot q (and scatters its edge gradient when it
-// owns the pair), the quad exchanges the slot terms by shuffles, the lanes
-// share the channels (c = q, q + 4, ...) and sum d/du, d/dv by shuffles.
-// Grid-stride over the device-side count, so the launch needs no host sync.
+// pixel's chain of dependent loads is long, so a group of LANES lanes takes
+// one pixel: lane q evaluates pair slots q, q + LANES, ... (and scatters a
+// slot's edge gradient when it owns the pair), the group exchanges the slot
+// terms by shuffles, the lanes share the channels (c = q, q + LANES, ...) and
+// sum d/du, d/dv by shuffles.  Grid-stride over the device-side count, so
+// the launch needs no host sync; the grid is one resident wave
+// (list_kernel_grid).
 // The incoming image gradient of one item: the gradient buffer times the
 // upstream scale, or (L1G, the forward that forms the loss's gradient) the
 // L1 sign gradient from the output and the target.
@@ -389,17 +391,35 @@ struct ItemGrad<true> {
     }
 };
 
-template <bool L1G>
+// Lanes per listed pixel in batch_aa_bwd_kernel.  Two lanes cover twice the
+// pixels of four per resident wave (the single-mesh step lists ~45K pixels:
+// one wave with two, two with four), but each lane's chain of slot
+// evaluations doubles and the kernel needs 74 registers; four measured
+// slightly faster on the single-mesh step (157.1 vs 159.2 us per step).
+#ifndef DRP_LIST_LANES
+#define DRP_LIST_LANES 4
+#endif
+constexpr int kListLanes = DRP_LIST_LANES;
+
+template <bool L1G, int LANES>
 __global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
+    static_assert(LANES == 2 || LANES == 4, "two or four lanes per listed pixel");
+    constexpr int SLOTS = 4 / LANES;  // pair slots each lane evaluates
     const unsigned n = *a.aa_count;
     const float gsc = (!L1G && a.grad_scale) ? *a.grad_scale : 1.0f;
-    const int lane = threadIdx.x & 31, q = lane & 3, qbase = lane & ~3;
-    const long long quads = ((long long)gridDim.x * blockDim.x) >> 2;
-    for (long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 2;; i += quads) {
+    const int lane = threadIdx.x & 31, q = lane & (LANES - 1), qbase = lane & ~(LANES - 1);
+    const long long groups = ((long long)gridDim.x * blockDim.x) / LANES;
+    for (long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / LANES;; i += groups) {
         const bool active = i < n;
-        if (!__any_sync(0xffffffffu, active)) break;  // warp-uniform exit (quads step together)
-        int role = 0, tgt = 0, pix = 0, C = 0;
-        float wt = 0.f;
+        if (!__any_sync(0xffffffffu, active)) break;  // warp-uniform exit (lane groups step together)
+        int role[SLOTS], tgt[SLOTS], pix = 0, C = 0;
+        float wt[SLOTS];
+#pragma unroll
+        for (int j = 0; j < SLOTS; ++j) {
+            role[j] = 0;
+            tgt[j] = 0;
+            wt[j] = 0.f;
+        }
         const drp_batch_item* itp = nullptr;
         if (active) {
             const long long gpix = a.aa_list[i];
@@ -409,35 +429,39 @@ __global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
             C = it.channels;
             const int W = it.width, H = it.height;
             const int py = pix / W, px = pix - py * W;
-            int A, B, ax, ay;
-            bool vert;
-            if (pair_slot(q, pix, px, py, W, H, A, B, ax, ay, vert)) {
-                const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
-                const float4 rs = R[pix], ro = R[A == pix ? B : A];
-                if (ro.w != rs.w) {
-                    AAPair p;
-                    aa_pair(a.aa_rec + it.prim_offset * 2, it.tri_count, A, B, ax, ay, vert, A == pix ? rs : ro,
-                            A == pix ? ro : rs, p);
-                    if (p.valid) {
-                        role = p.target == pix ? 1 : 2;
-                        tgt = p.target;
-                        wt = p.w;
-                        if (A == pix && !p.clamped)
-                            aa_edge_grad_g(p, a.color + it.image_offset, ItemGrad<L1G>::of(a, it, gsc), C,
-                                           reinterpret_cast<const float4*>(a.pos) + it.pos_offset,
-                                           a.tri + 3 * (long long)it.tri_first,
-                                           reinterpret_cast<float4*>(a.grad_pos) + it.pos_offset, 1.0f, W, H);
-                    }
-                }
+            const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
+            const float4 rs = R[pix];
+#pragma unroll
+            for (int j = 0; j < SLOTS; ++j) {
+                int A, B, ax, ay;
+                bool vert;
+                if (!pair_slot(q + j * LANES, pix, px, py, W, H, A, B, ax, ay, vert)) continue;
+                const float4 ro = R[A == pix ? B : A];
+                if (ro.w == rs.w) continue;
+                AAPair p;
+                aa_pair(a.aa_rec + it.prim_offset * 2, it.tri_count, A, B, ax, ay, vert, A == pix ? rs : ro,
+                        A == pix ? ro : rs, p);
+                if (!p.valid) continue;
+                role[j] = p.target == pix ? 1 : 2;
+                tgt[j] = p.target;
+                wt[j] = p.w;
+                if (A == pix && !p.clamped)
+                    aa_edge_grad_g(p, a.color + it.image_offset, ItemGrad<L1G>::of(a, it, gsc), C,
+                                   reinterpret_cast<const float4*>(a.pos) + it.pos_offset,
+                                   a.tri + 3 * (long long)it.tri_first,
+                                   reinterpret_cast<float4*>(a.grad_pos) + it.pos_offset, 1.0f, W, H);
             }
         }
+        // slot k was evaluated by lane (k % LANES) of the group, as its
+        // (k / LANES)-th slot
         AATerms at;
         at.any = false;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            at.role[k] = __shfl_sync(0xffffffffu, role, qbase | k);
-            at.tgt[k] = __shfl_sync(0xffffffffu, tgt, qbase | k);
-            at.wt[k] = __shfl_sync(0xffffffffu, wt, qbase | k);
+            const int src = qbase | (k % LANES);
+            at.role[k] = __shfl_sync(0xffffffffu, role[k / LANES], src);
+            at.tgt[k] = __shfl_sync(0xffffffffu, tgt[k / LANES], src);
+            at.wt[k] = __shfl_sync(0xffffffffu, wt[k / LANES], src);
             at.any = at.any || at.role[k] != 0;
         }
         int t = -1, i0 = 0, i1 = 0, i2 = 0;
@@ -452,7 +476,7 @@ __global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
                 const float* A = a.attr + it.attr_offset;
                 float* GA = a.grad_attr + it.attr_offset;
                 const float u = r.x, v = r.y, w = 1.0f - u - v;
-                for (int c = q; c < C; c += 4) {
+                for (int c = q; c < C; c += LANES) {
                     const float g = aa_bwd_channel_g(at, grad, C, pix, c);
                     const float x0 = A[(long long)i0 * C + c], x1 = A[(long long)i1 * C + c],
                                 x2 = A[(long long)i2 * C + c];
@@ -464,10 +488,11 @@ __global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
                 }
             }
         }
-        gu += __shfl_xor_sync(0xffffffffu, gu, 1);
-        gv += __shfl_xor_sync(0xffffffffu, gv, 1);
-        gu += __shfl_xor_sync(0xffffffffu, gu, 2);
-        gv += __shfl_xor_sync(0xffffffffu, gv, 2);
+#pragma unroll
+        for (int off = 1; off < LANES; off <<= 1) {
+            gu += __shfl_xor_sync(0xffffffffu, gu, off);
+            gv += __shfl_xor_sync(0xffffffffu, gv, off);
+        }
         if (active && t >= 0 && q == 0) {
             const drp_batch_item& it = *itp;
             const int W = it.width, H = it.height;
@@ -483,6 +508,22 @@ __global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
             atomic_add4(GP + i2, make_float4(g3[2].x, g3[2].y, 0.f, g3[2].w));
         }
     }
+}
+
+// One resident wave of the listed-pixel kernel (its CTAs per SM from the
+// occupancy query, cached per instantiation), capped by the pixel blocks.
+template <bool L1G>
+static long long list_kernel_grid(long long pix_blocks) {
+    static std::atomic<int> per_sm{0};
+    int per = per_sm.load(std::memory_order_relaxed);
+    if (per == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_aa_bwd_kernel<L1G, kListLanes>, 256, 0);
+        per = per > 0 ? per : 1;
+        per_sm.store(per, std::memory_order_relaxed);
+    }
+    const int sms = drp_current_sm_count();
+    const long long grid = (long long)(sms > 0 ? sms : 1) * per;
+    return pix_blocks < grid ? pix_blocks : grid;
 }
 
 // Fused backward of one pixel: antialias colour gradient -> interpolation
@@ -985,16 +1026,14 @@ int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream
             drp_note_launch();
             // the listed pixels' whole backward beside the final loss sum
             // (both read only what the loss pass wrote)
-            const int sms = drp_current_sm_count();
-            const long long grid = (long long)(sms > 0 ? sms : 1) * 4;
-            const long long g = a.n_pix_blocks < grid ? a.n_pix_blocks : grid;
+            const long long g = list_kernel_grid<true>(a.n_pix_blocks);
             SideStream side;
             const bool fork = side_stream(s, side);
             if (fork) {
                 cudaEventRecord(side.fork, s);
                 cudaStreamWaitEvent(side.stream, side.fork, 0);
             }
-            batch_aa_bwd_kernel<true><<<(unsigned)g, 256, 0, fork ? side.stream : s>>>(a);
+            batch_aa_bwd_kernel<true, kListLanes><<<(unsigned)g, 256, 0, fork ? side.stream : s>>>(a);
             drp_note_launch();
             launch_l1_final(a.block_loss, a.n_pix_blocks, a.l1_scale, a.loss, s);
             if (fork) {
@@ -1038,9 +1077,7 @@ int launch_batch_backward(BatchArgs a, void* ws, const BatchLayout& L, bool reus
     // and the fused backward of all other pixels are independent: fork the
     // list kernel onto a side stream so it fills the SMs beside the main
     // kernel and its tail, then join.  Both only add into the gradients.
-    const int sms = drp_current_sm_count();
-    const long long grid = (long long)(sms > 0 ? sms : 1) * 4;
-    const long long g = a.n_pix_blocks < grid ? a.n_pix_blocks : grid;
+    const long long g = list_kernel_grid<false>(a.n_pix_blocks);
     SideStream side;
     const bool fork = side_stream(s, side);
     if (fork) {
@@ -1049,7 +1086,7 @@ int launch_batch_backward(BatchArgs a, void* ws, const BatchLayout& L, bool reus
     }
     batch_bwd_kernel<<<(unsigned)a.n_pix_blocks, 256, 0, s>>>(a);
     drp_note_launch();
-    batch_aa_bwd_kernel<false><<<(unsigned)g, 256, 0, fork ? side.stream : s>>>(a);
+    batch_aa_bwd_kernel<false, kListLanes><<<(unsigned)g, 256, 0, fork ? side.stream : s>>>(a);
     drp_note_launch();
     if (fork) {
         cudaEventRecord(side.join, side.stream);
