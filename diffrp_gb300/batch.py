@@ -616,6 +616,9 @@ class _BatchL1GradFn(torch.autograd.Function):
                 cr._backward_raw(pos[c.rows], attr, rast, color, gout[c.floats], grad_pos[c.rows], grad_attr,
                                  cr._fwd_gen, aa_flags=flags)
             return grad_pos, grad_attr, None, None
-        flags, rast, color = saved[5:]
-        r._backward_raw(pos, attr, rast, color, gout, grad_pos, grad_attr, ctx.gen, aa_flags=flags)
+        _, rast, color = saved[5:]
+        # the gradient-forming forward fills only the state's pixel list, not
+        # its per-pixel flags: the backward evaluates every pixel's
+        # antialias terms itself
+        r._backward_raw(pos, attr, rast, color, gout, grad_pos, grad_attr, ctx.gen)
         return grad_pos, grad_attr, None, None

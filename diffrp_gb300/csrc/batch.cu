@@ -284,9 +284,12 @@ __global__ void __launch_bounds__(256) batch_aa_setup_kernel(BatchArgs a) {
 // Record a pixel some blending pair touches: its flag, and (warp-aggregated)
 // its global index in the list the antialias backward walks.  All 32 lanes
 // of the warp call it.
+// FLAGS = false: the list only (the forward that forms the loss's gradient
+// has no backward pass to read the per-pixel flags).
+template <bool FLAGS = true>
 __device__ __forceinline__ void aa_note_pixel(const BatchArgs& a, long long gpix, bool in, unsigned bits) {
     if (!a.aa_flags) return;
-    if (in) a.aa_flags[gpix] = bits ? 1 : 0;
+    if (FLAGS && in) a.aa_flags[gpix] = bits ? 1 : 0;
     const bool need = in && bits != 0u;
     const unsigned m = __ballot_sync(0xffffffffu, need);
     if (!m) return;
@@ -796,7 +799,7 @@ __global__ void __launch_bounds__(256, 4) batch_aa_l1_grad_kernel(BatchArgs a) {
         s = aa_fwd_pixel_l1(R, a.color + it.image_offset, a.aa_rec + it.prim_offset * 2, it.tri_count, W, H, C, pix,
                             a.target + row, a.l1_scale, a.out + row, nullptr, &bits, &nz, &ps);
     }
-    aa_note_pixel(a, it.pixel_offset + pix, in, bits);
+    aa_note_pixel<false>(a, it.pixel_offset + pix, in, bits);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
     if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = s;
