@@ -362,6 +362,67 @@ __device__ __forceinline__ uint32_t block_mask(int x0, int x1, int y0, int y1) {
     return (uint32_t)(cols * REP & rows);
 }
 
+// Column bits of one block row where a tile-local edge C + A dx + B dy holds
+// a pixel centre: bit i for the 8x4 block at columns [8i, 8i + 8) of the
+// rows [by, by + 4).  The edge's largest value over a block is at the corner
+// its steps point to; along the row it changes by 8 A per block.  In range of
+// int32 for every pixel of the tile (prepare_tile_prim keeps 32-bit steps only
+// where the edge's span over the tile is below 2^30).
+template <int COLS>
+__device__ __forceinline__ uint32_t edge_row_blocks(int A, int B, int C, int by) {
+    const int v = C + (A > 0 ? 7 * A : 0) + B * (B > 0 ? by + 3 : by);
+    uint32_t bits = 0u;
+#pragma unroll
+    for (int i = 0; i < COLS; ++i) bits |= (v + 8 * i * A >= 0 ? 1u : 0u) << i;
+    return bits;
+}
+
+// Narrow each prepared primitive's bounding-box block mask to the 8x4 blocks
+// that hold a pixel centre inside all three of its edges (exact: a block
+// dropped here has no pixel the primitive covers).  The bounding box of a
+// thin or diagonal triangle meets many blocks it never touches; each such
+// block would otherwise test the primitive at all 32 pixels.  One lane per
+// (primitive, block row): a warp handles 32 / (T / 4) primitives at a time
+// (4 on 32-pixel tiles), each lane testing the T / 8 blocks of its row, and
+// the rows' bits are OR-ed across the primitive's lanes.  BIG primitives
+// (64-bit edges) keep their bounding-box mask.  The result goes to
+// pcls[class][j] (class: facing, TP_NEG), 0 in the other class's row, so the
+// fine loop selects a class and a block with one load.
+template <int T, int NTHREADS>
+__device__ __forceinline__ void refine_block_masks(const TilePrim* prims, const uint32_t* pmask,
+                                                   uint32_t (*pcls)[NTHREADS], int n) {
+    constexpr int ROWS = T / 4, COLS = T / 8;  // 8x4 blocks per tile column / row
+    constexpr int PPW = 32 / ROWS;              // primitives per warp pass
+    constexpr int NW = NTHREADS / 32;
+    static_assert(ROWS * COLS <= 32 && 32 % ROWS == 0, "refine_block_masks: at most 32 blocks per tile");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / ROWS, row = lane % ROWS;
+    const int shift = row * COLS;
+    for (int j0 = warp * PPW; j0 < n; j0 += NW * PPW) {
+        const int j = j0 + sub;
+        uint32_t bits = 0u;
+        int neg = 0;
+        if (j < n) {
+            const int fl = prims[j].e2.y;
+            neg = (fl & TP_NEG) ? 1 : 0;
+            bits = (pmask[j] >> shift) & ((1u << COLS) - 1u);
+            if (bits && !(fl & TP_BIG)) {
+                const int4 e0 = prims[j].e0, e1 = prims[j].e1, e2 = prims[j].e2;
+                const int by = row * 4;
+                bits &= edge_row_blocks<COLS>(e0.x, e0.y, e0.z, by) & edge_row_blocks<COLS>(e0.w, e1.x, e1.y, by) &
+                        edge_row_blocks<COLS>(e1.z, e1.w, e2.x, by);
+            }
+        }
+        uint32_t m = bits << shift;
+#pragma unroll
+        for (int off = 1; off < ROWS; off <<= 1) m |= __shfl_xor_sync(0xffffffffu, m, off);
+        if (row == 0 && j < n) {
+            pcls[neg][j] = m;
+            pcls[1 - neg][j] = 0u;
+        }
+    }
+}
+
 // One tile's work for the fine raster.
 struct FineTile {
     const int4* recs;           // primitive records
@@ -405,6 +466,7 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
     __shared__ unsigned long long keys[NPIX];
     __shared__ TilePrim prims[CHUNK];
     __shared__ uint32_t pmask[CHUNK];  // 8x4 blocks each prepared primitive's bbox overlaps
+    __shared__ uint32_t pcls[2][CHUNK];  // TPT == 0: [facing class][prim] narrowed block masks
     __shared__ uint32_t pzlo[CHUNK];   // depth_order of a lower bound of the primitive's fragment depths
     __shared__ int n_complex;
     __shared__ int blk_next;           // next 8x4 block a warp takes (TPT == 0)
@@ -463,14 +525,14 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
         if (tid == 0) blk_next = 0;
         __syncthreads();
         if (TPT == 0) {
+            refine_block_masks<T, NTHREADS>(prims, pmask, pcls, n);
+            __syncthreads();
             // Facing class holding the nearest primitive (every warp computes
             // the same answer).
             uint32_t zmin0 = 0xffffffffu, zmin1 = 0xffffffffu;
             for (int j = lane; j < n; j += 32) {
-                const int f = prims[j].e2.y;
-                if (!(f & TP_ACTIVE)) continue;
-                if (f & TP_NEG) zmin1 = min(zmin1, pzlo[j]);
-                else zmin0 = min(zmin0, pzlo[j]);
+                if (pcls[0][j]) zmin0 = min(zmin0, pzlo[j]);
+                if (pcls[1][j]) zmin1 = min(zmin1, pzlo[j]);
             }
             const int first = __reduce_min_sync(0xffffffffu, zmin0) <= __reduce_min_sync(0xffffffffu, zmin1) ? 0 : 1;
             // keys are final at the end of this chunk unless a clipped
@@ -499,12 +561,11 @@ __device__ __forceinline__ void fine_tile(const FineTile& ft, Emit& emit) {
                         pass == 0 ? 0xffffffffu : __reduce_max_sync(0xffffffffu, (uint32_t)(best >> 32));
                     for (int j0 = 0; j0 < n; j0 += 32) {
                         const int j = j0 + lane;
-                        const bool meets = j < n && (pmask[j] & bit) && ((prims[j].e2.y & TP_NEG) ? 1 : 0) == want;
+                        const bool meets = j < n && (pcls[want][j] & bit) && pzlo[j] <= bmax;
                         uint32_t hits = __ballot_sync(0xffffffffu, meets);
                         while (hits) {
                             const int h = __ffs(hits) - 1;
                             hits &= hits - 1;
-                            if (pzlo[j0 + h] > bmax) continue;  // warp-uniform
                             const TilePrim& tp = prims[j0 + h];
                             const int4 e0 = tp.e0, e1 = tp.e1, e2 = tp.e2;
                             if (!tile_prim_covers(tp, e0, e1, e2, dx, dy, sx, sy)) continue;
