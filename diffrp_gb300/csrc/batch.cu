@@ -214,57 +214,61 @@ template <int TILE_LOG2, int TPT>
 __global__ void __launch_bounds__((1 << (2 * TILE_LOG2)) < 256 ? (1 << (2 * TILE_LOG2)) : 256,
                                   TILE_LOG2 == 3 ? 12 : 4)
 batch_fine_kernel(BatchArgs a) {
+    // The tile's parameters live in shared memory, filled by thread 0 with
+    // the job: held in registers through the fine raster they pushed its
+    // working set past the 64 registers of 4 CTAs per SM (spills).
     __shared__ long long job;
-    __shared__ int job_item;
+    __shared__ FineTile ft;
+    __shared__ BatchEmit e;
     pdl_wait();
     pdl_launch_dependents();
     for (;;) {
+        __syncthreads();  // every thread is done with the previous tile's job, ft and e
         if (threadIdx.x == 0) {
             const long long j = (long long)atomicAdd(a.queue, 1u);
-            job = j < a.total_tiles && a.tile_order ? (long long)a.tile_order[j] : j;
-            job_item = j < a.total_tiles ? find_item_by_tile(a.items, a.num_items, job) : -1;
+            const long long t = j < a.total_tiles && a.tile_order ? (long long)a.tile_order[j] : j;
+            job = t;
+            if (t < a.total_tiles) {
+                const int ii = find_item_by_tile(a.items, a.num_items, t);
+                const drp_batch_item& it = a.items[ii];
+                const int tile = (int)(t - it.tile_offset);
+                ft.recs = a.prims;
+                ft.cnt = a.tile_count[t];
+                if (a.bin_depth) {
+                    ft.list = a.tile_list + (unsigned long long)t * a.bin_depth;
+                    ft.overflow = ft.cnt > a.bin_depth;
+                    if (ft.overflow) atomicMax(a.stats + 3, ft.cnt);  // sizes the next depth
+                } else {
+                    const uint32_t off = a.tile_offset[t];
+                    ft.list = a.tile_list + off;
+                    ft.overflow = (unsigned long long)off + ft.cnt > a.list_capacity;
+                }
+                ft.scan_base = it.prim_offset;
+                ft.scan_count = it.tri_count;
+                ft.tx0 = (tile % it.tiles_x) << TILE_LOG2;
+                ft.ty0 = (tile / it.tiles_x) << TILE_LOG2;
+                ft.W = it.width;
+                ft.H = it.height;
+                ft.P = reinterpret_cast<const float4*>(a.pos) + it.pos_offset;
+                ft.tri = a.tri + 3 * (long long)it.tri_first;
+                ft.prev = nullptr;
+                ft.stats = a.stats;
+                e.P = ft.P;
+                e.tri = ft.tri;
+                e.A = a.attr + it.attr_offset;
+                e.W = it.width;
+                e.H = it.height;
+                e.C = it.channels;
+                e.rast = reinterpret_cast<float4*>(a.rast) + it.pixel_offset;
+                e.color = a.color + it.image_offset;
+                e.out = a.emit_out ? a.out + it.image_offset : nullptr;
+                e.vec = (it.channels & 3) == 0 &&
+                        ((reinterpret_cast<uintptr_t>(e.A) | reinterpret_cast<uintptr_t>(e.color) |
+                          reinterpret_cast<uintptr_t>(e.out)) & 15) == 0;
+            }
         }
         __syncthreads();
-        const long long t = job;
-        const int ii = job_item;
-        __syncthreads();
-        if (t >= a.total_tiles) break;
-        const drp_batch_item& it = a.items[ii];
-        const int tile = (int)(t - it.tile_offset);
-        FineTile ft;
-        ft.recs = a.prims;
-        ft.cnt = a.tile_count[t];
-        if (a.bin_depth) {
-            ft.list = a.tile_list + (unsigned long long)t * a.bin_depth;
-            ft.overflow = ft.cnt > a.bin_depth;
-            if (ft.overflow && threadIdx.x == 0) atomicMax(a.stats + 3, ft.cnt);  // sizes the next depth
-        } else {
-            const uint32_t off = a.tile_offset[t];
-            ft.list = a.tile_list + off;
-            ft.overflow = (unsigned long long)off + ft.cnt > a.list_capacity;
-        }
-        ft.scan_base = it.prim_offset;
-        ft.scan_count = it.tri_count;
-        ft.tx0 = (tile % it.tiles_x) << TILE_LOG2;
-        ft.ty0 = (tile / it.tiles_x) << TILE_LOG2;
-        ft.W = it.width;
-        ft.H = it.height;
-        ft.P = reinterpret_cast<const float4*>(a.pos) + it.pos_offset;
-        ft.tri = a.tri + 3 * (long long)it.tri_first;
-        ft.prev = nullptr;
-        ft.stats = a.stats;
-        BatchEmit e;
-        e.P = ft.P;
-        e.tri = ft.tri;
-        e.A = a.attr + it.attr_offset;
-        e.W = it.width;
-        e.H = it.height;
-        e.C = it.channels;
-        e.rast = reinterpret_cast<float4*>(a.rast) + it.pixel_offset;
-        e.color = a.color + it.image_offset;
-        e.out = a.emit_out ? a.out + it.image_offset : nullptr;
-        e.vec = (it.channels & 3) == 0 && ((reinterpret_cast<uintptr_t>(e.A) | reinterpret_cast<uintptr_t>(e.color) |
-                                            reinterpret_cast<uintptr_t>(e.out)) & 15) == 0;
+        if (job >= a.total_tiles) break;
         fine_tile<TILE_LOG2, TPT, false>(ft, e);
     }
 }
@@ -375,7 +379,10 @@ __device__ __forceinline__ int find_item_by_pixel(const drp_batch_item* items, i
 // terms by shuffles, the lanes share the channels (c = q, q + LANES, ...) and
 // sum d/du, d/dv by shuffles.  Grid-stride over the device-side count, so
 // the launch needs no host sync; the grid is one resident wave
-// (list_kernel_grid).
+// (list_kernel_grid).  L1G (the forward that forms the loss's gradient): the
+// kernel follows the antialias / loss pass on the launch chain, and its last
+// block first adds the loss from that pass's partials (no separate
+// final-sum launch).
 // The incoming image gradient of one item: the gradient buffer times the
 // upstream scale, or (L1G, the forward that forms the loss's gradient) the
 // L1 sign gradient from the output and the target.
@@ -408,6 +415,13 @@ template <bool L1G, int LANES>
 __global__ void __launch_bounds__(256) batch_aa_bwd_kernel(BatchArgs a) {
     static_assert(LANES == 2 || LANES == 4, "two or four lanes per listed pixel");
     constexpr int SLOTS = 4 / LANES;  // pair slots each lane evaluates
+    pdl_wait();
+    pdl_launch_dependents();
+    // the forward that forms the loss's gradient ends here: its last block
+    // also adds the loss (the partials of the antialias / loss pass)
+    static_assert(kFinalThreads == 256, "the list kernel's blocks form the loss");
+    if (L1G && blockIdx.x == gridDim.x - 1)
+        l1_final_block<kFinalThreads>(a.block_loss, a.n_pix_blocks, a.l1_scale, a.loss);
     const unsigned n = *a.aa_count;
     const float gsc = (!L1G && a.grad_scale) ? *a.grad_scale : 1.0f;
     const int lane = threadIdx.x & 31, q = lane & (LANES - 1), qbase = lane & ~(LANES - 1);
@@ -1027,22 +1041,11 @@ int launch_batch_forward(BatchArgs a, void* ws, const BatchLayout& L, cudaStream
         if (a.n_pix_blocks > 0) {
             launch_pdl(batch_aa_l1_grad_kernel, dim3((unsigned)a.n_pix_blocks), dim3(256), s, a);
             drp_note_launch();
-            // the listed pixels' whole backward beside the final loss sum
-            // (both read only what the loss pass wrote)
+            // the listed pixels' whole backward, and (its last block) the
+            // final loss sum: one launch on the chain
             const long long g = list_kernel_grid<true>(a.n_pix_blocks);
-            SideStream side;
-            const bool fork = side_stream(s, side);
-            if (fork) {
-                cudaEventRecord(side.fork, s);
-                cudaStreamWaitEvent(side.stream, side.fork, 0);
-            }
-            batch_aa_bwd_kernel<true, kListLanes><<<(unsigned)g, 256, 0, fork ? side.stream : s>>>(a);
+            launch_pdl(batch_aa_bwd_kernel<true, kListLanes>, dim3((unsigned)g), dim3(256), s, a);
             drp_note_launch();
-            launch_l1_final(a.block_loss, a.n_pix_blocks, a.l1_scale, a.loss, s);
-            if (fork) {
-                cudaEventRecord(side.join, side.stream);
-                cudaStreamWaitEvent(s, side.join, 0);
-            }
         } else {
             launch_l1_final(a.block_loss, a.n_pix_blocks, a.l1_scale, a.loss, s);
         }

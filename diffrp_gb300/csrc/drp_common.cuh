@@ -412,4 +412,61 @@ __device__ __forceinline__ void atomic_add4(float4* dst, const float4& v) {
 #endif
 }
 
+// s + x exactly as a float pair: s' = fl(s + x), err = (s + x) - s' (Knuth's
+// TwoSum, no branch).  Sums of pairs carry their rounding errors in c.
+__device__ __forceinline__ void two_sum(float& s, float& c, float x) {
+    const float t = s + x;
+    const float bp = t - s;
+    const float err = (s - (t - bp)) + (x - bp);
+    s = t;
+    c += err;
+}
+
+// Threads of the block that forms a loss from its per-block partials.
+constexpr int kFinalThreads = 256;
+
+// *loss = scale * (sum of nblocks partials), by one whole block of NT
+// threads: every thread adds its strided elements (eight loads in flight)
+// in index order as a (sum, error) float pair, then the pairs are combined
+// by a fixed shuffle tree within warps and across them -- a fixed order, so
+// the loss is reproducible from run to run.  Float pairs instead of doubles:
+// FP64 issues at a small fraction of the FP32 rate on this part, and this
+// block sits on the step's critical path.  Every thread of the block calls
+// it (it has a barrier).
+template <int NT>
+__device__ __forceinline__ void l1_final_block(const float* partial, long long nblocks, float scale, float* loss) {
+    static_assert(NT % 32 == 0 && NT <= 1024, "l1_final_block: whole warps, at most 1024 threads");
+    __shared__ float warp_s[NT / 32], warp_c[NT / 32];
+    float s = 0.0f, c = 0.0f;
+    for (long long i = threadIdx.x; i < nblocks; i += 8 * NT) {
+        float v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = i + k * NT < nblocks ? partial[i + k * NT] : 0.0f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) two_sum(s, c, v[k]);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float os = __shfl_xor_sync(0xffffffffu, s, off), oc = __shfl_xor_sync(0xffffffffu, c, off);
+        c += oc;
+        two_sum(s, c, os);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        warp_s[threadIdx.x >> 5] = s;
+        warp_c[threadIdx.x >> 5] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const bool have = threadIdx.x < NT / 32;
+        float v = have ? warp_s[threadIdx.x] : 0.0f, w = have ? warp_c[threadIdx.x] : 0.0f;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, v, off), ow = __shfl_xor_sync(0xffffffffu, w, off);
+            w += ow;
+            two_sum(v, w, ov);
+        }
+        if (threadIdx.x == 0) *loss = (v + w) * scale;
+    }
+}
+
 }  // namespace drp

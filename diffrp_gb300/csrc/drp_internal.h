@@ -151,10 +151,10 @@ size_t aa_ws_bytes(int B, long long F);
 int launch_aa_fwd(const AAArgs& a, cudaStream_t s);
 int launch_aa_bwd(const AAArgs& a, cudaStream_t s);
 
-// loss = scale * (sum of nblocks partial sums).  One 1024-thread block adds
-// the partials as (sum, error) float pairs with TwoSum, in a fixed order
-// (per thread, then by shuffles, then across warps), so the result is
-// reproducible from run to run.
+// loss = scale * (sum of nblocks partial sums).  One block of kFinalThreads
+// adds the partials as (sum, error) float pairs with TwoSum, in a fixed order
+// (per thread, then by shuffles, then across warps; l1_final_block), so the
+// result is reproducible from run to run.
 void launch_l1_final(const float* partial, long long nblocks, float scale, float* loss, cudaStream_t s);
 
 }  // namespace drp

@@ -63,62 +63,17 @@ __global__ void __launch_bounds__(kLossThreads) l1_partial_kernel(const float* p
     }
 }
 
-// s + x exactly as a float pair: s' = fl(s + x), err = (s + x) - s' (Knuth's
-// TwoSum, no branch).  Sums of pairs carry their rounding errors in c.
-__device__ inline void two_sum(float& s, float& c, float x) {
-    const float t = s + x;
-    const float bp = t - s;
-    const float err = (s - (t - bp)) + (x - bp);
-    s = t;
-    c += err;
-}
-
-// Fixed-order compensated sum of the partials: every thread adds its strided
-// elements (eight loads in flight) in index order, then the (sum, error)
-// pairs are combined by a fixed shuffle tree within warps and across them.
-// Float pairs instead of doubles: FP64 issues at a small fraction of the
-// FP32 rate on this part, and this single block sits on the step's critical
-// path.
-__global__ void __launch_bounds__(1024) l1_final_kernel(const float* partial, long long nblocks, float scale,
-                                                        float* loss) {
-    __shared__ float warp_s[32], warp_c[32];
+// Fixed-order compensated sum of the partials (l1_final_block,
+// drp_common.cuh) in one block.
+__global__ void __launch_bounds__(kFinalThreads) l1_final_kernel(const float* partial, long long nblocks, float scale,
+                                                                 float* loss) {
     pdl_wait();
     pdl_launch_dependents();
-    float s = 0.0f, c = 0.0f;
-    const long long step = (long long)blockDim.x;
-    for (long long i = threadIdx.x; i < nblocks; i += 8 * step) {
-        float v[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) v[k] = i + k * step < nblocks ? partial[i + k * step] : 0.0f;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) two_sum(s, c, v[k]);
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const float os = __shfl_xor_sync(0xffffffffu, s, off), oc = __shfl_xor_sync(0xffffffffu, c, off);
-        c += oc;
-        two_sum(s, c, os);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        warp_s[threadIdx.x >> 5] = s;
-        warp_c[threadIdx.x >> 5] = c;
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        const bool have = threadIdx.x < (int)(blockDim.x >> 5);
-        float v = have ? warp_s[threadIdx.x] : 0.0f, w = have ? warp_c[threadIdx.x] : 0.0f;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const float ov = __shfl_xor_sync(0xffffffffu, v, off), ow = __shfl_xor_sync(0xffffffffu, w, off);
-            w += ow;
-            two_sum(v, w, ov);
-        }
-        if (threadIdx.x == 0) *loss = (v + w) * scale;
-    }
+    l1_final_block<kFinalThreads>(partial, nblocks, scale, loss);
 }
 
 void launch_l1_final(const float* partial, long long nblocks, float scale, float* loss, cudaStream_t s) {
-    launch_pdl(l1_final_kernel, dim3(1), dim3(1024), s, partial, nblocks, scale, loss);
+    launch_pdl(l1_final_kernel, dim3(1), dim3(kFinalThreads), s, partial, nblocks, scale, loss);
     drp_note_launch();
 }
 
@@ -184,8 +139,7 @@ extern "C" __attribute__((visibility("default"))) int drp_l1_loss_fwd(void* work
     float* partial = static_cast<float*>(workspace);
     drp::l1_partial_kernel<<<(unsigned)nblocks, drp::kLossThreads, 0, s>>>(pred, target, n, scale, grad, partial);
     drp_note_launch();
-    drp::l1_final_kernel<<<1, 1024, 0, s>>>(partial, nblocks, scale, loss);
-    drp_note_launch();
+    drp::launch_l1_final(partial, nblocks, scale, loss, s);
     return drp_check_launch("drp_l1_loss_fwd");
 }
 
