@@ -78,20 +78,25 @@ struct BatchArgs {
 // kSetupFill: append to the exact lists (after the scan); kSetupBins: setup,
 // record and append to fixed-depth bins in one pass.
 constexpr int kSetupCount = 0, kSetupFill = 1, kSetupBins = 2;
+// CTAs per 256-triangle block of the map, and triangles per CTA: the work is
+// a chain of dependent loads per triangle, so smaller CTAs spread one mesh's
+// few hundred map blocks over every SM.
+constexpr int kSetupSplit = 4, kSetupTris = 256 / kSetupSplit;
 
 template <int TILE_LOG2, int MODE>
-__global__ void __launch_bounds__(512) batch_setup_bin_kernel(BatchArgs a) {
+__global__ void __launch_bounds__(2 * kSetupTris) batch_setup_bin_kernel(BatchArgs a) {
     pdl_wait();
     pdl_launch_dependents();
     constexpr bool FILL = MODE == kSetupFill;
-    const int2 blk = a.prim_blocks[blockIdx.x];
+    const int2 blk = a.prim_blocks[blockIdx.x / kSetupSplit];
     const drp_batch_item& it = a.items[blk.x];
-    // Count / bin launches with antialias records use 512 threads: the upper
-    // half writes the records of the block's 256 triangles while the lower
-    // half sets them up and bins them (two shorter chains of dependent loads
-    // instead of one).  Whole warps take one side.
-    if (threadIdx.x >= 256) {
-        const long long jr = (long long)blk.y * 256 + (threadIdx.x - 256);
+    const long long j0 = (long long)blk.y * 256 + (blockIdx.x % kSetupSplit) * kSetupTris;
+    // Count / bin launches with antialias records use 2 * kSetupTris threads:
+    // the upper half writes the records of the CTA's triangles while the
+    // lower half sets them up and bins them (two shorter chains of dependent
+    // loads instead of one).  Whole warps take one side.
+    if (threadIdx.x >= kSetupTris) {
+        const long long jr = j0 + (threadIdx.x - kSetupTris);
         if (!FILL && a.aa_records && jr < it.tri_count)
             aa_tri_record(reinterpret_cast<const float4*>(a.pos) + it.pos_offset,
                           a.tri + 3 * (long long)it.tri_first, a.nbr ? a.nbr + 3 * (long long)it.tri_first : nullptr,
@@ -99,7 +104,7 @@ __global__ void __launch_bounds__(512) batch_setup_bin_kernel(BatchArgs a) {
                           a.aa_rec + (it.prim_offset + jr) * 2);
         return;
     }
-    const long long j = (long long)blk.y * 256 + threadIdx.x;
+    const long long j = j0 + threadIdx.x;
     if (j >= it.tri_count) return;
     const long long pidx = it.prim_offset + j;
     int4* rec = a.prims + pidx * 3;
@@ -950,16 +955,16 @@ static void launch_batch_fine(const BatchArgs& a, cudaStream_t s) {
 template <int TL>
 static void launch_batch_raster(const BatchArgs& a, cudaStream_t s) {
     if (a.n_prim_blocks > 0 && a.bin_depth) {
-        launch_pdl(batch_setup_bin_kernel<TL, kSetupBins>, dim3((unsigned)a.n_prim_blocks),
-                   dim3(a.aa_records ? 512 : 256), s, a);
+        launch_pdl(batch_setup_bin_kernel<TL, kSetupBins>, dim3((unsigned)(a.n_prim_blocks * kSetupSplit)),
+                   dim3(a.aa_records ? 2 * kSetupTris : kSetupTris), s, a);
         drp_note_launch();
     } else if (a.n_prim_blocks > 0) {
-        launch_pdl(batch_setup_bin_kernel<TL, kSetupCount>, dim3((unsigned)a.n_prim_blocks),
-                   dim3(a.aa_records ? 512 : 256), s, a);
+        launch_pdl(batch_setup_bin_kernel<TL, kSetupCount>, dim3((unsigned)(a.n_prim_blocks * kSetupSplit)),
+                   dim3(a.aa_records ? 2 * kSetupTris : kSetupTris), s, a);
         drp_note_launch();
         launch_tile_scan(a.tile_count, a.tile_offset, a.tile_cursor, a.total_tiles, a.chunk_sums,
                          reinterpret_cast<unsigned long long*>(a.stats), s);
-        batch_setup_bin_kernel<TL, kSetupFill><<<(unsigned)a.n_prim_blocks, 256, 0, s>>>(a);
+        batch_setup_bin_kernel<TL, kSetupFill><<<(unsigned)(a.n_prim_blocks * kSetupSplit), kSetupTris, 0, s>>>(a);
         drp_note_launch();
     } else {
         cudaMemsetAsync(a.tile_offset, 0, sizeof(uint32_t) * a.total_tiles, s);
@@ -1188,7 +1193,7 @@ static int batch_common(void* ws, size_t ws_bytes, const drp_batch_item* items, 
     if (!ws || (reinterpret_cast<uintptr_t>(ws) & 255)) return bfail("batch: workspace must be 256-byte aligned");
     if (!items || num_items <= 0 || !pos || !tri || !attr) return bfail("batch: null table or buffer");
     if ((prim_blocks > 0 && !prim_block_map) || (pixel_blocks > 0 && !pixel_block_map) || prim_blocks < 0 ||
-        pixel_blocks < 0 || prim_blocks > 0x7fffffffll || pixel_blocks > 0x7fffffffll)
+        pixel_blocks < 0 || prim_blocks > 0x7fffffffll / drp::kSetupSplit || pixel_blocks > 0x7fffffffll)
         return bfail("batch: bad block maps");
     if ((reinterpret_cast<uintptr_t>(pos) & 15)) return bfail("batch: pos must be 16-byte aligned");
     if (list_capacity > 0x7fffffffull) return bfail("batch: list_capacity above 2^31 - 1");

@@ -334,7 +334,9 @@ typedef struct drp_batch_item {
 int drp_batch_plan(drp_batch_item* items, int num_items, int tile_log2, long long* totals);
 
 /* Host-side block maps (int pairs: item, block within the item) of 256
- * triangle slots / 256 pixels; sizes from totals[4] / totals[5]. */
+ * triangle slots / 256 pixels; sizes from totals[4] / totals[5].  The
+ * launches take at most (2^31 - 1) / 4 triangle blocks (each is set up by
+ * four CTAs) and 2^31 - 1 pixel blocks. */
 int drp_batch_block_maps(const drp_batch_item* items, int num_items, int* prim_block_map, int* pixel_block_map);
 
 int drp_batch_workspace_size(long long total_prims, long long total_tiles, unsigned long long list_capacity,
