@@ -301,14 +301,16 @@ def test_batch_recompute_chunks_match_stored(cuda_lib):
         assert float((got - ref).abs().max() / ref.abs().max()) <= 1e-5
 
 
-@pytest.mark.parametrize("recompute", RECOMPUTE)
+@pytest.mark.parametrize("recompute,tile_log2", [(m, 4) for m in RECOMPUTE] + [(False, 3), (False, 5)])
 @pytest.mark.parametrize("use_images", [False, True])
-def test_batch_render_l1_grads_in_forward(cuda_lib, recompute, use_images):
+def test_batch_render_l1_grads_in_forward(cuda_lib, recompute, tile_log2, use_images):
     """render_l1 with the loss's gradient formed in the forward pass gives
     the images bit for bit, the same loss and the gradients of the ordinary
     backward (to 1e-5), with a non-unit upstream loss gradient; when the
-    images reach the objective too, the full backward runs instead."""
-    r, pos, attr, _ = _renderer(recompute=recompute)
+    images reach the objective too, the full backward runs instead.  On 8-,
+    16- and 32-pixel tiles (stored buffers), and in the three recompute modes
+    on 16-pixel tiles."""
+    r, pos, attr, _ = _renderer(recompute=recompute, tile_log2=tile_log2)
     g = torch.Generator(device="cuda").manual_seed(11)
     target = torch.rand(r.image_floats, device="cuda", generator=g)
     w = torch.linspace(-1, 1, r.image_floats, device="cuda")
