@@ -108,12 +108,16 @@ def tune_rasterizer(ctx, pos, tri, resolution, ranges=None, reps=5, candidates=N
     return choice
 
 
-def tune_batch(renderer, pos, attr, reps=5, candidates=None):
+def tune_batch(renderer, pos, attr, reps=3, burst=8, candidates=None):
     """Time the batched forward (``drp_batch_forward``) of ``renderer`` on
     its own items for every (tile size, threads per primitive) candidate and
-    keep the fastest; returns the choice with the measured times.  A
-    recompute renderer is timed on its first chunk (the size it renders at),
-    so tuning allocates no more than one chunk's buffers."""
+    keep the fastest; returns the choice with the measured times.  Each
+    timing is ``burst`` forwards enqueued back to back between two events
+    (the device, not the host's launch rate, sets the pace: a single eager
+    forward of about 0.1 ms was too close to its launch overhead to separate
+    16- from 32-pixel tiles), the fastest of ``reps`` bursts per candidate.
+    A recompute renderer is timed on its first chunk (the size it renders
+    at), so tuning allocates no more than one chunk's buffers."""
     top = renderer
     if renderer.recompute:
         chunk = renderer._chunks[0]
@@ -128,18 +132,20 @@ def tune_batch(renderer, pos, attr, reps=5, candidates=None):
     for tl, tpt in candidates:
         renderer.set_raster_shape(tl, tpt)
         rast, color, out = renderer.forward_buffers(pos, attr)  # sizes the tile lists
+        p, a = pos.contiguous(), attr.contiguous().reshape(-1)
         ts = []
         for _ in range(reps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            renderer._forward_raw(pos.contiguous(), attr.contiguous().reshape(-1), rast, color, out)
+            for _ in range(burst):
+                renderer._forward_raw(p, a, rast, color, out)
             e1.record(stream)
             e1.synchronize()
-            ts.append(e0.elapsed_time(e1))
-        ts.sort()
-        times["%d/%d" % (tl, tpt)] = ts[len(ts) // 2]
-        if best is None or ts[len(ts) // 2] < best[0]:
-            best = (ts[len(ts) // 2], tl, tpt)
+            ts.append(e0.elapsed_time(e1) / burst)
+        t = min(ts)
+        times["%d/%d" % (tl, tpt)] = t
+        if best is None or t < best[0]:
+            best = (t, tl, tpt)
     top.set_raster_shape(best[1], best[2])
     renderer.forward_buffers(pos, attr)
     return {"tile_log2": best[1], "threads_per_tri": best[2], "ms": best[0], "times_ms": times}

@@ -104,18 +104,21 @@ __global__ void __launch_bounds__(2 * kSetupTris) batch_setup_bin_kernel(BatchAr
                           a.aa_rec + (it.prim_offset + jr) * 2);
         return;
     }
+    // every lane stays to the binning (a warp-collective call)
     const long long j = j0 + threadIdx.x;
-    if (j >= it.tri_count) return;
-    const long long pidx = it.prim_offset + j;
+    const bool in = j < it.tri_count;
+    const long long pidx = it.prim_offset + (in ? j : 0);
     int4* rec = a.prims + pidx * 3;
     PrimBox bx;
+    bx.px0 = 1;
+    bx.px1 = bx.py0 = bx.py1 = 0;
     bool live = false;
     if (FILL) {
-        bx = unpack_box(rec[1], rec[2]);
-        live = bx.px0 <= bx.px1;
-    } else {
-        bx.px0 = 1;
-        bx.px1 = bx.py0 = bx.py1 = 0;
+        if (in) {
+            bx = unpack_box(rec[1], rec[2]);
+            live = bx.px0 <= bx.px1;
+        }
+    } else if (in) {
         const long long t = (long long)it.tri_first + j;
         const int i0 = a.tri[3 * t], i1 = a.tri[3 * t + 1], i2 = a.tri[3 * t + 2];
         if (i0 < 0 || i1 < 0 || i2 < 0 || i0 >= it.num_vertices || i1 >= it.num_vertices || i2 >= it.num_vertices) {

@@ -50,19 +50,22 @@ template <int TILE_LOG2, int MODE>
 __global__ void __launch_bounds__(256) setup_bin_kernel(RasterArgs a) {
     constexpr bool FILL = MODE == kSetupFill;
     const int b = blockIdx.y;
+    // every lane stays to the binning (a warp-collective call)
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= a.max_view_tris) return;
-    const long long pidx = (long long)b * a.max_view_tris + j;
+    const bool in = j < a.max_view_tris;
+    const long long pidx = (long long)b * a.max_view_tris + (in ? j : 0);
     int4* rec = reinterpret_cast<int4*>(a.ws.prims) + pidx * 3;
     PrimBox bx;
+    bx.px0 = 1;
+    bx.px1 = bx.py0 = bx.py1 = 0;
     bool live = false;
     if (FILL) {
-        bx = unpack_box(rec[1], rec[2]);
-        live = bx.px0 <= bx.px1;
-    } else {
+        if (in) {
+            bx = unpack_box(rec[1], rec[2]);
+            live = bx.px0 <= bx.px1;
+        }
+    } else if (in) {
         const ViewRange vr = view_range(a.ranges, b, (int)a.num_triangles);
-        bx.px0 = 1;
-        bx.px1 = bx.py0 = bx.py1 = 0;
         if (j < vr.count) {
             const long long t = (long long)vr.first + j;
             const int i0 = a.tri[3 * t], i1 = a.tri[3 * t + 1], i2 = a.tri[3 * t + 2];

@@ -122,28 +122,55 @@ __device__ __forceinline__ bool build_prim(const float4& p0, const float4& p1, c
 
 // For every tile the box overlaps: count (list == null) or append `pidx` to
 // the tile's list through the cursors (warp-aggregated slots; entries past
-// `capacity` are dropped and the tile falls back to a full scan).  Every
-// lane of the warp must call this (n = 0 for lanes with nothing to bin).
-template <int TILE_LOG2>
+// `capacity` are dropped and the tile falls back to a full scan).
 // depth == 0: counters are cursors into one list of `capacity` entries
 // (slot = list index); depth > 0: counters count per tile and tile t's
 // entries go to list[t * depth + slot] while slot < depth (fixed-depth bins).
+// All 32 lanes of the warp call this (live = false for lanes with nothing to
+// bin), with one counters / tiles_x for the whole warp.  The warp's (box,
+// tile) pairs are dealt out over its lanes -- pair k to lane k % 32 -- so a
+// box covering many tiles costs its warp ceil(pairs / 32) rounds of
+// dependent atomics instead of one round per tile of the largest box.
+template <int TILE_LOG2>
 __device__ __forceinline__ void bin_box(const PrimBox& bx, bool live, int tiles_x, uint32_t* counters,
                                         uint32_t* list, unsigned long long capacity, uint32_t pidx,
                                         uint32_t depth = 0) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = lane_id();
     const int tx0 = bx.px0 >> TILE_LOG2, tx1 = bx.px1 >> TILE_LOG2, ty0 = bx.py0 >> TILE_LOG2,
               ty1 = bx.py1 >> TILE_LOG2;
     const int n = live ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0;
-    const int w = tx1 - tx0 + 1;
-    for (int i = 0;; ++i) {
-        const unsigned active = __ballot_sync(__activemask(), i < n);
-        if (i >= n) break;
-        const uint32_t tile = (uint32_t)((ty0 + i / w) * tiles_x + tx0 + i % w);
+    const int w = live ? tx1 - tx0 + 1 : 1;
+    int incl = n;  // inclusive prefix of the lanes' pair counts
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, d);
+        if (lane >= d) incl += y;
+    }
+    const int total = __shfl_sync(FULL, incl, 31);
+    const int start = incl - n;
+    for (int k0 = 0; k0 < total; k0 += 32) {  // warp-uniform trip count
+        const int k = k0 + lane;
+        // owner of pair k: the number of lanes whose prefix ends at or before k
+        int o = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int v = __shfl_sync(FULL, incl, o + step - 1);
+            if (v <= k) o += step;
+        }
+        const int o_start = __shfl_sync(FULL, start, o), o_w = __shfl_sync(FULL, w, o);
+        const int o_tx0 = __shfl_sync(FULL, tx0, o), o_ty0 = __shfl_sync(FULL, ty0, o);
+        const uint32_t o_pidx = __shfl_sync(FULL, pidx, o);
+        const bool has = k < total;
+        const unsigned active = __ballot_sync(FULL, has);
+        if (!has) continue;
+        const int r = k - o_start;
+        const uint32_t tile = (uint32_t)((o_ty0 + r / o_w) * tiles_x + o_tx0 + r % o_w);
         const uint32_t slot = warp_agg_inc(counters, tile, active);
         if (depth) {
-            if (slot < depth) list[(unsigned long long)tile * depth + slot] = pidx;
+            if (slot < depth) list[(unsigned long long)tile * depth + slot] = o_pidx;
         } else if (list && slot < capacity) {
-            list[slot] = pidx;
+            list[slot] = o_pidx;
         }
     }
 }
