@@ -218,6 +218,65 @@ __device__ __forceinline__ bool aa_fwd_terms(const float4* R, const float4* rec,
     return any;
 }
 
+// aa_fwd_terms for a warp of consecutive pixels of one image (lane l + 1
+// holds pixel pix + 1; lanes past the image pass in = false).  A pixel's
+// left pair is its left lane's right pair -- the same pair, evaluated from
+// the same inputs -- so it is taken from that lane by shuffle instead of
+// being evaluated a second time (lane 0 and pixels of column 0 evaluate
+// theirs).  The terms are identical to aa_fwd_terms'.  All 32 lanes call.
+__device__ __forceinline__ bool aa_fwd_terms_row(const float4* R, const float4* rec, long long F, int W, int H,
+                                                 int pix, bool in, int (&src)[4], float (&wt)[4],
+                                                 unsigned* pair_bits = nullptr) {
+    const int lane = threadIdx.x & 31;
+    const int py = pix / W, px = pix - py * W;
+    const bool share = lane > 0 && px > 0;  // the left lane holds pixel pix - 1 of this row
+    int A[4], B[4], ax[4], ay[4];
+    bool vert[4], has[4];
+    float4 rn[4];
+    float4 rs = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (in) rs = R[pix];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        has[q] = in && pair_slot(q, pix, px, py, W, H, A[q], B[q], ax[q], ay[q], vert[q]) && !(q == 0 && share);
+        if (has[q]) rn[q] = R[A[q] == pix ? B[q] : A[q]];
+    }
+    bool any = false;
+    unsigned bits = 0;
+    int right = 0;  // the right pair's target: 1 this pixel, 2 its right neighbour (0: no pair)
+    float right_w = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        src[q] = -1;
+        wt[q] = 0.f;
+        if (!has[q] || rn[q].w == rs.w) continue;
+        AAPair pr;
+        const bool first = A[q] == pix;
+        aa_pair(rec, F, A[q], B[q], ax[q], ay[q], vert[q], first ? rs : rn[q], first ? rn[q] : rs, pr);
+        if (pr.valid) bits |= 1u << q;
+        if (pr.valid && pr.target == pix) {
+            src[q] = pr.src;
+            wt[q] = pr.w;
+            any = true;
+        }
+        if (q == 1 && pr.valid) {
+            right = pr.target == pix ? 1 : 2;
+            right_w = pr.w;
+        }
+    }
+    const int left = __shfl_up_sync(0xffffffffu, right, 1);
+    const float left_w = __shfl_up_sync(0xffffffffu, right_w, 1);
+    if (in && share && left != 0) {
+        bits |= 1u;
+        if (left == 2) {  // this pixel is the pair's target, its left neighbour the source
+            src[0] = pix - 1;
+            wt[0] = left_w;
+            any = true;
+        }
+    }
+    if (pair_bits) *pair_bits = bits;
+    return any;
+}
+
 // Forward of one pixel: out = c + sum over pair slots targeting this pixel of
 // w (c[src] - c), in slot order (fmaf).  R, Cc: the view's rast and colour.
 // COPY = false: o already holds c (the caller wrote it), so pixels without a
@@ -247,22 +306,20 @@ __device__ __forceinline__ float l1_sign(float d, float scale) {
     return d > 0.0f ? scale : (d < 0.0f ? -scale : 0.0f);
 }
 
-// Forward of one pixel with the mean-absolute-error loss fused: the output
-// value of every channel as aa_fwd_pixel computes it (written to o when o is
-// not null), g = sign(out - target) * scale (written when g is not null),
-// and the return value is the pixel's sum of |out - target| in channel
-// order.  tg, o, g: this pixel's target, output and gradient rows;
-// pair_bits: as aa_fwd_terms.  sign_nz / sign_pos (may be null; at most 32
-// channels): bit c set when out - target of channel c is nonzero / positive,
-// which is g without the buffer.
-__device__ __forceinline__ float aa_fwd_pixel_l1(const float4* R, const float* Cc, const float4* rec, long long F,
-                                                 int W, int H, int C, int pix, const float* tg, float scale, float* o,
-                                                 float* g, unsigned* pair_bits = nullptr, unsigned* sign_nz = nullptr,
-                                                 unsigned* sign_pos = nullptr) {
+// Forward of one pixel with the mean-absolute-error loss fused
+// (aa_fwd_pixel_l1 = aa_fwd_terms + aa_l1_channels): the output value of
+// every channel as aa_fwd_pixel computes it (written to o when o is not
+// null), g = sign(out - target) * scale (written when g is not null), and
+// the return value is the pixel's sum of |out - target| in channel order.
+// tg, o, g: this pixel's target, output and gradient rows; pair_bits: as
+// aa_fwd_terms.  sign_nz / sign_pos (may be null; at most 32 channels): bit c
+// set when out - target of channel c is nonzero / positive, which is g
+// without the buffer.  aa_l1_channels takes the blend terms (src, wt, any)
+// from aa_fwd_terms or aa_fwd_terms_row.
+__device__ __forceinline__ float aa_l1_channels(const float* Cc, int C, int pix, const int (&src)[4],
+                                                const float (&wt)[4], bool any, const float* tg, float scale, float* o,
+                                                float* g, unsigned* sign_nz = nullptr, unsigned* sign_pos = nullptr) {
     const float* cs = Cc + (long long)pix * C;
-    int src[4];
-    float wt[4];
-    const bool any = aa_fwd_terms(R, rec, F, W, H, pix, src, wt, pair_bits);
     float s = 0.0f;
     unsigned nz = 0u, ps = 0u;
     const bool vec = (C & 3) == 0 && (((uintptr_t)cs | (uintptr_t)tg | (uintptr_t)(g ? g : cs) |
@@ -316,6 +373,16 @@ __device__ __forceinline__ float aa_fwd_pixel_l1(const float4* R, const float* C
     if (sign_nz) *sign_nz = nz;
     if (sign_pos) *sign_pos = ps;
     return s;
+}
+
+__device__ __forceinline__ float aa_fwd_pixel_l1(const float4* R, const float* Cc, const float4* rec, long long F,
+                                                 int W, int H, int C, int pix, const float* tg, float scale, float* o,
+                                                 float* g, unsigned* pair_bits = nullptr, unsigned* sign_nz = nullptr,
+                                                 unsigned* sign_pos = nullptr) {
+    int src[4];
+    float wt[4];
+    const bool any = aa_fwd_terms(R, rec, F, W, H, pix, src, wt, pair_bits);
+    return aa_l1_channels(Cc, C, pix, src, wt, any, tg, scale, o, g, sign_nz, sign_pos);
 }
 
 // The incoming image gradient at flat index i (pixel * C + channel), as the

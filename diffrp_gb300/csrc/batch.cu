@@ -345,12 +345,17 @@ __global__ void __launch_bounds__(256, 5) batch_aa_l1_kernel(BatchArgs a) {
     float s = 0.0f;
     const bool in = pix < it.width * it.height;
     unsigned bits = 0;
-    if (in) {
+    {
         const float4* R = reinterpret_cast<const float4*>(a.rast) + it.pixel_offset;
-        const long long row = it.image_offset + (long long)pix * it.channels;
-        s = aa_fwd_pixel_l1(R, a.color + it.image_offset, a.aa_rec + it.prim_offset * 2, it.tri_count, it.width,
-                            it.height, it.channels, pix, a.target + row, a.l1_scale, a.out ? a.out + row : nullptr,
-                            a.l1_grad + row, &bits);
+        int src[4];
+        float wt[4];
+        const bool any = aa_fwd_terms_row(R, a.aa_rec + it.prim_offset * 2, it.tri_count, it.width, it.height, pix,
+                                          in, src, wt, &bits);  // all lanes: pairs shared along the row
+        if (in) {
+            const long long row = it.image_offset + (long long)pix * it.channels;
+            s = aa_l1_channels(a.color + it.image_offset, it.channels, pix, src, wt, any, a.target + row,
+                               a.l1_scale, a.out ? a.out + row : nullptr, a.l1_grad + row);
+        }
     }
     aa_note_pixel(a, it.pixel_offset + pix, in, bits);
 #pragma unroll
@@ -816,10 +821,16 @@ __global__ void __launch_bounds__(256, 4) batch_aa_l1_grad_kernel(BatchArgs a) {
     }
     float s = 0.0f;
     unsigned bits = 0u, nz = 0u, ps = 0u;
-    if (in) {
-        const long long row = it.image_offset + (long long)pix * C;
-        s = aa_fwd_pixel_l1(R, a.color + it.image_offset, a.aa_rec + it.prim_offset * 2, it.tri_count, W, H, C, pix,
-                            a.target + row, a.l1_scale, a.out + row, nullptr, &bits, &nz, &ps);
+    {
+        int src[4];
+        float wt[4];
+        const bool any = aa_fwd_terms_row(R, a.aa_rec + it.prim_offset * 2, it.tri_count, W, H, pix, in, src, wt,
+                                          &bits);  // all lanes: pairs shared along the row
+        if (in) {
+            const long long row = it.image_offset + (long long)pix * C;
+            s = aa_l1_channels(a.color + it.image_offset, C, pix, src, wt, any, a.target + row, a.l1_scale,
+                               a.out + row, nullptr, &nz, &ps);
+        }
     }
     aa_note_pixel<false>(a, it.pixel_offset + pix, in, bits);
 #pragma unroll
