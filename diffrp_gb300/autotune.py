@@ -64,10 +64,13 @@ def apply(ctx, choice):
     return ctx
 
 
-def tune_rasterizer(ctx, pos, tri, resolution, ranges=None, reps=5, candidates=None, use_cache=True):
+def tune_rasterizer(ctx, pos, tri, resolution, ranges=None, reps=3, burst=8, candidates=None, use_cache=True):
     """Time every (tile size, threads per primitive) candidate on this
     geometry, set the fastest on ``ctx`` and return it (with the measured
-    times in milliseconds)."""
+    times in milliseconds).  Each timing is ``burst`` rasterisations enqueued
+    back to back between two events, the fastest of ``reps`` bursts: a
+    single call of about 0.05 ms sat too close to its own launch overhead
+    to separate the candidates reliably."""
     B = pos.shape[0] if pos.dim() == 3 else (1 if ranges is None else ranges.shape[0])
     key = workload_key(pos.device, B, resolution, tri.shape[0])
     if use_cache:
@@ -87,12 +90,12 @@ def tune_rasterizer(ctx, pos, tri, resolution, ranges=None, reps=5, candidates=N
         for _ in range(reps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            nvdr.rasterize(probe, pos, tri, resolution, ranges=ranges, grad_db=False)
+            for _ in range(burst):
+                nvdr.rasterize(probe, pos, tri, resolution, ranges=ranges, grad_db=False)
             e1.record(stream)
             e1.synchronize()
-            ts.append(e0.elapsed_time(e1))
-        ts.sort()
-        t = ts[len(ts) // 2]
+            ts.append(e0.elapsed_time(e1) / burst)
+        t = min(ts)
         times["%d/%d" % (tl, tpt)] = t
         if best is None or t < best[0]:
             best = (t, tl, tpt, probe.last_list_entries)
