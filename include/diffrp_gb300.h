@@ -398,8 +398,9 @@ int drp_batch_forward_l1(void* workspace, size_t workspace_bytes, const drp_batc
  * scale.  The pixels no blending pair touches get their backward inside the
  * antialias + loss kernel (their rast row and signs at hand, no gradient
  * image written); the listed ones in a second kernel that forms the sign from
- * out and target, forked onto the side stream drp_batch_backward uses, beside
- * the final loss sum.  out and aa_state are required; no sign-gradient image
+ * out and target and whose last block also forms the loss, the next launch
+ * on the caller's stream.  block_loss holds pixel_blocks floats.  out and
+ * aa_state are required; no sign-gradient image
  * is written.  At most 32 channels per item (an item with more sets
  * DRP_DEVERR_CHANNELS in the stats block and gets no gradient).  A caller
  * whose loss is the only consumer of the images can then skip the backward
