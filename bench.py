@@ -613,6 +613,17 @@ def _clock_sampler():
     return p, f.name
 
 
+def _hold_load(fn, seconds):
+    """Replay fn (untimed) for about `seconds`, so that the clock sampler
+    (nvidia-smi every 200 ms) sees the GPU under the timed step's own load."""
+    import torch
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        for _ in range(20):
+            fn()
+        torch.cuda.synchronize()
+
+
 def _clock_summary(proc, path, gpu_index):
     if proc is None:
         return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
@@ -954,8 +965,16 @@ def main():
     # -- device-resident timing: the batching form captured as one CUDA graph
     # is the headline; the drop-in (plain per-op) path is reported beside it,
     # graph-captured and eager ---------------------------------------------
+    # clocks: sampled while the headline graph runs, the same replays
+    # continuing untimed around the timed steps so that the 200 ms sampler
+    # records several samples under that load
     clk, clk_path = _clock_sampler()
+    if args.mode == "full":
+        _hold_load(batched, 0.6)
     total_ms = timed(batched, args.steps)
+    if args.mode == "full":
+        _hold_load(batched, 0.3)
+        clocks = _clock_summary(clk, clk_path, dev.index if dev.index is not None else 0)
     if args.mode == "steps":
         if clk is not None:
             clk.terminate()
@@ -982,7 +1001,6 @@ def main():
 
     e2e_graphs = [e2e_of(bstep), e2e_of(bstep, zero_copy=False), e2e_of(step)]
     e2e_ms, e2e_engine_ms, e2e_plain_ms = [timed(gs, args.steps) for gs in e2e_graphs]
-    clocks = _clock_summary(clk, clk_path, dev.index if dev.index is not None else 0)
     if world > 1:
         t = torch.tensor([total_ms, e2e_ms, eager_ms, plain_ms, e2e_plain_ms, e2e_engine_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
