@@ -1,6 +1,7 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles ``drp_oracle.c`` twice with gcc:
+Compiles ``drp_oracle.c`` and ``drp_oracle_tex.c`` (texture sampling)
+twice with gcc:
 
 * ``liborc_f32.so`` -- float shading, the bit-exact parity build;
 * ``liborc_f64.so`` -- double shading, the gradient / finite-difference build.
@@ -17,7 +18,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build")
-SRC = os.path.join(HERE, "drp_oracle.c")
+SRCS = [os.path.join(HERE, "drp_oracle.c"), os.path.join(HERE, "drp_oracle_tex.c")]
 
 
 def _compile(target, defines, openmp):
@@ -25,7 +26,7 @@ def _compile(target, defines, openmp):
            "-D_GNU_SOURCE", "-Wall", "-Wno-unknown-pragmas"]
     if openmp:
         cmd.append("-fopenmp")
-    cmd += defines + [SRC, "-o", target, "-lm"]
+    cmd += defines + SRCS + ["-o", target, "-lm"]
     return subprocess.run(cmd, capture_output=True, text=True)
 
 
@@ -37,7 +38,7 @@ def build(verbose=False):
     }
     for name, defs in variants.items():
         target = os.path.join(OUT, name)
-        if os.path.exists(target) and os.path.getmtime(target) >= os.path.getmtime(SRC):
+        if os.path.exists(target) and os.path.getmtime(target) >= max(os.path.getmtime(f) for f in SRCS):
             continue
         r = _compile(target, defs, openmp=True)
         if r.returncode != 0:

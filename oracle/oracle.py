@@ -27,6 +27,7 @@ __all__ = [
     "load", "triidx_to_float", "float_to_triidx", "raster_ids", "rasterize", "raster_bwd",
     "interpolate", "interpolate_bwd", "interpolate_sparse", "topology", "antialias", "antialias_bwd",
     "key_tri", "default_threads", "aa_plan", "l1_fixed_visibility",
+    "TEX_FILTERS", "TEX_BOUNDARIES", "tex_levels", "tex_mip_build", "tex_mip_bwd", "tex_fwd", "tex_bwd",
 ]
 
 _LIBS = {}
@@ -69,6 +70,20 @@ def load(precision="f32"):
         lib.orc_l1_fixed_visibility.argtypes = [_p, _p, _p, _c_int, _c_int, _c_int, _p, _p, _p, _c_long, _p, _p,
                                                 _c_int]
         lib.orc_l1_fixed_visibility.restype = _c_int
+        lib.orc_tex_levels.argtypes = [_c_int, _c_int, _c_int]
+        lib.orc_tex_levels.restype = _c_int
+        lib.orc_tex_pyramid_texels.argtypes = [_c_int, _c_int, _c_int]
+        lib.orc_tex_pyramid_texels.restype = _c_long
+        lib.orc_tex_mip_build.argtypes = [_p, _c_int, _c_int, _c_int, _c_int, _c_int, _p]
+        lib.orc_tex_mip_build.restype = None
+        lib.orc_tex_mip_bwd.argtypes = [_p, _c_int, _c_int, _c_int, _c_int, _c_int, _p]
+        lib.orc_tex_mip_bwd.restype = None
+        lib.orc_tex_fwd.argtypes = [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _c_int, _c_int, _c_int,
+                                    _c_int, _c_int, _p]
+        lib.orc_tex_fwd.restype = None
+        lib.orc_tex_bwd.argtypes = [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _c_int, _c_int, _c_int,
+                                    _c_int, _c_int, _p, _p, _p, _p, _p]
+        lib.orc_tex_bwd.restype = None
         for name in ["orc_raster_ids", "orc_shade", "orc_raster_bwd", "orc_interp_fwd", "orc_interp_bwd",
                      "orc_interp_sparse_fwd", "orc_topology", "orc_aa_fwd", "orc_aa_bwd"]:
             getattr(lib, name).restype = _c_int
@@ -346,3 +361,78 @@ def l1_fixed_visibility(pos, tri, attr, ids, sign, plan, resolution, tri_flag=No
                                                _ptr(plan), plan.shape[0], _ptr(flag), _ptr(out),
                                                nthreads or default_threads()), "l1_fixed_visibility")
     return float(out[0])
+
+
+# ---------------------------------------------------------------------------
+# Texture sampling (drp_oracle_tex.c): the mip-mapped sampler the CUDA
+# texture kernels restate.  tex (Nt, H, W, C), uv (N, h, w, 2), uv_da
+# (N, h, w, 4) = (du/dX, du/dY, dv/dX, dv/dY) or None.
+# ---------------------------------------------------------------------------
+TEX_FILTERS = {"nearest": 0, "linear": 1, "linear-mipmap-nearest": 2, "linear-mipmap-linear": 3}
+TEX_BOUNDARIES = {"wrap": 0, "clamp": 1, "zero": 2}
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def tex_levels(H, W, max_level=-1):
+    return load("f32").orc_tex_levels(H, W, -1 if max_level is None else max_level)
+
+
+def tex_mip_build(tex, levels, precision="f32"):
+    """Levels 1 .. levels-1 of the pyramid, level-major: a flat array of
+    Nt * C * texels(levels 1 ..) values (level 0 is tex itself)."""
+    lib, dt = load(precision), _dt(precision)
+    tex = np.ascontiguousarray(tex, dt)
+    N, H, W, C = tex.shape
+    n = lib.orc_tex_pyramid_texels(H, W, levels)
+    pyr = np.zeros(max(1, N * n * C), dt)
+    lib.orc_tex_mip_build(_ptr(tex), N, H, W, C, levels, _ptr(pyr))
+    return pyr
+
+
+def tex_mip_bwd(grad_tex, grad_pyr, levels, precision="f32"):
+    """grad_tex (Nt, H, W, C) plus the pyramid gradient carried down to it
+    (returns a new array; grad_pyr is not modified)."""
+    lib, dt = load(precision), _dt(precision)
+    out = np.ascontiguousarray(grad_tex, dt).copy()
+    g = np.ascontiguousarray(grad_pyr, dt).copy()
+    N, H, W, C = out.shape
+    lib.orc_tex_mip_bwd(_ptr(g), N, H, W, C, levels, _ptr(out))
+    return out
+
+
+def tex_fwd(tex, pyr, levels, uv, uv_da=None, filter_mode="linear", boundary_mode="wrap", precision="f32"):
+    lib, dt = load(precision), _dt(precision)
+    tex = np.ascontiguousarray(tex, dt)
+    pyr = np.ascontiguousarray(pyr, dt)
+    uv = np.ascontiguousarray(uv, dt)
+    Nt, H, W, C = tex.shape
+    N, h, w, _ = uv.shape
+    da = None if uv_da is None else np.ascontiguousarray(uv_da, dt)
+    out = np.zeros((N, h, w, C), dt)
+    lib.orc_tex_fwd(_ptr(tex), _ptr(pyr), Nt, H, W, C, levels, _ptr(uv), None if da is None else _ptr(da), N, h, w,
+                    TEX_FILTERS[filter_mode], TEX_BOUNDARIES[boundary_mode], _ptr(out))
+    return out
+
+
+def tex_bwd(tex, pyr, levels, uv, uv_da, grad_out, filter_mode="linear", boundary_mode="wrap", precision="f32"):
+    """(grad_tex, grad_pyr, grad_uv, grad_uv_da or None); grad_tex holds the
+    level-0 share only (tex_mip_bwd adds the pyramid's)."""
+    lib, dt = load(precision), _dt(precision)
+    tex = np.ascontiguousarray(tex, dt)
+    pyr = np.ascontiguousarray(pyr, dt)
+    uv = np.ascontiguousarray(uv, dt)
+    g = np.ascontiguousarray(grad_out, dt)
+    Nt, H, W, C = tex.shape
+    N, h, w, _ = uv.shape
+    da = None if uv_da is None else np.ascontiguousarray(uv_da, dt)
+    gtex = np.zeros_like(tex)
+    gpyr = np.zeros_like(pyr)
+    guv = np.zeros_like(uv)
+    gda = None if da is None else np.zeros_like(da)
+    lib.orc_tex_bwd(_ptr(tex), _ptr(pyr), Nt, H, W, C, levels, _ptr(uv), None if da is None else _ptr(da), N, h, w,
+                    TEX_FILTERS[filter_mode], TEX_BOUNDARIES[boundary_mode], _ptr(g), _ptr(gtex), _ptr(gpyr),
+                    _ptr(guv), None if gda is None else _ptr(gda))
+    return gtex, gpyr, guv, gda
