@@ -10,13 +10,15 @@ diffrp calls exactly these names:
 * ``interpolate(attr, rast, tri)``                    interpolator.py:83
 * ``antialias(color, rast, pos, tri)``                surface_deferred.py:775
 
-plus ``rasterize`` and ``antialias_construct_topology_hash`` from the same
-public API.  Argument order, tensor layouts, return tuples and error types
+plus ``rasterize``, ``antialias_construct_topology_hash`` and the mip-mapped
+``texture`` / ``texture_construct_mip`` (the consumer of interpolate's
+derivatives) from the same public API.  Argument order, tensor layouts, return tuples and error types
 follow nvdiffrast's documented interface; the arithmetic is this project's own
 CUDA (``libdiffrp_gb300.so`` through ``_ffi``).  There is no CPU path: every op
 requires CUDA tensors and the built library.
 """
 import collections
+import ctypes
 import numbers
 import threading
 
@@ -28,7 +30,7 @@ from . import _ffi
 
 __all__ = [
     "RasterizeCudaContext", "RasterizeGLContext", "DepthPeeler", "rasterize", "interpolate", "antialias",
-    "antialias_construct_topology_hash", "get_log_level", "set_log_level",
+    "antialias_construct_topology_hash", "texture", "texture_construct_mip", "get_log_level", "set_log_level",
 ]
 
 _log_level = 1
@@ -580,3 +582,136 @@ def antialias(color, rast, pos, tri, topology_hash=None, pos_gradient_boost=1.0)
         raise RuntimeError("topology_hash must come from antialias_construct_topology_hash(tri)")
     return _AntialiasFn.apply(color.contiguous(), rast.contiguous(), pos.contiguous(), tri, topology_hash,
                               float(pos_gradient_boost))
+
+
+# ---------------------------------------------------------------------------
+# Texture sampling
+# ---------------------------------------------------------------------------
+_TEX_FILTERS = {"nearest": 0, "linear": 1, "linear-mipmap-nearest": 2, "linear-mipmap-linear": 3}
+_TEX_BOUNDARIES = {"wrap": 0, "clamp": 1, "zero": 2}
+
+
+def _tex_levels(H, W, max_mip_level):
+    n = ctypes.c_int(0)
+    _ffi.call("drp_texture_levels", H, W, -1 if max_mip_level is None else int(max_mip_level), ctypes.byref(n))
+    return n.value
+
+
+def _tex_pyramid_floats(N, H, W, C, levels):
+    n = ctypes.c_longlong(0)
+    _ffi.call("drp_texture_pyramid_floats", N, H, W, C, levels, ctypes.byref(n))
+    return n.value
+
+
+def _tex_build(tex, levels):
+    N, H, W, C = tex.shape
+    pyr = torch.empty(max(1, _tex_pyramid_floats(N, H, W, C, levels)), dtype=torch.float32, device=tex.device)
+    if levels > 1:
+        _ffi.call("drp_texture_mip_build", tex.data_ptr(), N, H, W, C, levels, pyr.data_ptr(), _stream(tex.device))
+    return pyr
+
+
+class TextureMip:
+    """A pre-built mip pyramid (texture_construct_mip): levels 1 and up of
+    ``tex``, reused by texture(..., mip=...) instead of being rebuilt."""
+
+    def __init__(self, tex, levels, pyr):
+        self.tex, self.levels, self.pyr = tex, levels, pyr
+
+
+def texture_construct_mip(tex, max_mip_level=None, cube_mode=False):
+    """Build the mip pyramid of ``tex`` (N, H, W, C) once, for texture calls
+    that sample the same texture again (2x2 box average per level)."""
+    if cube_mode:
+        raise NotImplementedError("cube map textures are not supported")
+    _check_tensor("tex", tex, torch.float32, (4,))
+    tex = tex.contiguous()
+    levels = _tex_levels(tex.shape[1], tex.shape[2], max_mip_level)
+    with torch.no_grad():
+        return TextureMip(tex, levels, _tex_build(tex.detach(), levels))
+
+
+class _TextureFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, tex, uv, uv_da, pyr, levels, filt, bnd):
+        Nt, H, W, C = tex.shape
+        N, h, w = uv.shape[:3]
+        if pyr is None:
+            pyr = _tex_build(tex, levels)
+        out = torch.empty((N, h, w, C), dtype=torch.float32, device=tex.device)
+        _ffi.call("drp_texture_fwd", tex.data_ptr(), pyr.data_ptr(), Nt, H, W, C, levels, uv.data_ptr(),
+                  _ptr(uv_da), N, h, w, filt, bnd, out.data_ptr(), _stream(tex.device))
+        ctx.save_for_backward(tex, uv, uv_da, pyr)
+        ctx.meta = (levels, filt, bnd)
+        ctx.set_materialize_grads(False)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        tex, uv, uv_da, pyr = ctx.saved_tensors
+        levels, filt, bnd = ctx.meta
+        if grad_out is None:
+            return None, None, None, None, None, None, None
+        Nt, H, W, C = tex.shape
+        N, h, w = uv.shape[:3]
+        grad_out = grad_out.contiguous()
+        grad_tex = torch.zeros_like(tex)
+        grad_pyr = torch.empty_like(pyr)
+        grad_uv = torch.empty_like(uv)
+        want_da = uv_da is not None and ctx.needs_input_grad[2]
+        grad_da = torch.empty_like(uv_da) if want_da else None
+        _ffi.call("drp_texture_bwd", tex.data_ptr(), pyr.data_ptr(), Nt, H, W, C, levels, uv.data_ptr(),
+                  _ptr(uv_da), N, h, w, filt, bnd, grad_out.data_ptr(), grad_tex.data_ptr(), grad_pyr.data_ptr(),
+                  grad_uv.data_ptr(), _ptr(grad_da), _stream(tex.device))
+        return (grad_tex if ctx.needs_input_grad[0] else None, grad_uv if ctx.needs_input_grad[1] else None,
+                grad_da, None, None, None, None)
+
+
+def texture(tex, uv, uv_da=None, mip_level_bias=None, mip=None, filter_mode="auto", boundary_mode="wrap",
+            max_mip_level=None):
+    """Sample ``tex`` (N or 1, H, W, C) at ``uv`` (N, h, w, 2); returns (N, h, w, C).
+
+    Texel (x, y) is centred at ((x + 0.5) / W, (y + 0.5) / H).  filter_mode
+    'nearest', 'linear', 'linear-mipmap-nearest', 'linear-mipmap-linear' or
+    'auto' (trilinear with ``uv_da``, else bilinear); the mip-mapped modes
+    choose the level from ``uv_da`` (N, h, w, 4) = (du/dX, du/dY, dv/dX,
+    dv/dY), e.g. interpolate(..., diff_attrs=...)'s derivatives of uv.
+    boundary_mode 'wrap', 'clamp' or 'zero'.  ``mip`` reuses a
+    texture_construct_mip pyramid of ``tex``.  Gradients reach ``tex``
+    (through the pyramid), ``uv`` and ``uv_da`` (trilinear, where the level of
+    detail is not clamped).  Not supported: mip_level_bias and cube maps.
+    """
+    if mip_level_bias is not None:
+        raise NotImplementedError("mip_level_bias is not supported")
+    if boundary_mode not in _TEX_BOUNDARIES:
+        if boundary_mode == "cube":
+            raise NotImplementedError("cube map textures are not supported")
+        raise ValueError("boundary_mode must be one of %s" % sorted(_TEX_BOUNDARIES))
+    if filter_mode == "auto":
+        filter_mode = "linear-mipmap-linear" if uv_da is not None else "linear"
+    if filter_mode not in _TEX_FILTERS:
+        raise ValueError("filter_mode must be 'auto' or one of %s" % sorted(_TEX_FILTERS))
+    mipmapped = filter_mode.startswith("linear-mipmap")
+    if mipmapped and uv_da is None:
+        raise ValueError("filter_mode %r needs uv_da" % filter_mode)
+    _check_tensor("tex", tex, torch.float32, (4,))
+    _check_tensor("uv", uv, torch.float32, (4,), device=tex.device, last=2)
+    if tex.shape[0] not in (1, uv.shape[0]):
+        raise RuntimeError("tex minibatch %d must be 1 or the uv minibatch %d" % (tex.shape[0], uv.shape[0]))
+    if uv_da is not None:
+        _check_tensor("uv_da", uv_da, torch.float32, (4,), device=tex.device, last=4)
+        if tuple(uv_da.shape[:3]) != tuple(uv.shape[:3]):
+            raise RuntimeError("uv_da must have the shape of uv with 4 channels")
+        uv_da = uv_da.contiguous() if mipmapped else None
+    tex = tex.contiguous()
+    pyr = None
+    if mipmapped:
+        levels = _tex_levels(tex.shape[1], tex.shape[2], max_mip_level)
+        if mip is not None:
+            if not isinstance(mip, TextureMip) or tuple(mip.tex.shape) != tuple(tex.shape) or mip.levels != levels:
+                raise RuntimeError("mip was not built from this texture with this max_mip_level")
+            pyr = mip.pyr
+    else:
+        levels = 1
+    return _TextureFn.apply(tex, uv.contiguous(), uv_da, pyr, levels, _TEX_FILTERS[filter_mode],
+                            _TEX_BOUNDARIES[boundary_mode])

@@ -286,6 +286,47 @@ int drp_transform_points_bwd(const float* grad_out, long long num_vertices, cons
                              float* grad_verts, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Mip-mapped texture sampling: the consumer of interpolate's screen-space  */
+/* derivatives (uv_da), nvdiffrast's dr.texture as this project fixes it,   */
+/* for the texture lookups of diffrp's materials (reference:                */
+/* diffrp/materials/gltf_material.py:47-48 through                          */
+/* diffrp/utils/shader_ops.py:224 sample2d, which samples without mipmaps). */
+/* ------------------------------------------------------------------------ */
+/*
+ * Texture tex (num_tex, height, width, channels) float32; level 0 is tex
+ * itself, levels 1 .. levels-1 live in a caller buffer `pyr` of
+ * drp_texture_pyramid_floats() floats, level-major (level k: (num_tex, H_k,
+ * W_k, channels), H_k = max(1, H_{k-1} >> 1)), filled by
+ * drp_texture_mip_build (2x2 box average, indices clamped).
+ * Sampling: uv (num_views, out_height, out_width, 2), texel (x, y) centred
+ * at ((x + 0.5) / W, (y + 0.5) / H); uv_da (num_views, out_height,
+ * out_width, 4) = (du/dX, du/dY, dv/dX, dv/dY), 16-byte aligned, or NULL.
+ * num_tex is 1 (shared) or num_views.  filter_mode: 0 nearest, 1 linear,
+ * 2 linear-mipmap-nearest, 3 linear-mipmap-linear (level of detail 0.5
+ * log2 of the larger squared footprint in level-0 texels, clamped to the
+ * pyramid).  boundary_mode: 0 wrap, 1 clamp, 2 zero.  Textures of at most
+ * 32768 x 32768.
+ */
+int drp_texture_levels(int height, int width, int max_mip_level, int* levels);
+int drp_texture_pyramid_floats(int num_tex, int height, int width, int channels, int levels, long long* floats);
+int drp_texture_mip_build(const float* tex, int num_tex, int height, int width, int channels, int levels,
+                          float* pyr, void* stream);
+int drp_texture_fwd(const float* tex, const float* pyr, int num_tex, int height, int width, int channels,
+                    int levels, const float* uv, const float* uv_da, int num_views, int out_height, int out_width,
+                    int filter_mode, int boundary_mode, float* out, void* stream);
+/*
+ * Backward of drp_texture_fwd (and of the pyramid): grad_tex (tex layout) is
+ * accumulated (caller zeroes); grad_pyr is scratch of the pyramid's size
+ * (zeroed and consumed by the call); grad_uv (uv layout) is written;
+ * grad_uv_da (uv_da layout, may be NULL) is written -- nonzero only for
+ * linear-mipmap-linear where the level of detail is not clamped.
+ */
+int drp_texture_bwd(const float* tex, const float* pyr, int num_tex, int height, int width, int channels,
+                    int levels, const float* uv, const float* uv_da, int num_views, int out_height, int out_width,
+                    int filter_mode, int boundary_mode, const float* grad_out, float* grad_tex, float* grad_pyr,
+                    float* grad_uv, float* grad_uv_da, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Host transport (no counterpart in the reference, which leaves transfers  */
 /* to torch)                                                                */
 /* ------------------------------------------------------------------------ */

@@ -372,10 +372,6 @@ TEX_FILTERS = {"nearest": 0, "linear": 1, "linear-mipmap-nearest": 2, "linear-mi
 TEX_BOUNDARIES = {"wrap": 0, "clamp": 1, "zero": 2}
 
 
-def _ptr(a):
-    return a.ctypes.data_as(ctypes.c_void_p)
-
-
 def tex_levels(H, W, max_level=-1):
     return load("f32").orc_tex_levels(H, W, -1 if max_level is None else max_level)
 

@@ -1,0 +1,131 @@
+"""Mip-mapped texture sampling (nvdr.texture, csrc/texture.cu) against the
+oracle (oracle/drp_oracle_tex.c, itself pinned against grid_sample and
+float64 central differences in test_cpu_texture.py).
+
+* the pyramid and every filter x boundary forward: bit-exact;
+* gradients to the texture (through the pyramid), uv and uv_da: within 1e-5
+  of the largest component of the oracle's float32 backward (float atomics
+  change only the order of the texel sums);
+* the derivatives interpolate() produces, fed to texture(): the drop-in
+  chain rasterize -> interpolate(diff_attrs) -> texture, against the oracle;
+* argument errors.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FILTERS = ["nearest", "linear", "linear-mipmap-nearest", "linear-mipmap-linear"]
+BOUNDARIES = ["wrap", "clamp", "zero"]
+
+
+def _case(Nt, N, H, W, C, h, w, seed=0):
+    rng = np.random.default_rng(seed)
+    tex = rng.uniform(-1, 1, (Nt, H, W, C)).astype(np.float32)
+    uv = rng.uniform(-0.4, 1.4, (N, h, w, 2)).astype(np.float32)
+    # footprints from below one texel to beyond the whole texture
+    da = (rng.uniform(-1, 1, (N, h, w, 4)) * 2.0 ** rng.uniform(-2, np.log2(max(H, W)) + 1, (N, h, w, 1))
+          / max(H, W)).astype(np.float32)
+    return tex, uv, da
+
+
+def _t(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def test_pyramid_matches_oracle(cuda_lib):
+    from diffrp_gb300 import nvdr as dr
+    for (Nt, H, W, C) in [(1, 64, 64, 4), (2, 37, 53, 3), (1, 1, 9, 2), (3, 16, 1, 1)]:
+        tex = _case(Nt, 1, H, W, C, 1, 1)[0]
+        mip = dr.texture_construct_mip(_t(tex))
+        L = O.tex_levels(H, W)
+        assert mip.levels == L
+        ref = O.tex_mip_build(tex, L)
+        n = ref.size if L > 1 else 0
+        np.testing.assert_array_equal(mip.pyr.cpu().numpy()[:n], ref[:n])
+
+
+@pytest.mark.parametrize("filter_mode", FILTERS)
+@pytest.mark.parametrize("boundary", BOUNDARIES)
+@pytest.mark.parametrize("Nt", [1, 2])
+def test_forward_bit_exact(cuda_lib, filter_mode, boundary, Nt):
+    from diffrp_gb300 import nvdr as dr
+    H, W, C = 37, 53, 3
+    tex, uv, da = _case(Nt, 2, H, W, C, 19, 23, seed=Nt)
+    mipped = filter_mode.startswith("linear-mipmap")
+    got = dr.texture(_t(tex), _t(uv), _t(da) if mipped else None, filter_mode=filter_mode, boundary_mode=boundary)
+    L = O.tex_levels(H, W) if mipped else 1
+    ref = O.tex_fwd(tex, O.tex_mip_build(tex, L), L, uv, da if mipped else None, filter_mode, boundary)
+    np.testing.assert_array_equal(got.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("filter_mode", FILTERS)
+@pytest.mark.parametrize("boundary", BOUNDARIES)
+def test_gradients_match_oracle(cuda_lib, filter_mode, boundary):
+    from diffrp_gb300 import nvdr as dr
+    H, W, C = 32, 24, 4
+    tex, uv, da = _case(1, 2, H, W, C, 17, 13, seed=5)
+    mipped = filter_mode.startswith("linear-mipmap")
+    gout = np.random.default_rng(9).normal(size=(2, 17, 13, C)).astype(np.float32)
+    tex_t, uv_t = _t(tex).requires_grad_(True), _t(uv).requires_grad_(True)
+    da_t = _t(da).requires_grad_(True) if mipped else None
+    out = dr.texture(tex_t, uv_t, da_t, filter_mode=filter_mode, boundary_mode=boundary)
+    out.backward(_t(gout))
+    L = O.tex_levels(H, W) if mipped else 1
+    pyr = O.tex_mip_build(tex, L)
+    g0, gpyr, guv, gda = O.tex_bwd(tex, pyr, L, uv, da if mipped else None, gout, filter_mode, boundary)
+    gtex = O.tex_mip_bwd(g0, gpyr, L)
+    for got, ref, what in [(tex_t.grad, gtex, "tex"), (uv_t.grad, guv, "uv")] + \
+            ([(da_t.grad, gda, "uv_da")] if mipped else []):
+        got = got.cpu().numpy()
+        scale = max(float(np.abs(ref).max()), 1e-30)
+        assert float(np.abs(got - ref).max()) <= 1e-5 * scale, what
+    if filter_mode == "linear-mipmap-linear":
+        assert np.abs(gda).max() > 0  # the level of detail carries a gradient
+
+
+def test_interpolated_derivatives_drive_the_level(cuda_lib):
+    """rasterize -> interpolate(uv, diff_attrs) -> texture on a plane seen at
+    a grazing angle: the trilinear result equals the oracle's on the same
+    uv / uv_da, and far pixels sample coarser levels than near ones."""
+    from diffrp_gb300 import nvdr as dr
+    H = W = 128
+    # a quad receding in depth, uv tiled 8 times
+    pos = np.array([[-1, -1, 0.2, 1], [1, -1, 0.2, 1], [-4, 6, 0.9, 6], [4, 6, 0.9, 6]], np.float32)
+    tri = np.array([[0, 1, 2], [1, 3, 2]], np.int32)
+    uvs = np.array([[0, 0], [8, 0], [0, 8], [8, 8]], np.float32)
+    ctx = dr.RasterizeCudaContext()
+    rast, db = dr.rasterize(ctx, _t(pos), _t(tri), (H, W))
+    uv, uv_da = dr.interpolate(_t(uvs), rast, _t(tri), rast_db=db, diff_attrs="all")
+    rng = np.random.default_rng(2)
+    tex = rng.uniform(0, 1, (1, 64, 64, 3)).astype(np.float32)
+    got = dr.texture(_t(tex), uv, uv_da, filter_mode="linear-mipmap-linear", boundary_mode="wrap").cpu().numpy()
+    L = O.tex_levels(64, 64)
+    ref = O.tex_fwd(tex, O.tex_mip_build(tex, L), L, uv.cpu().numpy(), uv_da.cpu().numpy(), "linear-mipmap-linear",
+                    "wrap")
+    np.testing.assert_array_equal(got, ref)
+    # far rows (top) average more texels: their values vary less than near rows
+    cov = rast[0, ..., 3].cpu().numpy() > 0
+    near, far = got[0, 4:20][cov[4:20]], got[0, -40:-20][cov[-40:-20]]
+    assert near.size and far.size and far.std() < near.std()
+
+
+def test_argument_errors(cuda_lib):
+    from diffrp_gb300 import nvdr as dr
+    tex, uv, da = _case(1, 1, 8, 8, 1, 4, 4)
+    with pytest.raises(NotImplementedError):
+        dr.texture(_t(tex), _t(uv), _t(da), mip_level_bias=_t(da[..., 0]))
+    with pytest.raises(ValueError):
+        dr.texture(_t(tex), _t(uv), filter_mode="linear-mipmap-linear")
+    with pytest.raises(NotImplementedError):
+        dr.texture(_t(tex), _t(uv), boundary_mode="cube")
+    with pytest.raises(RuntimeError):
+        dr.texture(_t(np.concatenate([tex, tex, tex])), _t(np.concatenate([uv, uv])))
+    mip = dr.texture_construct_mip(_t(tex), max_mip_level=1)
+    with pytest.raises(RuntimeError):
+        dr.texture(_t(tex), _t(uv), _t(da), mip=mip)  # built for a different max_mip_level
+    out = dr.texture(_t(tex), _t(uv), _t(da), mip=mip, max_mip_level=1)
+    assert out.shape == (1, 4, 4, 1)
