@@ -1,2 +1,3 @@
 from .base_material import *  # noqa: F401,F403
 from .default_material import DefaultMaterial  # noqa: F401
+from .textured_material import TexturedMaterial, sample_texture  # noqa: F401

@@ -125,6 +125,15 @@ class SurfaceInput:
 
     @property
     @cached
+    def uv_da(self):
+        """Screen-space derivatives of ``uv``, (du/dX, du/dY, dv/dX, dv/dY)
+        in the layout of ``uv`` with 4 channels: the level of detail of
+        mip-mapped texture sampling.  Needs a session with
+        ``derivatives=True`` (an addition to the reference API)."""
+        return self.interpolator.derivatives(self.vertex_buffers.uv)
+
+    @property
+    @cached
     def world_tangent(self):
         return self.interpolate_ex(self.vertex_buffers.tangents, "vector3norex1")
 

@@ -81,32 +81,58 @@ class Interpolator(metaclass=abc.ABCMeta):
     def interpolate(self, vertex_buffer):
         raise NotImplementedError
 
+    def derivatives(self, vertex_buffer):
+        """Screen-space derivatives (dA/dX, dA/dY per channel) of an
+        interpolated attribute; needs the layer's rast_db (the session option
+        ``derivatives``)."""
+        raise RuntimeError("screen-space derivatives need the layer's rast_db "
+                           "(SurfaceDeferredRenderSessionOptions(derivatives=True))")
+
+
+def _derivatives(vertex_buffer, rast, tris, rast_db):
+    if rast_db is None or rast_db.shape[-1] != 4:
+        raise RuntimeError("screen-space derivatives need the layer's rast_db "
+                           "(SurfaceDeferredRenderSessionOptions(derivatives=True))")
+    _, da = dr.interpolate(vertex_buffer.contiguous(), rast, tris, rast_db=rast_db, diff_attrs="all")
+    return da
+
 
 class FullScreenInterpolator(Interpolator):
-    """Interpolates over the whole (1, H, W) rast with ``dr.interpolate``."""
+    """Interpolates over the whole (1, H, W) rast with ``dr.interpolate``;
+    with the layer's ``rast_db`` it also gives (1, H, W, 2C) derivatives."""
 
-    def __init__(self, vi_data, tris):
+    def __init__(self, vi_data, tris, rast_db=None):
         self.vi_data = vi_data.contiguous()
         self.tris = tris.contiguous()
+        self.rast_db = rast_db
 
     def interpolate(self, vertex_buffer):
         attr, _ = dr.interpolate(vertex_buffer.contiguous(), self.vi_data, self.tris)
         return attr
 
+    def derivatives(self, vertex_buffer):
+        return _derivatives(vertex_buffer, self.vi_data, self.tris, self.rast_db)
+
 
 class MaskedSparseInterpolator(Interpolator):
     """Interpolates only the pixels selected by ``mask`` (one material's
-    stencil); results are (N, C) rows in ``mask.nonzero`` order."""
+    stencil); results are (N, C) rows in ``mask.nonzero`` order.  With the
+    layer's ``rast_db``, derivatives are (N, 2C) rows in the same order."""
 
-    def __init__(self, vi_data, tris, mask, indices=None):
+    def __init__(self, vi_data, tris, mask, indices=None, rast_db=None):
         self.tris = tris
         # indices: the mask's nonzero index tuple when the caller already has it
         self.indices = mask.nonzero(as_tuple=True) if indices is None else indices
+        self.rast = vi_data
+        self.rast_db = rast_db
         self.vi_data = vi_data[self.indices]
         self.tri_idx = tris[float_to_triidx(self.vi_data[..., -1]) - 1].long()
 
     def interpolate(self, vertex_buffer):
         return polyfill_interpolate(vertex_buffer, self.vi_data, self.tri_idx)
+
+    def derivatives(self, vertex_buffer):
+        return _derivatives(vertex_buffer, self.rast.contiguous(), self.tris.contiguous(), self.rast_db)[self.indices]
 
 
 def stencil_groups(stencil, n_objects):

@@ -42,6 +42,10 @@ class SurfaceDeferredRenderSessionOptions:
         own pixels as (N, C) rows) or 'full_screen' ((1, H, W, C) buffers).
     deterministic and the ibl_* fields are accepted for API compatibility;
         lighting is not part of this package.
+    derivatives: rasterise with screen-space derivatives (rast_db), so that
+        materials can read ``SurfaceInput.uv_da`` for mip-mapped texture
+        sampling (an addition; off by default, as the reference discards
+        rast_db).
     """
     max_layers: int = 0
     interpolator_impl: str = "stencil_masked"
@@ -51,6 +55,7 @@ class SurfaceDeferredRenderSessionOptions:
     ibl_specular_mip_levels: int = 5
     ibl_diffuse_sample_resolution: int = 64
     ibl_diffuse_base_resolution: int = 16
+    derivatives: bool = False
 
     def __post_init__(self):
         if self.max_layers <= 0:
@@ -118,18 +123,36 @@ class SurfaceDeferredRenderSession(RenderSessionMixin):
     @cached
     def rasterize(self):
         """Rasterised layers, front to back; each (1, H, W, 4) =
-        (u, v, z/w, triangle id + 1) with u v1 + v v2 + (1 - u - v) v3 = p."""
+        (u, v, z/w, triangle id + 1) with u v1 + v v2 + (1 - u - v) v3 = p.
+
+        Peeling stops at the first empty layer, which is dropped unless it is
+        the last layer allowed (surface_deferred.py:258-266).  The emptiness
+        of a chunk of up to 4 layers is read back at once: one host wait per
+        chunk instead of one per layer (layers past the first empty one are
+        rasterised, found empty and dropped).  With options.derivatives the
+        layers' screen-space derivatives are kept for the interpolators."""
         vao = self.vertex_array_object()
         clip = self.clip_space()
         h, w = self.camera.resolution()
         ranges = torch.tensor([[0, len(vao.tris)]], dtype=torch.int32)
+        L = self.options.max_layers
         layers: List[torch.Tensor] = []
-        with dr.DepthPeeler(self.ctx, clip, vao.tris.contiguous(), (h, w), ranges, grad_db=False) as peeler:
-            for i in range(self.options.max_layers):
-                rast, _ = peeler.rasterize_next_layer()
-                if i < self.options.max_layers - 1 and bool((rast[..., 3] <= 0).all()):
+        dbs: List[Optional[torch.Tensor]] = []
+        with dr.DepthPeeler(self.ctx, clip, vao.tris.contiguous(), (h, w), ranges,
+                            grad_db=self.options.derivatives) as peeler:
+            i = 0
+            while i < L:
+                batch = [peeler.rasterize_next_layer() for _ in range(min(4, L - i))]
+                checked = [j for j in range(len(batch)) if i + j < L - 1]
+                empty = torch.stack([(batch[j][0][..., 3] <= 0).all() for j in checked]).tolist() if checked else []
+                stop = next((j for j, e in zip(checked, empty) if e), None)
+                keep = batch if stop is None else batch[:stop]
+                layers += [r for r, _ in keep]
+                dbs += [db if self.options.derivatives else None for _, db in keep]
+                if stop is not None:
                     break
-                layers.append(rast)
+                i += len(batch)
+        self._layer_db = dbs
         return layers
 
     # -- materials ----------------------------------------------------------
@@ -139,7 +162,10 @@ class SurfaceDeferredRenderSession(RenderSessionMixin):
         cam_v, cam_p = self.camera_V(), self.camera_P()
         impl = self.options.interpolator_impl
         out = []
-        for rast in self.rasterize():
+        layers = self.rasterize()
+        dbs = getattr(self, "_layer_db", None) or []  # absent when rasterize() was injected into the cache
+        for li, rast in enumerate(layers):
+            db = dbs[li] if li < len(dbs) else None
             mats = []
             if impl == "stencil_masked":
                 stencil = vao.stencils[float_to_triidx(rast[..., -1])]
@@ -147,9 +173,10 @@ class SurfaceDeferredRenderSession(RenderSessionMixin):
             for pi, obj in enumerate(self.scene.objects):
                 su = SurfaceUniform(obj.M, cam_v, cam_p)
                 if impl == "full_screen":
-                    si = SurfaceInput(su, vao, FullScreenInterpolator(rast, vao.tris))
+                    si = SurfaceInput(su, vao, FullScreenInterpolator(rast, vao.tris, rast_db=db))
                 elif impl == "stencil_masked":
-                    si = SurfaceInput(su, vao, MaskedSparseInterpolator(rast, vao.tris, None, indices=groups[pi]))
+                    si = SurfaceInput(su, vao, MaskedSparseInterpolator(rast, vao.tris, None, indices=groups[pi],
+                                                                        rast_db=db))
                     if len(si.interpolator.indices[0]) == 0:
                         mats.append((si, SurfaceOutputStandard()))
                         continue

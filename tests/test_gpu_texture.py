@@ -129,3 +129,82 @@ def test_argument_errors(cuda_lib):
         dr.texture(_t(tex), _t(uv), _t(da), mip=mip)  # built for a different max_mip_level
     out = dr.texture(_t(tex), _t(uv), _t(da), mip=mip, max_mip_level=1)
     assert out.shape == (1, 4, 4, 1)
+
+
+def test_sample_texture_keeps_sample2d_orientation(cuda_lib):
+    """materials.sample_texture without derivatives is diffrp's sample2d
+    (grid_sample with v flipped, border padding; diffrp/utils/shader_ops.py:
+    199-255) restated: uv (0, 0) at the bottom-left image corner."""
+    from diffrp_gb300.materials import sample_texture
+    rng = np.random.default_rng(4)
+    image = _t(rng.uniform(0, 1, (24, 40, 4)).astype(np.float32))
+    uv = _t(rng.uniform(-0.2, 1.2, (300, 2)).astype(np.float32))
+    got = sample_texture(image, uv, wrap="clamp")
+    grid = ((uv * 2 - 1) * torch.tensor([1.0, -1.0], device="cuda")).reshape(1, 1, -1, 2)
+    ref = torch.nn.functional.grid_sample(image[None].permute(0, 3, 1, 2), grid, mode="bilinear",
+                                          padding_mode="border", align_corners=False).view(4, -1).T
+    torch.testing.assert_close(got, ref, rtol=0, atol=2e-6)
+
+
+def _ground_scene(material):
+    from diffrp_gb300 import scene
+    # a plane below the default camera (at z = 3.2, looking down -z),
+    # receding to z = -8: uv tiled 8 x 40 across it
+    verts = torch.tensor([[-2, -0.6, 2.0], [2, -0.6, 2.0], [-2, -0.6, -8.0], [2, -0.6, -8.0]], device="cuda")
+    tris = torch.tensor([[0, 1, 2], [1, 3, 2]], dtype=torch.int32, device="cuda")
+    uv = torch.tensor([[0, 0], [8, 0], [0, 40], [8, 40]], dtype=torch.float32, device="cuda")
+    sc = scene.Scene()
+    sc.add_mesh_object(scene.MeshObject(material, verts, tris, uv=uv))
+    return sc
+
+
+def test_session_textured_material_uses_derivatives(cuda_lib):
+    """A textured ground plane through the session API: with derivatives the
+    material samples mip-mapped, so the far, minified part of the plane is
+    filtered (its albedo varies much less than with plain bilinear
+    sampling); both interpolator implementations give the same images."""
+    from diffrp_gb300.materials import TexturedMaterial
+    from diffrp_gb300.rendering import camera
+    from diffrp_gb300.rendering.surface_deferred import (SurfaceDeferredRenderSession,
+                                                         SurfaceDeferredRenderSessionOptions)
+    checker = ((np.indices((32, 32)).sum(0) % 2) * np.ones((4, 1, 1))).transpose(1, 2, 0).astype(np.float32)
+    cam = camera.PerspectiveCamera(fov=40, h=96, w=128)
+    images = {}
+    for impl in ["full_screen", "stencil_masked"]:
+        for deriv in [False, True]:
+            sc = _ground_scene(TexturedMaterial(_t(checker)))
+            opts = SurfaceDeferredRenderSessionOptions(interpolator_impl=impl, derivatives=deriv)
+            s = SurfaceDeferredRenderSession(sc, cam, opaque_only=True, options=opts)
+            images[impl, deriv] = s.albedo_layered()[0].cpu().numpy()[0]
+    for deriv in [False, True]:
+        np.testing.assert_allclose(images["full_screen", deriv], images["stencil_masked", deriv], rtol=0, atol=1e-6)
+    plain, mipped = images["full_screen", False], images["full_screen", True]
+    # the plane spans image rows 0 (near, bottom) to about 40 (far clip at
+    # distance 10); rows 25-38 see 10-60 texels per pixel
+    far_plain, far_mip = plain[25:38, 30:98, 0], mipped[25:38, 30:98, 0]
+    assert far_mip.std() < 0.5 * far_plain.std()
+    near = slice(0, 8)
+    np.testing.assert_allclose(mipped[near].mean(), plain[near].mean(), atol=0.1)
+
+
+def test_peeling_reads_emptiness_per_chunk(cuda_lib):
+    """Unlimited layers over a stack of 6 parallel quads: 6 layers (the
+    seventh is empty and dropped); a cap of 2 keeps 2, a cap of 9 keeps 6,
+    and a cap of 7 keeps its last layer although it is empty (the reference
+    loop, surface_deferred.py:258-266, drops an empty layer only before the
+    last one)."""
+    from diffrp_gb300 import scene, materials
+    from diffrp_gb300.rendering import camera
+    from diffrp_gb300.rendering.surface_deferred import (SurfaceDeferredRenderSession,
+                                                         SurfaceDeferredRenderSessionOptions)
+    cam = camera.PerspectiveCamera(fov=40, h=32, w=32)
+    for cap, want in [(0, 6), (2, 2), (9, 6), (6, 6), (7, 7)]:
+        sc = scene.Scene()
+        for k in range(6):
+            z = -0.5 * k
+            verts = torch.tensor([[-1, -1, z], [1, -1, z], [-1, 1, z], [1, 1, z]], device="cuda")
+            tris = torch.tensor([[0, 1, 2], [1, 3, 2]], dtype=torch.int32, device="cuda")
+            sc.add_mesh_object(scene.MeshObject(materials.DefaultMaterial(), verts, tris))
+        s = SurfaceDeferredRenderSession(sc, cam, opaque_only=False,
+                                         options=SurfaceDeferredRenderSessionOptions(max_layers=cap))
+        assert len(s.rasterize()) == want, (cap, len(s.rasterize()))
