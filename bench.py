@@ -560,6 +560,88 @@ def run_config1(dev, steps, warmup):
     return res
 
 
+WORKLOAD_TEX = ("1024x1024 RGBA texture, trilinear (linear-mipmap-linear, wrap), sampled at the 1024x1024 pixels of a "
+                "receding ground plane (uv tiled 16 x 64, uv / uv_da from rasterize + interpolate, levels 0-10), "
+                "fwd+bwd to the texture (through the pyramid), uv and uv_da")
+
+
+def texture_inputs(dev, n=1024, tex_n=1024, seed=0):
+    """uv and uv_da of a ground plane seen at a grazing angle (interpolated
+    once, outside the timed region), and a random texture."""
+    import torch
+    from diffrp_gb300 import nvdr as dr
+    pos = torch.tensor([[-1, -1, 0.2, 1], [1, -1, 0.2, 1], [-12, 16, 0.99, 16], [12, 16, 0.99, 16]],
+                       dtype=torch.float32, device=dev)
+    tri = torch.tensor([[0, 1, 2], [1, 3, 2]], dtype=torch.int32, device=dev)
+    uvs = torch.tensor([[0, 0], [16, 0], [0, 64], [16, 64]], dtype=torch.float32, device=dev)
+    rast, db = dr.rasterize(dr.RasterizeCudaContext(dev), pos, tri, (n, n))
+    uv, uv_da = dr.interpolate(uvs, rast, tri, rast_db=db, diff_attrs="all")
+    g = torch.Generator(device=dev).manual_seed(seed)
+    tex = torch.rand((1, tex_n, tex_n, 4), generator=g, device=dev)
+    return tex, uv.contiguous(), uv_da.contiguous()
+
+
+def run_texture(dev, steps, warmup, cpu=True):
+    """Mip-mapped texture sampling (nvdr.texture), fwd+bwd as one CUDA graph,
+    L2 flushed between steps; the CPU oracle on a sample of rows beside it."""
+    import torch
+    from diffrp_gb300 import nvdr as dr
+    n = 1024
+    tex0, uv0, da0 = texture_inputs(dev, n)
+    tex = tex0.clone().requires_grad_(True)
+    uv = uv0.clone().requires_grad_(True)
+    da = da0.clone().requires_grad_(True)
+    gout = torch.rand((1, n, n, 4), device=dev)
+
+    def step():
+        tex.grad = uv.grad = da.grad = None
+        out = dr.texture(tex, uv, da, filter_mode="linear-mipmap-linear", boundary_mode="wrap")
+        out.backward(gout)
+        return out
+
+    g = _graph(step, dev, warm=max(2, warmup))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    s = torch.cuda.current_stream(dev)
+    for _ in range(max(3, warmup)):
+        g.replay()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize(dev)
+    for i in range(steps):
+        flush.fill_(i & 0xff)
+        evs[i][0].record(s)
+        g.replay()
+        evs[i][1].record(s)
+    torch.cuda.synchronize(dev)
+    ms = sum(a.elapsed_time(b) for a, b in evs) / steps
+    P = n * n
+    T = tex.numel() * 4  # texture bytes; the pyramid adds a third
+    # pixel streams: uv, uv_da, output (fwd) + grad_out, uv, uv_da, grad_uv,
+    # grad_uv_da (bwd); texture streams: pyramid build (read T, write T/3),
+    # texels read by fwd and bwd (4T/3 each), gradient pyramid (zero T/3,
+    # texel gradients 4T/3, pyramid backward T/3 + grad_tex 2T)
+    nbytes = P * (8 + 16 + 16 + 16 + 8 + 16 + 8 + 16) + int(T * (1 + 1 / 3 + 8 / 3 + 1 / 3 + 4 / 3 + 1 / 3 + 2))
+    peak, _ = _peaks()
+    res = {"workload": WORKLOAD_TEX, "pixels_per_step": P, "value": P / ms / 1e3, "unit": UNIT, "ms_per_step": ms,
+           "step_bytes": nbytes, "step_roofline_frac": nbytes / (ms / 1e3) / 1e9 / peak,
+           "launches_per_step": g.launches_per_step}
+    if cpu:
+        import oracle as O
+        rows = 64
+        t_np, uv_np, da_np = tex0.cpu().numpy(), uv0[:, :rows].cpu().numpy(), da0[:, :rows].cpu().numpy()
+        g_np = gout[:, :rows].cpu().numpy()
+        L = O.tex_levels(1024, 1024)
+        t0 = time.perf_counter()
+        pyr = O.tex_mip_build(t_np, L)
+        O.tex_fwd(t_np, pyr, L, uv_np, da_np, "linear-mipmap-linear", "wrap")
+        g0, gp, _, _ = O.tex_bwd(t_np, pyr, L, uv_np, da_np, g_np, "linear-mipmap-linear", "wrap")
+        O.tex_mip_bwd(g0, gp, L)
+        el = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": rows * n / el / 1e6, "unit": UNIT, "cores": O.default_threads(),
+                               "kind": "port", "sample": "%d rows of the 1024x1024 output, fwd+bwd with the pyramid "
+                                                         "of the full texture, in %.2f s" % (rows, el)}
+    return res
+
+
 def run_sharded_views64(dev, steps, warmup, rank, world):
     """The 64-view workload sharded across ranks (strong scaling): each rank
     renders its share of the views (diffrp_gb300.replicas.shard_items) as one
@@ -1093,6 +1175,7 @@ def main():
                                  tile=(big["tile"].bit_length() - 1, big["threads_per_tri"]))
             big["stored_buffers"] = {"batched": stored["batched"], "peak_memory_gb": stored["peak_memory_gb"]}
             line["batched_large16"] = big
+            line["texture_trilinear"] = run_texture(dev, steps=k_small, warmup=W_, cpu=not args.no_cpu_baseline)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(verts_np, f, attr_np, mvp, target)
         if sharded is not None:

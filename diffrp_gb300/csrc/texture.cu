@@ -42,6 +42,7 @@ struct TexArgs {
     float* grad_pyr;
     float* grad_uv;
     float4* grad_uv_da;
+    int vec4;  // C == 4 with 16-byte aligned gradient levels: one float4 atomic per texel
 };
 
 __device__ __forceinline__ const float* tex_level(const TexArgs& a, const float* base0, const float* pyr, int k,
@@ -247,10 +248,50 @@ __global__ void __launch_bounds__(256) tex_fwd_kernel(TexArgs a) {
     }
 }
 
+// Adds v into *dst from every lane of the warp whose dst is the same
+// address: the lanes of one address (found with __match_any_sync) sum their
+// values by shuffles and one of them issues the atomic.  Under
+// minification thousands of pixels land on the same few texels of the
+// coarse levels; contended float atomics there serialise in L2.  dst ==
+// nullptr: nothing to add (the lane still takes part).
+__device__ __forceinline__ void warp_add(float* dst, float v, unsigned peers) {
+    float sum = 0.f;
+    unsigned rem = peers;
+    while (rem) {  // the group's lanes step through it together
+        const int src = __ffs(rem) - 1;
+        rem &= rem - 1;
+        sum += __shfl_sync(peers, v, src);
+    }
+    if (dst && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(dst, sum);
+}
+
+__device__ __forceinline__ void warp_add4(float4* dst, float4 v, unsigned peers) {
+    float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
+    unsigned rem = peers;
+    while (rem) {
+        const int src = __ffs(rem) - 1;
+        rem &= rem - 1;
+        sum.x += __shfl_sync(peers, v.x, src);
+        sum.y += __shfl_sync(peers, v.y, src);
+        sum.z += __shfl_sync(peers, v.z, src);
+        sum.w += __shfl_sync(peers, v.w, src);
+    }
+    if (dst && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(dst, sum);
+}
+
 __device__ __forceinline__ void bilin_bwd(const float* lvl, float* glvl, const Bilin& B, int w, int h, int C,
-                                          const float* g, float wl, float& gu, float& gv) {
+                                          bool vec4, const float* g, float wl, float& gu, float& gv) {
     const float fx = B.fx, fy = B.fy;
-    const float w00 = (1.f - fx) * (1.f - fy), w10 = fx * (1.f - fy), w01 = (1.f - fx) * fy, w11 = fx * fy;
+    const float wt[4] = {(1.f - fx) * (1.f - fy), fx * (1.f - fy), (1.f - fx) * fy, fx * fy};
+    const long long idx[4] = {B.i00, B.i10, B.i01, B.i11};
+    float* row[4];
+    unsigned peers[4];
+    const unsigned active = __activemask();
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        row[t] = idx[t] >= 0 ? glvl + idx[t] * C : nullptr;
+        peers[t] = __match_any_sync(active, reinterpret_cast<unsigned long long>(row[t]));
+    }
     float dx = 0.f, dy = 0.f;
     for (int c = 0; c < C; ++c) {
         const float gc = g[c] * wl;
@@ -258,10 +299,16 @@ __device__ __forceinline__ void bilin_bwd(const float* lvl, float* glvl, const B
         const float t01 = fetch(lvl, B.i01, C, c), t11 = fetch(lvl, B.i11, C, c);
         dx = fmaf(gc, fmaf(1.f - fy, t10 - t00, fy * (t11 - t01)), dx);
         dy = fmaf(gc, fmaf(fx, t11 - t01, t01) - fmaf(fx, t10 - t00, t00), dy);
-        if (B.i00 >= 0) atomicAdd(glvl + B.i00 * C + c, gc * w00);
-        if (B.i10 >= 0) atomicAdd(glvl + B.i10 * C + c, gc * w10);
-        if (B.i01 >= 0) atomicAdd(glvl + B.i01 * C + c, gc * w01);
-        if (B.i11 >= 0) atomicAdd(glvl + B.i11 * C + c, gc * w11);
+        if (vec4) continue;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) warp_add(row[t] ? row[t] + c : nullptr, gc * wt[t], peers[t]);
+    }
+    if (vec4) {
+        const float4 gc = make_float4(g[0] * wl, g[1] * wl, g[2] * wl, g[3] * wl);
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            warp_add4(reinterpret_cast<float4*>(row[t]),
+                      make_float4(gc.x * wt[t], gc.y * wt[t], gc.z * wt[t], gc.w * wt[t]), peers[t]);
     }
     gu = fmaf(dx, (float)w, gu);
     gv = fmaf(dy, (float)h, gv);
@@ -279,20 +326,21 @@ __global__ void __launch_bounds__(256) tex_bwd_kernel(TexArgs a) {
     if (a.filter == kTexNearest) {
         float* G0 = const_cast<float*>(tex_level(a, a.grad_tex, a.grad_pyr, 0, tn));
         const long long i = nearest_index(a, u, v);
-        if (i >= 0)
-            for (int c = 0; c < C; ++c) atomicAdd(G0 + i * C + c, g[c]);
+        float* row = i >= 0 ? G0 + i * C : nullptr;
+        const unsigned peers = __match_any_sync(__activemask(), reinterpret_cast<unsigned long long>(row));
+        for (int c = 0; c < C; ++c) warp_add(row ? row + c : nullptr, g[c], peers);
     } else {
         const TexLod L = tex_lod(a, p);
         const Bilin B0 = bilin_setup(u, v, a.lw[L.l0], a.lh[L.l0], a.boundary);
         const float* P0 = tex_level(a, a.tex, a.pyr, L.l0, tn);
         float* G0 = const_cast<float*>(tex_level(a, a.grad_tex, a.grad_pyr, L.l0, tn));
         const float f = L.f;
-        bilin_bwd(P0, G0, B0, a.lw[L.l0], a.lh[L.l0], C, g, f > 0.f ? 1.f - f : 1.f, gu, gv);
+        bilin_bwd(P0, G0, B0, a.lw[L.l0], a.lh[L.l0], C, a.vec4, g, f > 0.f ? 1.f - f : 1.f, gu, gv);
         if (f > 0.f) {
             const Bilin B1 = bilin_setup(u, v, a.lw[L.l1], a.lh[L.l1], a.boundary);
             const float* P1 = tex_level(a, a.tex, a.pyr, L.l1, tn);
             float* G1 = const_cast<float*>(tex_level(a, a.grad_tex, a.grad_pyr, L.l1, tn));
-            bilin_bwd(P1, G1, B1, a.lw[L.l1], a.lh[L.l1], C, g, f, gu, gv);
+            bilin_bwd(P1, G1, B1, a.lw[L.l1], a.lh[L.l1], C, a.vec4, g, f, gu, gv);
             if (a.grad_uv_da && L.interior) {
                 float dl = 0.f;
                 for (int c = 0; c < C; ++c) dl = fmaf(g[c], bilin_value(P1, B1, C, c) - bilin_value(P0, B0, C, c), dl);
@@ -464,6 +512,8 @@ DRP_API int drp_texture_bwd(const float* tex, const float* pyr, int num_tex, int
     a.grad_out = grad_out;
     a.grad_tex = grad_tex;
     a.grad_pyr = grad_pyr;
+    a.vec4 = channels == 4 && (reinterpret_cast<uintptr_t>(grad_tex) & 15) == 0 &&
+             (reinterpret_cast<uintptr_t>(grad_pyr) & 15) == 0;
     a.grad_uv = grad_uv;
     a.grad_uv_da = reinterpret_cast<float4*>(grad_uv_da);
     if (a.npix > 0) {
