@@ -42,7 +42,9 @@ struct TexArgs {
     float* grad_pyr;
     float* grad_uv;
     float4* grad_uv_da;
-    int vec4;  // C == 4 with 16-byte aligned gradient levels: one float4 atomic per texel
+    // C == 4 with every texel and pixel buffer of the call 16-byte aligned:
+    // float4 loads, stores and atomics
+    int vec4;
 };
 
 __device__ __forceinline__ const float* tex_level(const TexArgs& a, const float* base0, const float* pyr, int k,
@@ -124,7 +126,8 @@ __device__ __forceinline__ int wrap_index(int i, int n) {
     return r < 0 ? r + n : r;
 }
 
-__device__ __forceinline__ long long texel_index(int x, int y, int w, int h, int boundary) {
+// Texel index within its level (textures are at most 2^15 texels a side), or -1.
+__device__ __forceinline__ int texel_index(int x, int y, int w, int h, int boundary) {
     if (boundary == kTexWrap) {
         x = wrap_index(x, w);
         y = wrap_index(y, h);
@@ -134,7 +137,7 @@ __device__ __forceinline__ long long texel_index(int x, int y, int w, int h, int
     } else if (x < 0 || x >= w || y < 0 || y >= h) {
         return -1;
     }
-    return (long long)y * w + x;
+    return y * w + x;
 }
 
 __device__ __forceinline__ float tex_coord(float u, int size) {
@@ -146,7 +149,7 @@ __device__ __forceinline__ float tex_coord(float u, int size) {
 }
 
 struct Bilin {
-    long long i00, i10, i01, i11;
+    int i00, i10, i01, i11;
     float fx, fy;
 };
 
@@ -164,63 +167,102 @@ __device__ __forceinline__ Bilin bilin_setup(float u, float v, int w, int h, int
     return B;
 }
 
-__device__ __forceinline__ float fetch(const float* lvl, long long i, int C, int c) {
-    return i < 0 ? 0.f : __ldg(lvl + i * C + c);
+__device__ __forceinline__ float fetch(const float* lvl, int i, int C, int c) {
+    return i < 0 ? 0.f : __ldg(lvl + (long long)i * C + c);
 }
 
-__device__ __forceinline__ float bilin_value(const float* lvl, const Bilin& B, int C, int c) {
-    const float t00 = fetch(lvl, B.i00, C, c), t10 = fetch(lvl, B.i10, C, c);
-    const float t01 = fetch(lvl, B.i01, C, c), t11 = fetch(lvl, B.i11, C, c);
+__device__ __forceinline__ float4 fetch4(const float* lvl, int i) {
+    return i < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : __ldg(reinterpret_cast<const float4*>(lvl) + i);
+}
+
+__device__ __forceinline__ float bilerp(const Bilin& B, float t00, float t10, float t01, float t11) {
     const float r0 = fmaf(B.fx, t10 - t00, t00), r1 = fmaf(B.fx, t11 - t01, t01);
     return fmaf(B.fy, r1 - r0, r0);
 }
 
-__device__ __forceinline__ long long nearest_index(const TexArgs& a, float u, float v) {
+__device__ __forceinline__ float bilin_value(const float* lvl, const Bilin& B, int C, int c) {
+    return bilerp(B, fetch(lvl, B.i00, C, c), fetch(lvl, B.i10, C, c), fetch(lvl, B.i01, C, c),
+                  fetch(lvl, B.i11, C, c));
+}
+
+// The four texels of a bilinear tap, four channels each.
+struct Quad {
+    float4 t00, t10, t01, t11;
+};
+
+__device__ __forceinline__ Quad fetch_quad(const float* lvl, const Bilin& B) {
+    return Quad{fetch4(lvl, B.i00), fetch4(lvl, B.i10), fetch4(lvl, B.i01), fetch4(lvl, B.i11)};
+}
+
+__device__ __forceinline__ float4 bilerp4(const Bilin& B, const Quad& q) {
+    return make_float4(bilerp(B, q.t00.x, q.t10.x, q.t01.x, q.t11.x), bilerp(B, q.t00.y, q.t10.y, q.t01.y, q.t11.y),
+                       bilerp(B, q.t00.z, q.t10.z, q.t01.z, q.t11.z), bilerp(B, q.t00.w, q.t10.w, q.t01.w, q.t11.w));
+}
+
+__device__ __forceinline__ int nearest_index(const TexArgs& a, float u, float v) {
     const int ix = (int)floorf(tex_coord(u, a.W) + 0.5f), iy = (int)floorf(tex_coord(v, a.H) + 0.5f);
     return texel_index(ix, iy, a.W, a.H, a.boundary);
 }
 
-// Level k of every texture from level k - 1: the 2x2 box average, indices
-// clamped to level k - 1.
-__global__ void __launch_bounds__(256) tex_mip_level_kernel(const float* __restrict__ src, float* __restrict__ dst,
-                                                            int Nt, int hp, int wp, int hk, int wk, int C) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long per = (long long)hk * wk;
-    if (i >= (long long)Nt * per) return;
-    const int n = (int)(i / per);
-    const int r = (int)(i - (long long)n * per);
-    const int y = r / wk, x = r - y * wk;
-    const int x0 = 2 * x < wp - 1 ? 2 * x : wp - 1, x1 = 2 * x + 1 < wp - 1 ? 2 * x + 1 : wp - 1;
-    const int y0 = 2 * y < hp - 1 ? 2 * y : hp - 1, y1 = 2 * y + 1 < hp - 1 ? 2 * y + 1 : hp - 1;
-    const float* s = src + (long long)n * hp * wp * C;
-    float* d = dst + (long long)n * per * C + (long long)r * C;
-    for (int c = 0; c < C; ++c) {
-        const float pa = s[((long long)y0 * wp + x0) * C + c], pb = s[((long long)y0 * wp + x1) * C + c];
-        const float pc = s[((long long)y1 * wp + x0) * C + c], pd = s[((long long)y1 * wp + x1) * C + c];
-        d[c] = (((pa + pb) + pc) + pd) * 0.25f;
+// Levels base + 1 .. base + nl of every texture from level base.  Level k
+// texel (x, y) is the 2x2 box average (((a + b) + c) + d) / 4 of level k - 1
+// at x0 = 2x, x1 = 2x + 1, y0 = 2y, y1 = 2y + 1, indices clamped to level
+// k - 1.  One CTA builds a side x side tile of level base + 1 and the tiles
+// above it (side / 2, side / 4, ...), each level from the one below in shared
+// memory (a tile's parents lie in the tile below it), writing every level to
+// the pyramid: the same values as one pass per level, in one launch.
+__global__ void __launch_bounds__(256) tex_mip_tile_kernel(TexArgs a, int base, int nl, int side, int tiles_x,
+                                                           int tiles_y) {
+    extern __shared__ float4 sm4[];
+    float* sm = reinterpret_cast<float*>(sm4);
+    const int C = a.C;
+    const int per = tiles_x * tiles_y;
+    const int n = blockIdx.x / per;
+    const int rr = blockIdx.x - n * per;
+    const int ty = rr / tiles_x, tx = rr - ty * tiles_x;
+    const float* src = tex_level(a, a.tex, a.pyr, base, n);
+    int pw = a.lw[base], ph = a.lh[base];
+    int prev_off = 0, prev_side = 0, off = 0;
+    for (int s = 0; s < nl; ++s) {
+        const int k = base + 1 + s;
+        const int T = side >> s, w = a.lw[k], h = a.lh[k];
+        const int ox = tx * T, oy = ty * T;
+        float* dst = const_cast<float*>(tex_level(a, a.pyr, a.pyr, k, n));
+        for (int t = threadIdx.x; t < T * T; t += blockDim.x) {
+            const int ly = t / T, lx = t - ly * T;
+            const int x = ox + lx, y = oy + ly;
+            if (x >= w || y >= h) continue;
+            const int x0 = 2 * x < pw - 1 ? 2 * x : pw - 1, x1 = 2 * x + 1 < pw - 1 ? 2 * x + 1 : pw - 1;
+            const int y0 = 2 * y < ph - 1 ? 2 * y : ph - 1, y1 = 2 * y + 1 < ph - 1 ? 2 * y + 1 : ph - 1;
+            for (int c = 0; c < C; ++c) {
+                float pa, pb, pc, pd;
+                if (s == 0) {
+                    pa = src[((long long)y0 * pw + x0) * C + c];
+                    pb = src[((long long)y0 * pw + x1) * C + c];
+                    pc = src[((long long)y1 * pw + x0) * C + c];
+                    pd = src[((long long)y1 * pw + x1) * C + c];
+                } else {  // the tile below starts at (2 ox, 2 oy)
+                    const float* q = sm + prev_off;
+                    pa = q[((y0 - 2 * oy) * prev_side + (x0 - 2 * ox)) * C + c];
+                    pb = q[((y0 - 2 * oy) * prev_side + (x1 - 2 * ox)) * C + c];
+                    pc = q[((y1 - 2 * oy) * prev_side + (x0 - 2 * ox)) * C + c];
+                    pd = q[((y1 - 2 * oy) * prev_side + (x1 - 2 * ox)) * C + c];
+                }
+                const float v = (((pa + pb) + pc) + pd) * 0.25f;
+                dst[((long long)y * w + x) * C + c] = v;
+                if (s + 1 < nl) sm[off + (ly * T + lx) * C + c] = v;
+            }
+        }
+        __syncthreads();
+        prev_off = off;
+        prev_side = T;
+        off += T * T * C;
+        pw = w;
+        ph = h;
     }
 }
 
-// Pyramid backward, level k into level k - 1 (gather): texel (x, y) of level
-// k - 1 receives 0.25 of texel (x >> 1, y >> 1) of level k, twice along an
-// axis of size 1.
-__global__ void __launch_bounds__(256) tex_mip_bwd_kernel(const float* __restrict__ src, float* __restrict__ dst,
-                                                          int Nt, int hp, int wp, int hk, int wk, int C) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long per = (long long)hp * wp;
-    if (i >= (long long)Nt * per) return;
-    const int n = (int)(i / per);
-    const int r = (int)(i - (long long)n * per);
-    const int y = r / wp, x = r - y * wp;
-    const int cx = x >> 1, cy = y >> 1;
-    if (cx >= wk || cy >= hk) return;
-    const float mx = wp == 1 ? 2.f : 1.f, my = hp == 1 ? 2.f : 1.f;
-    const float* s = src + (long long)n * hk * wk * C + ((long long)cy * wk + cx) * C;
-    float* d = dst + (long long)n * per * C + (long long)r * C;
-    for (int c = 0; c < C; ++c) d[c] += (0.25f * mx) * my * s[c];
-}
-
-__global__ void __launch_bounds__(256) tex_fwd_kernel(TexArgs a) {
+__global__ void __launch_bounds__(256, 3) tex_fwd_kernel(TexArgs a) {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= a.npix) return;
     const int n = (int)(p / a.view_pix), tn = a.Nt == 1 ? 0 : n;
@@ -229,13 +271,24 @@ __global__ void __launch_bounds__(256) tex_fwd_kernel(TexArgs a) {
     float* o = a.out + p * C;
     if (a.filter == kTexNearest) {
         const float* l0 = tex_level(a, a.tex, a.pyr, 0, tn);
-        const long long i = nearest_index(a, u, v);
+        const int i = nearest_index(a, u, v);
         for (int c = 0; c < C; ++c) o[c] = fetch(l0, i, C, c);
         return;
     }
     const TexLod L = tex_lod(a, p);
     const Bilin B0 = bilin_setup(u, v, a.lw[L.l0], a.lh[L.l0], a.boundary);
     const float* v0 = tex_level(a, a.tex, a.pyr, L.l0, tn);
+    if (a.vec4) {  // the same arithmetic per channel, one load per texel
+        float4 r = bilerp4(B0, fetch_quad(v0, B0));
+        if (L.f > 0.f) {
+            const Bilin B1 = bilin_setup(u, v, a.lw[L.l1], a.lh[L.l1], a.boundary);
+            const float4 s1 = bilerp4(B1, fetch_quad(tex_level(a, a.tex, a.pyr, L.l1, tn), B1));
+            r = make_float4(fmaf(L.f, s1.x - r.x, r.x), fmaf(L.f, s1.y - r.y, r.y), fmaf(L.f, s1.z - r.z, r.z),
+                            fmaf(L.f, s1.w - r.w, r.w));
+        }
+        reinterpret_cast<float4*>(a.out)[p] = r;
+        return;
+    }
     if (L.f > 0.f) {
         const Bilin B1 = bilin_setup(u, v, a.lw[L.l1], a.lh[L.l1], a.boundary);
         const float* v1 = tex_level(a, a.tex, a.pyr, L.l1, tn);
@@ -248,50 +301,58 @@ __global__ void __launch_bounds__(256) tex_fwd_kernel(TexArgs a) {
     }
 }
 
-// Adds v into *dst from every lane of the warp whose dst is the same
-// address: the lanes of one address (found with __match_any_sync) sum their
-// values by shuffles and one of them issues the atomic.  Under
-// minification thousands of pixels land on the same few texels of the
-// coarse levels; contended float atomics there serialise in L2.  dst ==
-// nullptr: nothing to add (the lane still takes part).
-__device__ __forceinline__ void warp_add(float* dst, float v, unsigned peers) {
-    float sum = 0.f;
-    unsigned rem = peers;
-    while (rem) {  // the group's lanes step through it together
-        const int src = __ffs(rem) - 1;
-        rem &= rem - 1;
-        sum += __shfl_sync(peers, v, src);
+// Sum of v over this lane's group (the lanes of `peers`, all of `active`
+// taking part), left in the group's lowest lane: pointer jumping along the
+// group in lane order, ceil(log2(largest group)) rounds of shuffles instead of
+// one per member.  Under minification thousands of pixels land on the same
+// few texels of the coarse levels, so groups are large.
+template <int N>
+__device__ __forceinline__ void group_sum(float (&v)[N], unsigned peers, unsigned active) {
+    const int lane = threadIdx.x & 31;
+    const unsigned after = lane == 31 ? 0u : peers & (~0u << (lane + 1));
+    int next = after ? __ffs(after) - 1 : -1;
+    const int largest = __reduce_max_sync(active, (unsigned)__popc(peers));
+    const int rounds = largest <= 1 ? 0 : 32 - __clz(largest - 1);
+    for (int r = 0; r < rounds; ++r) {
+        const int src = next >= 0 ? next : lane;
+        float o[N];
+#pragma unroll
+        for (int c = 0; c < N; ++c) o[c] = __shfl_sync(active, v[c], src);
+        const int nn = __shfl_sync(active, next, src);
+        if (next >= 0) {
+#pragma unroll
+            for (int c = 0; c < N; ++c) v[c] += o[c];
+            next = nn;
+        }
     }
-    if (dst && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(dst, sum);
 }
 
-__device__ __forceinline__ void warp_add4(float4* dst, float4 v, unsigned peers) {
-    float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
-    unsigned rem = peers;
-    while (rem) {
-        const int src = __ffs(rem) - 1;
-        rem &= rem - 1;
-        sum.x += __shfl_sync(peers, v.x, src);
-        sum.y += __shfl_sync(peers, v.y, src);
-        sum.z += __shfl_sync(peers, v.z, src);
-        sum.w += __shfl_sync(peers, v.w, src);
+// Adds v (N consecutive floats; N == 4: a 16-byte aligned float4) into dst
+// from every lane of the warp whose dst is the same address: one atomic per
+// group, issued by its lowest lane.  nullptr: nothing to add (the lane still
+// takes part).
+template <int N>
+__device__ __forceinline__ void warp_add(float* dst, float (&v)[N], unsigned active) {
+    const unsigned peers = __match_any_sync(active, reinterpret_cast<unsigned long long>(dst));
+    group_sum<N>(v, peers, active);
+    if (!dst || (threadIdx.x & 31) != __ffs(peers) - 1) return;
+    if constexpr (N == 4) {
+        atomicAdd(reinterpret_cast<float4*>(dst), make_float4(v[0], v[1], v[2], v[3]));
+    } else {
+        atomicAdd(dst, v[0]);
     }
-    if (dst && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(dst, sum);
+}
+
+__device__ __forceinline__ float* grad_level(const TexArgs& a, int k, int n) {
+    return const_cast<float*>(tex_level(a, a.grad_tex, a.grad_pyr, k, n));
 }
 
 __device__ __forceinline__ void bilin_bwd(const float* lvl, float* glvl, const Bilin& B, int w, int h, int C,
-                                          bool vec4, const float* g, float wl, float& gu, float& gv) {
+                                          const float* g, float wl, float& gu, float& gv) {
     const float fx = B.fx, fy = B.fy;
     const float wt[4] = {(1.f - fx) * (1.f - fy), fx * (1.f - fy), (1.f - fx) * fy, fx * fy};
-    const long long idx[4] = {B.i00, B.i10, B.i01, B.i11};
-    float* row[4];
-    unsigned peers[4];
+    const int idx[4] = {B.i00, B.i10, B.i01, B.i11};
     const unsigned active = __activemask();
-#pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        row[t] = idx[t] >= 0 ? glvl + idx[t] * C : nullptr;
-        peers[t] = __match_any_sync(active, reinterpret_cast<unsigned long long>(row[t]));
-    }
     float dx = 0.f, dy = 0.f;
     for (int c = 0; c < C; ++c) {
         const float gc = g[c] * wl;
@@ -299,22 +360,46 @@ __device__ __forceinline__ void bilin_bwd(const float* lvl, float* glvl, const B
         const float t01 = fetch(lvl, B.i01, C, c), t11 = fetch(lvl, B.i11, C, c);
         dx = fmaf(gc, fmaf(1.f - fy, t10 - t00, fy * (t11 - t01)), dx);
         dy = fmaf(gc, fmaf(fx, t11 - t01, t01) - fmaf(fx, t10 - t00, t00), dy);
-        if (vec4) continue;
 #pragma unroll
-        for (int t = 0; t < 4; ++t) warp_add(row[t] ? row[t] + c : nullptr, gc * wt[t], peers[t]);
-    }
-    if (vec4) {
-        const float4 gc = make_float4(g[0] * wl, g[1] * wl, g[2] * wl, g[3] * wl);
-#pragma unroll
-        for (int t = 0; t < 4; ++t)
-            warp_add4(reinterpret_cast<float4*>(row[t]),
-                      make_float4(gc.x * wt[t], gc.y * wt[t], gc.z * wt[t], gc.w * wt[t]), peers[t]);
+        for (int t = 0; t < 4; ++t) {
+            float val[1] = {gc * wt[t]};
+            warp_add<1>(idx[t] >= 0 ? glvl + (long long)idx[t] * C + c : nullptr, val, active);
+        }
     }
     gu = fmaf(dx, (float)w, gu);
     gv = fmaf(dy, (float)h, gv);
 }
 
-__global__ void __launch_bounds__(256) tex_bwd_kernel(TexArgs a) {
+// bilin_bwd of four channels from one float4 load per texel (the same
+// arithmetic per channel); q: the texels, for the level-of-detail gradient.
+__device__ __forceinline__ void bilin_bwd4(const Quad& q, float* glvl, const Bilin& B, int w, int h, float4 g4,
+                                           float wl, float& gu, float& gv) {
+    const float fx = B.fx, fy = B.fy;
+    const float wt[4] = {(1.f - fx) * (1.f - fy), fx * (1.f - fy), (1.f - fx) * fy, fx * fy};
+    const int idx[4] = {B.i00, B.i10, B.i01, B.i11};
+    const unsigned active = __activemask();
+    const float gc[4] = {g4.x * wl, g4.y * wl, g4.z * wl, g4.w * wl};
+    const float a00[4] = {q.t00.x, q.t00.y, q.t00.z, q.t00.w}, a10[4] = {q.t10.x, q.t10.y, q.t10.z, q.t10.w};
+    const float a01[4] = {q.t01.x, q.t01.y, q.t01.z, q.t01.w}, a11[4] = {q.t11.x, q.t11.y, q.t11.z, q.t11.w};
+    float dx = 0.f, dy = 0.f;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const float t00 = a00[c], t10 = a10[c], t01 = a01[c], t11 = a11[c];
+        dx = fmaf(gc[c], fmaf(1.f - fy, t10 - t00, fy * (t11 - t01)), dx);
+        dy = fmaf(gc[c], fmaf(fx, t11 - t01, t01) - fmaf(fx, t10 - t00, t00), dy);
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        float val[4] = {gc[0] * wt[t], gc[1] * wt[t], gc[2] * wt[t], gc[3] * wt[t]};
+        warp_add<4>(idx[t] >= 0 ? glvl + (long long)idx[t] * 4 : nullptr, val, active);
+    }
+    gu = fmaf(dx, (float)w, gu);
+    gv = fmaf(dy, (float)h, gv);
+}
+
+// One pixel's gradients: texel gradients added into the levels, the uv and
+// uv_da gradients written.
+__global__ void __launch_bounds__(256, 3) tex_bwd_kernel(TexArgs a) {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= a.npix) return;
     const int n = (int)(p / a.view_pix), tn = a.Nt == 1 ? 0 : n;
@@ -324,41 +409,140 @@ __global__ void __launch_bounds__(256) tex_bwd_kernel(TexArgs a) {
     float gu = 0.f, gv = 0.f;
     float4 gda = make_float4(0.f, 0.f, 0.f, 0.f);
     if (a.filter == kTexNearest) {
-        float* G0 = const_cast<float*>(tex_level(a, a.grad_tex, a.grad_pyr, 0, tn));
-        const long long i = nearest_index(a, u, v);
-        float* row = i >= 0 ? G0 + i * C : nullptr;
-        const unsigned peers = __match_any_sync(__activemask(), reinterpret_cast<unsigned long long>(row));
-        for (int c = 0; c < C; ++c) warp_add(row ? row + c : nullptr, g[c], peers);
+        float* G0 = grad_level(a, 0, tn);
+        const int i = nearest_index(a, u, v);
+        const unsigned active = __activemask();
+        for (int c = 0; c < C; ++c) {
+            float val[1] = {g[c]};
+            warp_add<1>(i >= 0 ? G0 + (long long)i * C + c : nullptr, val, active);
+        }
     } else {
         const TexLod L = tex_lod(a, p);
         const Bilin B0 = bilin_setup(u, v, a.lw[L.l0], a.lh[L.l0], a.boundary);
         const float* P0 = tex_level(a, a.tex, a.pyr, L.l0, tn);
-        float* G0 = const_cast<float*>(tex_level(a, a.grad_tex, a.grad_pyr, L.l0, tn));
         const float f = L.f;
-        bilin_bwd(P0, G0, B0, a.lw[L.l0], a.lh[L.l0], C, a.vec4, g, f > 0.f ? 1.f - f : 1.f, gu, gv);
-        if (f > 0.f) {
-            const Bilin B1 = bilin_setup(u, v, a.lw[L.l1], a.lh[L.l1], a.boundary);
-            const float* P1 = tex_level(a, a.tex, a.pyr, L.l1, tn);
-            float* G1 = const_cast<float*>(tex_level(a, a.grad_tex, a.grad_pyr, L.l1, tn));
-            bilin_bwd(P1, G1, B1, a.lw[L.l1], a.lh[L.l1], C, a.vec4, g, f, gu, gv);
-            if (a.grad_uv_da && L.interior) {
-                float dl = 0.f;
-                for (int c = 0; c < C; ++c) dl = fmaf(g[c], bilin_value(P1, B1, C, c) - bilin_value(P0, B0, C, c), dl);
-                // lambda = 0.5 log2(r2): d lambda / d r2 = 0.5 / (r2 ln 2)
-                const float dr2 = dl * (0.72134752f / L.r2);
-                if (L.use_x) {
-                    gda.x = dr2 * 2.f * L.ax * (float)a.W;
-                    gda.z = dr2 * 2.f * L.ay * (float)a.H;
-                } else {
-                    gda.y = dr2 * 2.f * L.bx * (float)a.W;
-                    gda.w = dr2 * 2.f * L.by * (float)a.H;
+        float dl = 0.f;  // d out / d lambda . grad_out
+        if (a.vec4) {
+            const float4 g4 = reinterpret_cast<const float4*>(a.grad_out)[p];
+            const Quad q0 = fetch_quad(P0, B0);
+            bilin_bwd4(q0, grad_level(a, L.l0, tn), B0, a.lw[L.l0], a.lh[L.l0], g4, f > 0.f ? 1.f - f : 1.f, gu, gv);
+            if (f > 0.f) {
+                const Bilin B1 = bilin_setup(u, v, a.lw[L.l1], a.lh[L.l1], a.boundary);
+                const Quad q1 = fetch_quad(tex_level(a, a.tex, a.pyr, L.l1, tn), B1);
+                bilin_bwd4(q1, grad_level(a, L.l1, tn), B1, a.lw[L.l1], a.lh[L.l1], g4, f, gu, gv);
+                if (a.grad_uv_da && L.interior) {
+                    const float4 s0 = bilerp4(B0, q0), s1 = bilerp4(B1, q1);
+                    dl = fmaf(g4.x, s1.x - s0.x, dl);
+                    dl = fmaf(g4.y, s1.y - s0.y, dl);
+                    dl = fmaf(g4.z, s1.z - s0.z, dl);
+                    dl = fmaf(g4.w, s1.w - s0.w, dl);
                 }
+            }
+        } else {
+            bilin_bwd(P0, grad_level(a, L.l0, tn), B0, a.lw[L.l0], a.lh[L.l0], C, g, f > 0.f ? 1.f - f : 1.f, gu,
+                      gv);
+            if (f > 0.f) {
+                const Bilin B1 = bilin_setup(u, v, a.lw[L.l1], a.lh[L.l1], a.boundary);
+                const float* P1 = tex_level(a, a.tex, a.pyr, L.l1, tn);
+                bilin_bwd(P1, grad_level(a, L.l1, tn), B1, a.lw[L.l1], a.lh[L.l1], C, g, f, gu, gv);
+                if (a.grad_uv_da && L.interior)
+                    for (int c = 0; c < C; ++c)
+                        dl = fmaf(g[c], bilin_value(P1, B1, C, c) - bilin_value(P0, B0, C, c), dl);
+            }
+        }
+        if (f > 0.f && a.grad_uv_da && L.interior) {
+            // lambda = 0.5 log2(r2): d lambda / d r2 = 0.5 / (r2 ln 2)
+            const float dr2 = dl * (0.72134752f / L.r2);
+            if (L.use_x) {
+                gda.x = dr2 * 2.f * L.ax * (float)a.W;
+                gda.z = dr2 * 2.f * L.ay * (float)a.H;
+            } else {
+                gda.y = dr2 * 2.f * L.bx * (float)a.W;
+                gda.w = dr2 * 2.f * L.by * (float)a.H;
             }
         }
     }
     a.grad_uv[2 * p] = gu;
     a.grad_uv[2 * p + 1] = gv;
     if (a.grad_uv_da) a.grad_uv_da[p] = gda;
+}
+
+__device__ __forceinline__ float vadd(float a, float b) { return a + b; }
+__device__ __forceinline__ float vscale(float m, float t) { return m * t; }
+__device__ __forceinline__ float4 vadd(float4 a, float4 b) {
+    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+__device__ __forceinline__ float4 vscale(float m, float4 t) { return make_float4(m * t.x, m * t.y, m * t.z, m * t.w); }
+
+constexpr int kTexMaxChain = 15;  // pyramid levels above level 0 of a texture of at most 2^15 texels a side
+
+// The cascade of one channel group (V: float or float4) of level-1 texel
+// (x1, y1): every level's load issued first (levels above the top read the
+// top again; registers only), then the evaluation from the top.
+template <typename V>
+__device__ __forceinline__ V mip_chain(const TexArgs& a, int n, int x1, int y1, int top, int c) {
+    V g[kTexMaxChain];
+#pragma unroll
+    for (int k = 1; k <= kTexMaxChain; ++k) {  // level k holds (x1, y1)'s ancestor (x1 >> (k - 1), y1 >> (k - 1))
+        const int j = k < top ? k : top;
+        const float* G = a.grad_pyr + a.lofs[j] + (long long)n * a.lh[j] * a.lw[j] * a.C;
+        g[k - 1] = *reinterpret_cast<const V*>(G + ((long long)(y1 >> (j - 1)) * a.lw[j] + (x1 >> (j - 1))) * a.C + c);
+    }
+    V t = g[0];
+#pragma unroll
+    for (int k = kTexMaxChain; k >= 1; --k) {
+        if (k > top) continue;
+        if (k == top) {
+            t = g[k - 1];
+        } else {
+            const float m = (0.25f * (a.lw[k] == 1 ? 2.f : 1.f)) * (a.lh[k] == 1 ? 2.f : 1.f);
+            t = vadd(g[k - 1], vscale(m, t));
+        }
+    }
+    return t;
+}
+
+// Pyramid backward in one pass: texel (x, y) of level k - 1 receives 0.25 of
+// texel (x >> 1, y >> 1) of level k (twice along an axis of size 1; nothing
+// beyond twice level k's size), after level k has received its own share
+// from level k + 1.  One thread per level-1 texel follows its chain of
+// parents and evaluates that cascade from the top (t_{k-1} = G_{k-1} +
+// c_{k-1} t_k, the operations of one pass per level in the same order), then
+// adds c_0 t_1 into the gradients of its (up to) four level-0 texels.
+__global__ void __launch_bounds__(256) tex_mip_chain_kernel(TexArgs a) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int w1 = a.lw[1], h1 = a.lh[1];
+    const long long per = (long long)h1 * w1;
+    if (i >= (long long)a.Nt * per) return;
+    const int n = (int)(i / per);
+    const int r = (int)(i - (long long)n * per);
+    const int y1 = r / w1, x1 = r - y1 * w1;
+    int top = 1;  // the highest level of the chain
+    while (top + 1 < a.levels && (x1 >> top) < a.lw[top + 1] && (y1 >> top) < a.lh[top + 1]) ++top;
+    const float m = (0.25f * (a.W == 1 ? 2.f : 1.f)) * (a.H == 1 ? 2.f : 1.f);
+    const int C = a.C;
+    float* g0 = a.grad_tex + (long long)n * a.H * a.W * C;
+    if (a.vec4) {
+        const float4 t = vscale(m, mip_chain<float4>(a, n, x1, y1, top, 0));
+        for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx) {
+                const int x = 2 * x1 + dx, y = 2 * y1 + dy;
+                if (x >= a.W || y >= a.H) continue;
+                float4* d = reinterpret_cast<float4*>(g0) + (long long)y * a.W + x;
+                *d = vadd(*d, t);
+            }
+    } else {
+        for (int c = 0; c < C; ++c) {
+            const float t = m * mip_chain<float>(a, n, x1, y1, top, c);
+            for (int dy = 0; dy < 2; ++dy)
+                for (int dx = 0; dx < 2; ++dx) {
+                    const int x = 2 * x1 + dx, y = 2 * y1 + dy;
+                    if (x >= a.W || y >= a.H) continue;
+                    float* d = g0 + ((long long)y * a.W + x) * C + c;
+                    *d = *d + t;
+                }
+        }
+    }
 }
 
 // The texture's level table (sizes, pyramid offsets) after checking its
@@ -426,6 +610,8 @@ static int tex_setup(TexArgs& a, const char* who, const float* tex, const float*
 
 #define DRP_API extern "C" __attribute__((visibility("default")))
 
+static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
 DRP_API int drp_texture_levels(int height, int width, int max_mip_level, int* levels) {
     if (!levels || height < 1 || width < 1) {
         drp_set_last_error("drp_texture_levels: bad arguments");
@@ -464,11 +650,26 @@ DRP_API int drp_texture_mip_build(const float* tex, int num_tex, int height, int
     int st = drp::tex_levels_setup(a, "drp_texture_mip_build", tex, pyr, num_tex, height, width, channels, levels);
     if (st) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    for (int k = 1; k < levels; ++k) {
-        const float* src = k == 1 ? tex : pyr + a.lofs[k - 1];
-        const long long n = (long long)num_tex * a.lh[k] * a.lw[k];
-        drp::tex_mip_level_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
-            src, pyr + a.lofs[k], num_tex, a.lh[k - 1], a.lw[k - 1], a.lh[k], a.lw[k], channels);
+    // tile side: 16 texels, less where the tiles of C channels exceed 48 KB
+    int side = 16, per_launch = 5;
+    while (side > 1 && (size_t)side * side * 2 * channels * sizeof(float) > (48u << 10)) {
+        side >>= 1;
+        --per_launch;
+    }
+    if ((size_t)side * side * 2 * channels * sizeof(float) > (48u << 10)) {
+        drp_set_last_error("drp_texture_mip_build: more than 6144 channels");
+        return DRP_STATUS_INVALID_ARGUMENT;
+    }
+    for (int base = 0; base + 1 < levels; base += per_launch) {
+        const int nl = levels - 1 - base < per_launch ? levels - 1 - base : per_launch;
+        const int tiles_x = (a.lw[base + 1] + side - 1) / side, tiles_y = (a.lh[base + 1] + side - 1) / side;
+        const long long blocks = (long long)num_tex * tiles_x * tiles_y;
+        if (blocks > 0x7fffffff) {
+            drp_set_last_error("drp_texture_mip_build: too many textures");
+            return DRP_STATUS_INVALID_ARGUMENT;
+        }
+        const size_t smem = (size_t)side * side * 2 * channels * sizeof(float);  // the tiles above the first
+        drp::tex_mip_tile_kernel<<<(unsigned)blocks, 256, smem, s>>>(a, base, nl, side, tiles_x, tiles_y);
         drp_note_launch();
     }
     return drp_check_launch("drp_texture_mip_build");
@@ -487,6 +688,7 @@ DRP_API int drp_texture_fwd(const float* tex, const float* pyr, int num_tex, int
     }
     if (a.npix == 0) return DRP_STATUS_OK;
     a.out = out;
+    a.vec4 = channels == 4 && aligned16(tex) && aligned16(pyr) && aligned16(out);
     drp::tex_fwd_kernel<<<(unsigned)((a.npix + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(a);
     drp_note_launch();
     return drp_check_launch("drp_texture_fwd");
@@ -512,19 +714,17 @@ DRP_API int drp_texture_bwd(const float* tex, const float* pyr, int num_tex, int
     a.grad_out = grad_out;
     a.grad_tex = grad_tex;
     a.grad_pyr = grad_pyr;
-    a.vec4 = channels == 4 && (reinterpret_cast<uintptr_t>(grad_tex) & 15) == 0 &&
-             (reinterpret_cast<uintptr_t>(grad_pyr) & 15) == 0;
+    a.vec4 = channels == 4 && aligned16(tex) && aligned16(pyr) && aligned16(grad_out) && aligned16(grad_tex) &&
+             aligned16(grad_pyr);
     a.grad_uv = grad_uv;
     a.grad_uv_da = reinterpret_cast<float4*>(grad_uv_da);
     if (a.npix > 0) {
         drp::tex_bwd_kernel<<<(unsigned)((a.npix + 255) / 256), 256, 0, s>>>(a);
         drp_note_launch();
     }
-    for (int k = levels - 1; k >= 1; --k) {
-        float* dst = k == 1 ? grad_tex : grad_pyr + a.lofs[k - 1];
-        const long long n = (long long)num_tex * a.lh[k - 1] * a.lw[k - 1];
-        drp::tex_mip_bwd_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
-            grad_pyr + a.lofs[k], dst, num_tex, a.lh[k - 1], a.lw[k - 1], a.lh[k], a.lw[k], channels);
+    if (levels > 1 && a.filter >= drp::kTexMipNearest) {
+        const long long n = (long long)num_tex * a.lh[1] * a.lw[1];
+        drp::tex_mip_chain_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
         drp_note_launch();
     }
     return drp_check_launch("drp_texture_bwd");

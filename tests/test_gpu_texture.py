@@ -62,12 +62,18 @@ def test_forward_bit_exact(cuda_lib, filter_mode, boundary, Nt):
     np.testing.assert_array_equal(got.cpu().numpy(), ref)
 
 
+# (textures, H, W, C): four channels take the float4 path; odd sizes, a
+# size-1 axis and per-view textures the per-channel one
+GRAD_SHAPES = [(1, 32, 24, 4), (2, 37, 53, 3), (1, 1, 9, 2), (2, 20, 44, 4)]
+
+
+@pytest.mark.parametrize("shape", GRAD_SHAPES)
 @pytest.mark.parametrize("filter_mode", FILTERS)
 @pytest.mark.parametrize("boundary", BOUNDARIES)
-def test_gradients_match_oracle(cuda_lib, filter_mode, boundary):
+def test_gradients_match_oracle(cuda_lib, filter_mode, boundary, shape):
     from diffrp_gb300 import nvdr as dr
-    H, W, C = 32, 24, 4
-    tex, uv, da = _case(1, 2, H, W, C, 17, 13, seed=5)
+    Nt, H, W, C = shape
+    tex, uv, da = _case(Nt, 2, H, W, C, 17, 13, seed=5)
     mipped = filter_mode.startswith("linear-mipmap")
     gout = np.random.default_rng(9).normal(size=(2, 17, 13, C)).astype(np.float32)
     tex_t, uv_t = _t(tex).requires_grad_(True), _t(uv).requires_grad_(True)
