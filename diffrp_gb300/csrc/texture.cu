@@ -122,8 +122,24 @@ __device__ __forceinline__ TexLod tex_lod(const TexArgs& a, long long p) {
 }
 
 __device__ __forceinline__ int wrap_index(int i, int n) {
+    if ((n & (n - 1)) == 0) return i & (n - 1);  // a power of two (two's complement)
     const int r = i % n;
     return r < 0 ? r + n : r;
+}
+
+// Texel columns (or rows) i and i + 1 of a bilinear tap after the boundary
+// rule (texel_index's); -1: outside (zero boundary).
+__device__ __forceinline__ void tap_pair(int i, int n, int boundary, int& a, int& b) {
+    if (boundary == kTexWrap) {
+        a = wrap_index(i, n);
+        b = a + 1 == n ? 0 : a + 1;
+    } else if (boundary == kTexClamp) {
+        a = i < 0 ? 0 : (i > n - 1 ? n - 1 : i);
+        b = i + 1 < 0 ? 0 : (i + 1 > n - 1 ? n - 1 : i + 1);
+    } else {
+        a = i >= 0 && i < n ? i : -1;
+        b = i + 1 >= 0 && i + 1 < n ? i + 1 : -1;
+    }
 }
 
 // Texel index within its level (textures are at most 2^15 texels a side), or -1.
@@ -151,6 +167,7 @@ __device__ __forceinline__ float tex_coord(float u, int size) {
 struct Bilin {
     int i00, i10, i01, i11;
     float fx, fy;
+    int ix, iy;  // the tap's first texel before the boundary rule
 };
 
 __device__ __forceinline__ Bilin bilin_setup(float u, float v, int w, int h, int boundary) {
@@ -160,10 +177,15 @@ __device__ __forceinline__ Bilin bilin_setup(float u, float v, int w, int h, int
     B.fx = x - x0;
     B.fy = y - y0;
     const int ix = (int)x0, iy = (int)y0;
-    B.i00 = texel_index(ix, iy, w, h, boundary);
-    B.i10 = texel_index(ix + 1, iy, w, h, boundary);
-    B.i01 = texel_index(ix, iy + 1, w, h, boundary);
-    B.i11 = texel_index(ix + 1, iy + 1, w, h, boundary);
+    B.ix = ix;
+    B.iy = iy;
+    int xa, xb, ya, yb;
+    tap_pair(ix, w, boundary, xa, xb);
+    tap_pair(iy, h, boundary, ya, yb);
+    B.i00 = xa < 0 || ya < 0 ? -1 : ya * w + xa;
+    B.i10 = xb < 0 || ya < 0 ? -1 : ya * w + xb;
+    B.i01 = xa < 0 || yb < 0 ? -1 : yb * w + xa;
+    B.i11 = xb < 0 || yb < 0 ? -1 : yb * w + xb;
     return B;
 }
 
@@ -371,9 +393,13 @@ __device__ __forceinline__ void bilin_bwd(const float* lvl, float* glvl, const B
 }
 
 // bilin_bwd of four channels from one float4 load per texel (the same
-// arithmetic per channel); q: the texels, for the level-of-detail gradient.
-__device__ __forceinline__ void bilin_bwd4(const Quad& q, float* glvl, const Bilin& B, int w, int h, float4 g4,
-                                           float wl, float& gu, float& gv) {
+// arithmetic per channel); q: the texels.  Lanes whose taps start at the same
+// texel (ix, iy) of the same level and texture share all four texels: one
+// match finds them, one group sum adds their 4 x 4 values and the group's
+// lowest lane issues the four float4 atomics.
+__device__ __forceinline__ void bilin_bwd4(const Quad& q, float* glvl, const Bilin& B, int level, int tn,
+                                           bool per_view, int w, int h, float4 g4, float wl, float& gu,
+                                           float& gv) {
     const float fx = B.fx, fy = B.fy;
     const float wt[4] = {(1.f - fx) * (1.f - fy), fx * (1.f - fy), (1.f - fx) * fy, fx * fy};
     const int idx[4] = {B.i00, B.i10, B.i01, B.i11};
@@ -388,10 +414,24 @@ __device__ __forceinline__ void bilin_bwd4(const Quad& q, float* glvl, const Bil
         dx = fmaf(gc[c], fmaf(1.f - fy, t10 - t00, fy * (t11 - t01)), dx);
         dy = fmaf(gc[c], fmaf(fx, t11 - t01, t01) - fmaf(fx, t10 - t00, t00), dy);
     }
+    // ix, iy within +-2^24 + 1 (tex_coord's clamp): 26 bits each after the offset
+    const unsigned long long key = ((unsigned long long)level << 56) |
+                                   ((unsigned long long)((B.ix + (1 << 25)) & 0x3ffffff) << 26) |
+                                   (unsigned long long)((B.iy + (1 << 25)) & 0x3ffffff);
+    unsigned peers = __match_any_sync(active, key);
+    if (per_view) peers &= __match_any_sync(active, (unsigned)tn);
+    float val[16];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        float val[4] = {gc[0] * wt[t], gc[1] * wt[t], gc[2] * wt[t], gc[3] * wt[t]};
-        warp_add<4>(idx[t] >= 0 ? glvl + (long long)idx[t] * 4 : nullptr, val, active);
+    for (int t = 0; t < 4; ++t)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) val[4 * t + c] = gc[c] * wt[t];
+    group_sum<16>(val, peers, active);
+    if ((threadIdx.x & 31) == __ffs(peers) - 1) {
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            if (idx[t] >= 0)
+                atomicAdd(reinterpret_cast<float4*>(glvl) + idx[t],
+                          make_float4(val[4 * t], val[4 * t + 1], val[4 * t + 2], val[4 * t + 3]));
     }
     gu = fmaf(dx, (float)w, gu);
     gv = fmaf(dy, (float)h, gv);
@@ -425,11 +465,13 @@ __global__ void __launch_bounds__(256, 3) tex_bwd_kernel(TexArgs a) {
         if (a.vec4) {
             const float4 g4 = reinterpret_cast<const float4*>(a.grad_out)[p];
             const Quad q0 = fetch_quad(P0, B0);
-            bilin_bwd4(q0, grad_level(a, L.l0, tn), B0, a.lw[L.l0], a.lh[L.l0], g4, f > 0.f ? 1.f - f : 1.f, gu, gv);
+            bilin_bwd4(q0, grad_level(a, L.l0, tn), B0, L.l0, tn, a.Nt > 1, a.lw[L.l0], a.lh[L.l0], g4,
+                       f > 0.f ? 1.f - f : 1.f, gu, gv);
             if (f > 0.f) {
                 const Bilin B1 = bilin_setup(u, v, a.lw[L.l1], a.lh[L.l1], a.boundary);
                 const Quad q1 = fetch_quad(tex_level(a, a.tex, a.pyr, L.l1, tn), B1);
-                bilin_bwd4(q1, grad_level(a, L.l1, tn), B1, a.lw[L.l1], a.lh[L.l1], g4, f, gu, gv);
+                bilin_bwd4(q1, grad_level(a, L.l1, tn), B1, L.l1, tn, a.Nt > 1, a.lw[L.l1], a.lh[L.l1], g4, f, gu,
+                           gv);
                 if (a.grad_uv_da && L.interior) {
                     const float4 s0 = bilerp4(B0, q0), s1 = bilerp4(B1, q1);
                     dl = fmaf(g4.x, s1.x - s0.x, dl);
