@@ -929,9 +929,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="full", choices=["full", "steps"],
                     help="steps: only the warm-up and timed device-resident steps (for profilers)")
-    ap.add_argument("--workload", default="single", choices=["single", "views64", "uneven48", "large16"],
+    ap.add_argument("--workload", default="single", choices=["single", "views64", "uneven48", "large16", "texture"],
                     help="single: the headline single-mesh line (with the 64-view batched comparison "
-                         "attached); others: one line for that batched workload")
+                         "attached); others: one line for that batched workload, or the mip-mapped "
+                         "texture workload")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the attached lines (64 views, config-1 session, 48 meshes, large heightfield)")
     ap.add_argument("--tile", default=None,
@@ -951,6 +952,20 @@ def main():
     torch.cuda.set_device(dev)
     import __graft_entry__
     __graft_entry__.build()
+    if args.workload == "texture":
+        W_ = max(3, args.warmup)
+        res = run_texture(dev, steps=args.steps, warmup=W_, cpu=rank == 0 and not args.no_cpu_baseline)
+        if rank == 0:
+            print(json.dumps({
+                "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+                "warmup": W_, "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded texture and gradient)",
+                "config": {"workload": WORKLOAD_TEX, "parallelism": "single GPU",
+                           "l2": "flushed between steps (256 MiB write outside the timed events)"},
+                "gpu_launches": res["launches_per_step"] * args.steps, "detail": res}))
+        if world > 1:
+            dist.destroy_process_group()
+        return 0
     if args.workload != "single":
         W_ = max(3, args.warmup)
         fixed = tuple(int(x) for x in args.tile.split(",")) if args.tile else None
