@@ -82,7 +82,8 @@ struct TexLod {
     float ax, ay, bx, by;
 };
 
-__device__ __forceinline__ TexLod tex_lod(const TexArgs& a, long long p) {
+// da: the pixel's (du/dX, du/dY, dv/dX, dv/dY) (zero without uv_da).
+__device__ __forceinline__ TexLod tex_lod(const TexArgs& a, float4 da) {
     TexLod L;
     L.l0 = L.l1 = 0;
     L.f = 0.f;
@@ -91,7 +92,6 @@ __device__ __forceinline__ TexLod tex_lod(const TexArgs& a, long long p) {
     L.use_x = true;
     L.ax = L.ay = L.bx = L.by = 0.f;
     if (!a.uv_da || a.levels <= 1 || a.filter < kTexMipNearest) return L;
-    const float4 da = a.uv_da[p];
     L.ax = da.x * (float)a.W;
     L.bx = da.y * (float)a.W;
     L.ay = da.z * (float)a.H;
@@ -284,11 +284,20 @@ __global__ void __launch_bounds__(256) tex_mip_tile_kernel(TexArgs a, int base, 
     }
 }
 
-__global__ void __launch_bounds__(256, 3) tex_fwd_kernel(TexArgs a) {
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.npix) return;
+// Pixels per thread of the sampling kernels: every pixel's uv and uv_da are
+// loaded first, so that the later pixels' loads overlap the first's work.
+constexpr int kTexPix = 2;
+
+// The pixel's uv and uv_da (zero without uv_da).
+__device__ __forceinline__ void tex_inputs(const TexArgs& a, long long p, float& u, float& v, float4& da) {
+    const float2 uv = reinterpret_cast<const float2*>(a.uv)[p];
+    u = uv.x;
+    v = uv.y;
+    da = a.uv_da ? a.uv_da[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ void tex_fwd_pixel(const TexArgs& a, long long p, float u, float v, float4 da) {
     const int n = (int)(p / a.view_pix), tn = a.Nt == 1 ? 0 : n;
-    const float u = a.uv[2 * p], v = a.uv[2 * p + 1];
     const int C = a.C;
     float* o = a.out + p * C;
     if (a.filter == kTexNearest) {
@@ -297,7 +306,7 @@ __global__ void __launch_bounds__(256, 3) tex_fwd_kernel(TexArgs a) {
         for (int c = 0; c < C; ++c) o[c] = fetch(l0, i, C, c);
         return;
     }
-    const TexLod L = tex_lod(a, p);
+    const TexLod L = tex_lod(a, da);
     const Bilin B0 = bilin_setup(u, v, a.lw[L.l0], a.lh[L.l0], a.boundary);
     const float* v0 = tex_level(a, a.tex, a.pyr, L.l0, tn);
     if (a.vec4) {  // the same arithmetic per channel, one load per texel
@@ -321,6 +330,19 @@ __global__ void __launch_bounds__(256, 3) tex_fwd_kernel(TexArgs a) {
     } else {
         for (int c = 0; c < C; ++c) o[c] = bilin_value(v0, B0, C, c);
     }
+}
+
+// kTexPix pixels per thread, blockDim.x apart.
+__global__ void __launch_bounds__(256, 3) tex_fwd_kernel(TexArgs a) {
+    const long long base = (long long)blockIdx.x * (kTexPix * blockDim.x) + threadIdx.x;
+    float u[kTexPix], v[kTexPix];
+    float4 da[kTexPix];
+#pragma unroll
+    for (int j = 0; j < kTexPix; ++j)
+        if (base + j * blockDim.x < a.npix) tex_inputs(a, base + j * blockDim.x, u[j], v[j], da[j]);
+#pragma unroll
+    for (int j = 0; j < kTexPix; ++j)
+        if (base + j * blockDim.x < a.npix) tex_fwd_pixel(a, base + j * blockDim.x, u[j], v[j], da[j]);
 }
 
 // Sum of v over this lane's group (the lanes of `peers`, all of `active`
@@ -439,11 +461,8 @@ __device__ __forceinline__ void bilin_bwd4(const Quad& q, float* glvl, const Bil
 
 // One pixel's gradients: texel gradients added into the levels, the uv and
 // uv_da gradients written.
-__global__ void __launch_bounds__(256, 3) tex_bwd_kernel(TexArgs a) {
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.npix) return;
+__device__ __forceinline__ void tex_bwd_pixel(const TexArgs& a, long long p, float u, float v, float4 da) {
     const int n = (int)(p / a.view_pix), tn = a.Nt == 1 ? 0 : n;
-    const float u = a.uv[2 * p], v = a.uv[2 * p + 1];
     const int C = a.C;
     const float* g = a.grad_out + p * C;
     float gu = 0.f, gv = 0.f;
@@ -457,7 +476,7 @@ __global__ void __launch_bounds__(256, 3) tex_bwd_kernel(TexArgs a) {
             warp_add<1>(i >= 0 ? G0 + (long long)i * C + c : nullptr, val, active);
         }
     } else {
-        const TexLod L = tex_lod(a, p);
+        const TexLod L = tex_lod(a, da);
         const Bilin B0 = bilin_setup(u, v, a.lw[L.l0], a.lh[L.l0], a.boundary);
         const float* P0 = tex_level(a, a.tex, a.pyr, L.l0, tn);
         const float f = L.f;
@@ -504,9 +523,22 @@ __global__ void __launch_bounds__(256, 3) tex_bwd_kernel(TexArgs a) {
             }
         }
     }
-    a.grad_uv[2 * p] = gu;
-    a.grad_uv[2 * p + 1] = gv;
+    reinterpret_cast<float2*>(a.grad_uv)[p] = make_float2(gu, gv);
     if (a.grad_uv_da) a.grad_uv_da[p] = gda;
+}
+
+// kTexPix pixels per thread, blockDim.x apart (the warp's lanes take each
+// pixel together: its atomics are aggregated over the warp).
+__global__ void __launch_bounds__(256, 3) tex_bwd_kernel(TexArgs a) {
+    const long long base = (long long)blockIdx.x * (kTexPix * blockDim.x) + threadIdx.x;
+    float u[kTexPix], v[kTexPix];
+    float4 da[kTexPix];
+#pragma unroll
+    for (int j = 0; j < kTexPix; ++j)
+        if (base + j * blockDim.x < a.npix) tex_inputs(a, base + j * blockDim.x, u[j], v[j], da[j]);
+#pragma unroll
+    for (int j = 0; j < kTexPix; ++j)
+        if (base + j * blockDim.x < a.npix) tex_bwd_pixel(a, base + j * blockDim.x, u[j], v[j], da[j]);
 }
 
 __device__ __forceinline__ float vadd(float a, float b) { return a + b; }
@@ -731,7 +763,9 @@ DRP_API int drp_texture_fwd(const float* tex, const float* pyr, int num_tex, int
     if (a.npix == 0) return DRP_STATUS_OK;
     a.out = out;
     a.vec4 = channels == 4 && aligned16(tex) && aligned16(pyr) && aligned16(out);
-    drp::tex_fwd_kernel<<<(unsigned)((a.npix + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(a);
+    const long long per_block = 256 * drp::kTexPix;
+    drp::tex_fwd_kernel<<<(unsigned)((a.npix + per_block - 1) / per_block), 256, 0,
+                          static_cast<cudaStream_t>(stream)>>>(a);
     drp_note_launch();
     return drp_check_launch("drp_texture_fwd");
 }
@@ -761,7 +795,8 @@ DRP_API int drp_texture_bwd(const float* tex, const float* pyr, int num_tex, int
     a.grad_uv = grad_uv;
     a.grad_uv_da = reinterpret_cast<float4*>(grad_uv_da);
     if (a.npix > 0) {
-        drp::tex_bwd_kernel<<<(unsigned)((a.npix + 255) / 256), 256, 0, s>>>(a);
+        const long long per_block = 256 * drp::kTexPix;
+        drp::tex_bwd_kernel<<<(unsigned)((a.npix + per_block - 1) / per_block), 256, 0, s>>>(a);
         drp_note_launch();
     }
     if (levels > 1 && a.filter >= drp::kTexMipNearest) {
