@@ -22,7 +22,7 @@
 namespace drp {
 
 constexpr int kTexNearest = 0, kTexMipNearest = 2, kTexMipLinear = 3;  // 1: linear (bilinear, level 0)
-constexpr int kTexWrap = 0, kTexClamp = 1, kTexZero = 2;
+constexpr int kTexWrap = 0, kTexClamp = 1, kTexZero = 2, kTexMirror = 3;
 constexpr int kTexMaxLevels = 32;
 
 struct TexArgs {
@@ -127,6 +127,14 @@ __device__ __forceinline__ int wrap_index(int i, int n) {
     return r < 0 ? r + n : r;
 }
 
+// Mirrored repeat: period 2n, the second half reversed (glTF
+// MIRRORED_REPEAT; for bilinear taps the same as reflecting the coordinate
+// about the texture's edges, grid_sample's 'reflection' padding).
+__device__ __forceinline__ int mirror_index(int i, int n) {
+    const int m = wrap_index(i, 2 * n);
+    return m < n ? m : 2 * n - 1 - m;
+}
+
 // Texel columns (or rows) i and i + 1 of a bilinear tap after the boundary
 // rule (texel_index's); -1: outside (zero boundary).
 __device__ __forceinline__ void tap_pair(int i, int n, int boundary, int& a, int& b) {
@@ -136,6 +144,9 @@ __device__ __forceinline__ void tap_pair(int i, int n, int boundary, int& a, int
     } else if (boundary == kTexClamp) {
         a = i < 0 ? 0 : (i > n - 1 ? n - 1 : i);
         b = i + 1 < 0 ? 0 : (i + 1 > n - 1 ? n - 1 : i + 1);
+    } else if (boundary == kTexMirror) {
+        a = mirror_index(i, n);
+        b = mirror_index(i + 1, n);
     } else {
         a = i >= 0 && i < n ? i : -1;
         b = i + 1 >= 0 && i + 1 < n ? i + 1 : -1;
@@ -150,6 +161,9 @@ __device__ __forceinline__ int texel_index(int x, int y, int w, int h, int bound
     } else if (boundary == kTexClamp) {
         x = x < 0 ? 0 : (x > w - 1 ? w - 1 : x);
         y = y < 0 ? 0 : (y > h - 1 ? h - 1 : y);
+    } else if (boundary == kTexMirror) {
+        x = mirror_index(x, w);
+        y = mirror_index(y, h);
     } else if (x < 0 || x >= w || y < 0 || y >= h) {
         return -1;
     }
@@ -664,7 +678,7 @@ static int tex_setup(TexArgs& a, const char* who, const float* tex, const float*
     if (st) return st;
     if (!uv || num_views < 1 || (num_tex != 1 && num_tex != num_views) || out_height < 0 || out_width < 0 ||
         filter_mode < kTexNearest || filter_mode > kTexMipLinear || boundary_mode < kTexWrap ||
-        boundary_mode > kTexZero || (reinterpret_cast<uintptr_t>(uv) & 7) ||
+        boundary_mode > kTexMirror || (reinterpret_cast<uintptr_t>(uv) & 7) ||
         (reinterpret_cast<uintptr_t>(uv_da) & 15)) {
         char msg[160];
         snprintf(msg, sizeof(msg), "%s: bad sampling arguments", who);

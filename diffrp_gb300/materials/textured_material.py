@@ -16,7 +16,7 @@ from .base_material import SurfaceMaterial, SurfaceOutputStandard
 
 __all__ = ["sample_texture", "TexturedMaterial"]
 
-_WRAP = {"repeat": "wrap", "clamp": "clamp", "zero": "zero"}
+_WRAP = {"repeat": "wrap", "clamp": "clamp", "zero": "zero", "mirror": "mirror"}
 
 
 def sample_texture(image, uv, uv_da=None, wrap="repeat", filter_mode="auto", mip=None):
@@ -26,7 +26,8 @@ def sample_texture(image, uv, uv_da=None, wrap="repeat", filter_mode="auto", mip
 
     ``uv_da`` (..., 4) = (du/dX, du/dY, dv/dX, dv/dY) selects the mip level
     (filter_mode 'auto': trilinear with derivatives, else bilinear).  wrap:
-    'repeat', 'clamp' (to the edge, sample2d's 'border') or 'zero'.
+    'repeat', 'clamp' (to the edge, sample2d's 'border'), 'zero' or 'mirror'
+    (mirrored repeat, sample2d's 'reflection').
     ``mip``: a dr.texture_construct_mip of ``image[None]``.
     """
     if wrap not in _WRAP:

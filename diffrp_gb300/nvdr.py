@@ -588,7 +588,9 @@ def antialias(color, rast, pos, tri, topology_hash=None, pos_gradient_boost=1.0)
 # Texture sampling
 # ---------------------------------------------------------------------------
 _TEX_FILTERS = {"nearest": 0, "linear": 1, "linear-mipmap-nearest": 2, "linear-mipmap-linear": 3}
-_TEX_BOUNDARIES = {"wrap": 0, "clamp": 1, "zero": 2}
+# 'mirror' (mirrored repeat) is an addition to nvdiffrast's modes: diffrp's
+# sample2d 'reflection' padding and glTF's MIRRORED_REPEAT
+_TEX_BOUNDARIES = {"wrap": 0, "clamp": 1, "zero": 2, "mirror": 3}
 
 
 def _tex_levels(H, W, max_mip_level):
@@ -676,7 +678,7 @@ def texture(tex, uv, uv_da=None, mip_level_bias=None, mip=None, filter_mode="aut
     'auto' (trilinear with ``uv_da``, else bilinear); the mip-mapped modes
     choose the level from ``uv_da`` (N, h, w, 4) = (du/dX, du/dY, dv/dX,
     dv/dY), e.g. interpolate(..., diff_attrs=...)'s derivatives of uv.
-    boundary_mode 'wrap', 'clamp' or 'zero'.  ``mip`` reuses a
+    boundary_mode 'wrap', 'clamp', 'zero' or 'mirror' (mirrored repeat).  ``mip`` reuses a
     texture_construct_mip pyramid of ``tex``.  Gradients reach ``tex``
     (through the pyramid), ``uv`` and ``uv_da`` (trilinear, where the level of
     detail is not clamped).  Not supported: mip_level_bias and cube maps.

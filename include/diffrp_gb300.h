@@ -304,7 +304,8 @@ int drp_transform_points_bwd(const float* grad_out, long long num_vertices, cons
  * num_tex is 1 (shared) or num_views.  filter_mode: 0 nearest, 1 linear,
  * 2 linear-mipmap-nearest, 3 linear-mipmap-linear (level of detail 0.5
  * log2 of the larger squared footprint in level-0 texels, clamped to the
- * pyramid).  boundary_mode: 0 wrap, 1 clamp, 2 zero.  Textures of at most
+ * pyramid).  boundary_mode: 0 wrap, 1 clamp, 2 zero, 3 mirror (mirrored
+ * repeat: period 2 x size, the second half reversed).  Textures of at most
  * 32768 x 32768.
  */
 int drp_texture_levels(int height, int width, int max_mip_level, int* levels);

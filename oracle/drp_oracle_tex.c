@@ -20,7 +20,8 @@
  *  - Bilinear at level k: x = u W_k - 0.5, y = v H_k - 0.5, x0 = floor(x),
  *    fx = x - x0 (likewise y); r0 = fma(fx, t10 - t00, t00), r1 = fma(fx,
  *    t11 - t01, t01), value = fma(fy, r1 - r0, r0).  Boundary: wrap (index
- *    modulo the size), clamp (index clamped), zero (texels outside read 0).
+ *    modulo the size), clamp (index clamped), zero (texels outside read 0),
+ *    mirror (index modulo twice the size, the second half reversed).
  *  - Nearest: the texel of level 0 whose centre is nearest, (floor(x + 0.5),
  *    floor(y + 0.5)) with x, y as for bilinear, same boundaries.
  *  - Storage: level 0 is the texture; levels 1 .. L-1 form one level-major
@@ -58,7 +59,7 @@ typedef REAL real;
 #endif
 
 enum { TEX_NEAREST = 0, TEX_LINEAR = 1, TEX_MIP_NEAREST = 2, TEX_MIP_LINEAR = 3 };
-enum { TEX_WRAP = 0, TEX_CLAMP = 1, TEX_ZERO = 2 };
+enum { TEX_WRAP = 0, TEX_CLAMP = 1, TEX_ZERO = 2, TEX_MIRROR = 3 };
 
 static inline real r_fma(real a, real b, real c) {
 #ifdef REAL_IS_DOUBLE
@@ -239,6 +240,12 @@ static inline int wrap_index(int i, int n) {
     return r < 0 ? r + n : r;
 }
 
+/* Mirrored repeat: period 2n, the second half reversed. */
+static inline int mirror_index(int i, int n) {
+    const int m = wrap_index(i, 2 * n);
+    return m < n ? m : 2 * n - 1 - m;
+}
+
 /* Texel index for boundary mode; -1 outside (zero mode). */
 static inline long texel_index(int x, int y, int w, int h, int boundary) {
     if (boundary == TEX_WRAP) {
@@ -247,6 +254,9 @@ static inline long texel_index(int x, int y, int w, int h, int boundary) {
     } else if (boundary == TEX_CLAMP) {
         x = x < 0 ? 0 : (x > w - 1 ? w - 1 : x);
         y = y < 0 ? 0 : (y > h - 1 ? h - 1 : y);
+    } else if (boundary == TEX_MIRROR) {
+        x = mirror_index(x, w);
+        y = mirror_index(y, h);
     } else if (x < 0 || x >= w || y < 0 || y >= h) {
         return -1;
     }

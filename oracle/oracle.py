@@ -369,7 +369,7 @@ def l1_fixed_visibility(pos, tri, attr, ids, sign, plan, resolution, tri_flag=No
 # (N, h, w, 4) = (du/dX, du/dY, dv/dX, dv/dY) or None.
 # ---------------------------------------------------------------------------
 TEX_FILTERS = {"nearest": 0, "linear": 1, "linear-mipmap-nearest": 2, "linear-mipmap-linear": 3}
-TEX_BOUNDARIES = {"wrap": 0, "clamp": 1, "zero": 2}
+TEX_BOUNDARIES = {"wrap": 0, "clamp": 1, "zero": 2, "mirror": 3}
 
 
 def tex_levels(H, W, max_level=-1):

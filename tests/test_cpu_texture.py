@@ -1,9 +1,11 @@
 """The texture-sampling oracle (oracle/drp_oracle_tex.c) against independent
 references, on the CPU.
 
-* bilinear sampling with clamp / zero boundaries against
-  torch.nn.functional.grid_sample (align_corners=False, border / zeros
-  padding): the same texel-centre convention, computed by other code;
+* bilinear sampling with clamp / zero / mirror boundaries against
+  torch.nn.functional.grid_sample (align_corners=False, border / zeros /
+  reflection padding): the same texel-centre convention, computed by other
+  code (mirrored repeat of the bilinear taps equals reflecting the
+  coordinate about the texture's edges);
 * wrap against clamp on a texture tiled three times;
 * the mip pyramid against a numpy 2x2 reshape-mean (even sizes) and the
   size-1 rule (odd and degenerate sizes);
@@ -28,7 +30,7 @@ def _uv(N, h, w, lo=-0.2, hi=1.2, seed=1):
     return np.random.default_rng(seed).uniform(lo, hi, (N, h, w, 2)).astype(np.float32)
 
 
-@pytest.mark.parametrize("boundary,padding", [("clamp", "border"), ("zero", "zeros")])
+@pytest.mark.parametrize("boundary,padding", [("clamp", "border"), ("zero", "zeros"), ("mirror", "reflection")])
 def test_bilinear_matches_grid_sample(boundary, padding):
     tex = _tex(2, 13, 17, 3)
     uv = _uv(2, 9, 11)
@@ -105,7 +107,7 @@ def _central(fn, x, idx, eps):
 
 
 @pytest.mark.parametrize("filter_mode", ["linear", "linear-mipmap-nearest", "linear-mipmap-linear"])
-@pytest.mark.parametrize("boundary", ["wrap", "clamp", "zero"])
+@pytest.mark.parametrize("boundary", ["wrap", "clamp", "zero", "mirror"])
 def test_gradients_match_central_differences(filter_mode, boundary):
     H, W, C = 12, 10, 3
     L = O.tex_levels(H, W)

@@ -19,7 +19,7 @@ import oracle as O
 pytestmark = pytest.mark.gpu
 
 FILTERS = ["nearest", "linear", "linear-mipmap-nearest", "linear-mipmap-linear"]
-BOUNDARIES = ["wrap", "clamp", "zero"]
+BOUNDARIES = ["wrap", "clamp", "zero", "mirror"]
 
 
 def _case(Nt, N, H, W, C, h, w, seed=0):
@@ -256,3 +256,135 @@ def test_full_size_receding_plane(cuda_lib):
         scale = float(np.abs(want).max())
         assert scale > 0, what
         assert float(np.abs(got - want).max()) <= tol * scale, what
+
+
+def _sample2d(image, uv, padding, mode):
+    """diffrp's sample2d (diffrp/utils/shader_ops.py:199-255) restated:
+    grid_sample with v flipped, align_corners=False."""
+    C = image.shape[-1]
+    grid = ((uv.reshape(-1, 2) * 2 - 1) * torch.tensor([1.0, -1.0], device=uv.device)).reshape(1, 1, -1, 2)
+    out = torch.nn.functional.grid_sample(image[None].permute(0, 3, 1, 2), grid, mode=mode, padding_mode=padding,
+                                          align_corners=False).view(C, -1).T
+    return out.reshape(*uv.shape[:-1], C)
+
+
+@pytest.mark.parametrize("wrap_mode", ["repeat", "clamp", "mirror"])
+@pytest.mark.parametrize("interpolation", ["linear", "point"])
+def test_gltf_sampler_matches_reference_without_derivatives(cuda_lib, wrap_mode, interpolation):
+    """GLTFSampler.sample without derivatives is the reference's
+    GLTFSampler.sample (diffrp/materials/gltf_material.py:15-22): 'repeat'
+    takes uv modulo 1 and pads by reflection, 'clamp' pads by border,
+    'mirror' by reflection; 'point' is grid_sample's nearest.  Samples keep
+    away from exact nearest-texel ties (grid_sample rounds half to even).
+    Tolerance 1e-5: grid_sample reflects the continuous coordinate in float
+    arithmetic (up to 92 texels here, an ulp of 7.6e-6), the kernel mirrors
+    integer texel indices, so bilinear weights differ by an ulp of x."""
+    from diffrp_gb300.materials import GLTFSampler
+    rng = np.random.default_rng(21)
+    image = _t(rng.uniform(0, 1, (24, 40, 3)).astype(np.float32))
+    uv = _t(rng.uniform(-1.3, 2.3, (50, 7, 2)).astype(np.float32))
+    got = GLTFSampler(image, wrap_mode, interpolation).sample(uv)
+    ref_uv = uv.remainder(1.0) if wrap_mode == "repeat" else uv
+    ref = _sample2d(image, ref_uv, "border" if wrap_mode == "clamp" else "reflection",
+                    "bilinear" if interpolation == "linear" else "nearest")
+    torch.testing.assert_close(got, ref, rtol=0, atol=1e-5)
+
+
+class _Fragments:
+    """A SurfaceInput stand-in: uv, vertex colour and (optionally) uv_da."""
+
+    def __init__(self, uv, color, uv_da=None):
+        self.uv, self.color, self._da = uv, color, uv_da
+
+    @property
+    def uv_da(self):
+        if self._da is None:
+            raise RuntimeError("no derivatives")
+        return self._da
+
+
+def _gltf(rng, alpha_mode):
+    from diffrp_gb300.materials import GLTFMaterial, GLTFSampler
+
+    def img(c):
+        return _t(rng.uniform(0, 1, (16, 24, c)).astype(np.float32))
+    return GLTFMaterial(
+        base_color_factor=_t(np.array([0.9, 0.8, 0.7, 0.6], np.float32)),
+        base_color_texture=GLTFSampler(img(4), "repeat"),
+        metallic_factor=0.7, roughness_factor=0.4,
+        metallic_roughness_texture=GLTFSampler(img(3), "mirror"),
+        normal_texture=GLTFSampler(img(3), "clamp"),
+        occlusion_texture=GLTFSampler(img(1), "repeat", "point"),
+        emissive_factor=_t(np.array([0.5, 0.25, 1.0], np.float32)),
+        emissive_texture=GLTFSampler(img(3), "clamp"),
+        alpha_cutoff=0.3, alpha_mode=alpha_mode)
+
+
+@pytest.mark.parametrize("alpha_mode", ["OPAQUE", "MASK", "BLEND"])
+def test_gltf_material_shade_matches_reference(cuda_lib, alpha_mode):
+    """GLTFMaterial.shade without derivatives against the reference's shade
+    (diffrp/materials/gltf_material.py:44-67) restated on sample2d; with
+    derivatives every 'linear' texture is sampled trilinearly, equal to the
+    oracle on the same (remaindered, mirrored) coordinates."""
+    rng = np.random.default_rng(22)
+    m = _gltf(rng, alpha_mode)
+    n = 500
+    uv = _t(rng.uniform(-0.5, 1.5, (n, 2)).astype(np.float32))
+    color = _t(rng.uniform(0.5, 1, (n, 4)).astype(np.float32))
+    out = m.shade(None, _Fragments(uv, color))
+
+    def ref_sample(s, uv_):
+        u2 = uv_.remainder(1.0) if s.wrap_mode == "repeat" else uv_
+        return _sample2d(s.image, u2, "border" if s.wrap_mode == "clamp" else "reflection",
+                         "bilinear" if s.interpolation == "linear" else "nearest")
+    rgba = m.base_color_factor * color * ref_sample(m.base_color_texture, uv)
+    mr = ref_sample(m.metallic_roughness_texture, uv)
+    want = {"albedo": rgba[..., :3], "normal": 2 * ref_sample(m.normal_texture, uv) - 1,
+            "emission": m.emissive_factor * ref_sample(m.emissive_texture, uv),
+            "metallic": m.metallic_factor * mr[..., 2:3], "smoothness": 1.0 - m.roughness_factor * mr[..., 1:2],
+            "occlusion": ref_sample(m.occlusion_texture, uv)[..., :1]}
+    if alpha_mode == "MASK":
+        want["alpha"] = (rgba[..., 3:4] > m.alpha_cutoff).float()
+    elif alpha_mode == "BLEND":
+        want["alpha"] = rgba[..., 3:4]
+    else:
+        assert out.alpha is None
+    for k, v in want.items():
+        torch.testing.assert_close(getattr(out, k), v, rtol=0, atol=1e-5, msg=k)
+    # with derivatives: trilinear, against the oracle
+    da = _t((rng.uniform(-1, 1, (n, 4)) * 2.0 ** rng.uniform(-2, 5, (n, 1)) / 24).astype(np.float32))
+    out_d = m.shade(None, _Fragments(uv, color, da))
+    s = m.emissive_texture  # clamp, linear
+    img = s.image.cpu().numpy()[None]
+    L = O.tex_levels(16, 24)
+    uv_t = torch.stack([uv[:, 0], 1 - uv[:, 1]], -1).cpu().numpy().reshape(1, 1, n, 2)
+    da_t = (da * _t(np.array([1, 1, -1, -1], np.float32))).cpu().numpy().reshape(1, 1, n, 4)
+    ref = O.tex_fwd(img, O.tex_mip_build(img, L), L, uv_t, da_t, "linear-mipmap-linear", "clamp").reshape(n, 3)
+    np.testing.assert_allclose(out_d.emission.cpu().numpy(), m.emissive_factor.cpu().numpy() * ref, rtol=0,
+                               atol=1e-6)
+
+
+def test_session_gltf_material_with_derivatives(cuda_lib):
+    """A glTF-textured ground plane through the session: trained base colour
+    texture (requires_grad) gets gradients through the mip pyramid; the
+    minified far part is filtered with derivatives."""
+    from diffrp_gb300.materials import GLTFMaterial, GLTFSampler
+    from diffrp_gb300.rendering import camera
+    from diffrp_gb300.rendering.surface_deferred import (SurfaceDeferredRenderSession,
+                                                         SurfaceDeferredRenderSessionOptions)
+    checker = ((np.indices((32, 32)).sum(0) % 2) * np.ones((4, 1, 1))).transpose(1, 2, 0).astype(np.float32)
+    cam = camera.PerspectiveCamera(fov=40, h=96, w=128)
+    images = {}
+    for deriv in [False, True]:
+        base = _t(checker).requires_grad_(True)
+        white = _t(np.ones((4, 4, 3), np.float32))
+        m = GLTFMaterial(_t(np.ones(4, np.float32)), GLTFSampler(base, "repeat"), 0.0, 1.0, GLTFSampler(white),
+                         None, None, None, GLTFSampler(white), 0.5, "OPAQUE")
+        s = SurfaceDeferredRenderSession(_ground_scene(m), cam, opaque_only=True,
+                                         options=SurfaceDeferredRenderSessionOptions(derivatives=deriv))
+        img = s.albedo_layered()[0]
+        img.sum().backward()
+        assert base.grad is not None and float(base.grad.abs().sum()) > 0
+        images[deriv] = img.detach().cpu().numpy()[0]
+    far_plain, far_mip = images[False][25:38, 30:98, 0], images[True][25:38, 30:98, 0]
+    assert far_mip.std() < 0.5 * far_plain.std()
