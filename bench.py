@@ -957,7 +957,8 @@ def main():
         res = run_texture(dev, steps=args.steps, warmup=W_, cpu=rank == 0 and not args.no_cpu_baseline)
         if rank == 0:
             print(json.dumps({
-                "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+                "metric": "fwd+bwd Mpix/s (mip pyramid, trilinear texture sample, backward to texture, uv and uv_da)",
+                "value": res["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
                 "warmup": W_, "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded texture and gradient)",
                 "config": {"workload": WORKLOAD_TEX, "parallelism": "single GPU",

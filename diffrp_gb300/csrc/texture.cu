@@ -270,6 +270,16 @@ __global__ void __launch_bounds__(256) tex_mip_tile_kernel(TexArgs a, int base, 
             if (x >= w || y >= h) continue;
             const int x0 = 2 * x < pw - 1 ? 2 * x : pw - 1, x1 = 2 * x + 1 < pw - 1 ? 2 * x + 1 : pw - 1;
             const int y0 = 2 * y < ph - 1 ? 2 * y : ph - 1, y1 = 2 * y + 1 < ph - 1 ? 2 * y + 1 : ph - 1;
+            if (s == 0 && a.vec4) {  // four channels, one float4 load per texel (the same sums)
+                const float4* q = reinterpret_cast<const float4*>(src);
+                const float4 ta = __ldg(q + (long long)y0 * pw + x0), tb = __ldg(q + (long long)y0 * pw + x1);
+                const float4 tc = __ldg(q + (long long)y1 * pw + x0), td = __ldg(q + (long long)y1 * pw + x1);
+                const float4 r = make_float4((((ta.x + tb.x) + tc.x) + td.x) * 0.25f, (((ta.y + tb.y) + tc.y) + td.y) * 0.25f,
+                                             (((ta.z + tb.z) + tc.z) + td.z) * 0.25f, (((ta.w + tb.w) + tc.w) + td.w) * 0.25f);
+                reinterpret_cast<float4*>(dst)[(long long)y * w + x] = r;
+                if (s + 1 < nl) reinterpret_cast<float4*>(sm + off)[ly * T + lx] = r;
+                continue;
+            }
             for (int c = 0; c < C; ++c) {
                 float pa, pb, pc, pd;
                 if (s == 0) {
@@ -748,6 +758,7 @@ DRP_API int drp_texture_mip_build(const float* tex, int num_tex, int height, int
         drp_set_last_error("drp_texture_mip_build: more than 6144 channels");
         return DRP_STATUS_INVALID_ARGUMENT;
     }
+    a.vec4 = channels == 4 && aligned16(tex) && aligned16(pyr);
     for (int base = 0; base + 1 < levels; base += per_launch) {
         const int nl = levels - 1 - base < per_launch ? levels - 1 - base : per_launch;
         const int tiles_x = (a.lw[base + 1] + side - 1) / side, tiles_y = (a.lh[base + 1] + side - 1) / side;
