@@ -107,3 +107,35 @@ def test_transform_and_transport_validation(lib):
         transform.clip_space_packed([])
     with pytest.raises(RuntimeError):
         hostio.device_view(torch.zeros(4))
+
+
+def test_texture_levels_and_validation(lib):
+    """The texture entry points' host-side rules: pyramid level counts and
+    sizes (floor halving to 1 x 1, max_mip_level), and bad arguments
+    rejected before any device work."""
+    from diffrp_gb300 import _ffi
+    n = ctypes.c_int(0)
+    for (h, w, mx), want in [((1024, 1024, -1), 11), ((1024, 1024, 3), 4), ((5, 7, -1), 3), ((1, 1, -1), 1),
+                             ((1, 9, -1), 4), ((32768, 1, -1), 16)]:
+        assert lib.drp_texture_levels(h, w, mx, ctypes.byref(n)) == 0
+        assert n.value == want, (h, w, mx)
+    assert lib.drp_texture_levels(0, 4, -1, ctypes.byref(n)) == 1
+    f = ctypes.c_longlong(0)
+    assert lib.drp_texture_pyramid_floats(2, 16, 8, 3, 5, ctypes.byref(f)) == 0
+    assert f.value == 2 * 3 * (8 * 4 + 4 * 2 + 2 * 1 + 1 * 1)  # levels 1 .. 4
+    before = _ffi.kernel_launches()
+    p = ctypes.c_void_p(256)  # never dereferenced: every call below fails validation
+    # texture larger than 2^15 a side
+    assert lib.drp_texture_mip_build(p, 1, 40000, 4, 4, 2, p, None) == 1
+    # levels above the texture's pyramid
+    assert lib.drp_texture_mip_build(p, 1, 8, 8, 4, 5, p, None) == 1
+    # num_tex neither 1 nor num_views
+    assert lib.drp_texture_fwd(p, p, 3, 8, 8, 4, 1, p, None, 2, 4, 4, 1, 0, p, None) == 1
+    # filter and boundary codes out of range
+    assert lib.drp_texture_fwd(p, p, 1, 8, 8, 4, 1, p, None, 1, 4, 4, 4, 0, p, None) == 1
+    assert lib.drp_texture_fwd(p, p, 1, 8, 8, 4, 1, p, None, 1, 4, 4, 1, 4, p, None) == 1
+    # uv not 8-byte aligned
+    assert lib.drp_texture_fwd(p, p, 1, 8, 8, 4, 1, ctypes.c_void_p(260), None, 1, 4, 4, 1, 0, p, None) == 1
+    # uv_da gradient without uv_da
+    assert lib.drp_texture_bwd(p, p, 1, 8, 8, 4, 1, p, None, 1, 4, 4, 1, 0, p, p, p, p, p, None) == 1
+    assert _ffi.kernel_launches() == before
