@@ -43,8 +43,8 @@ _SIGNATURES = {
     "drp_texture_levels": [_I, _I, _I, ctypes.POINTER(ctypes.c_int)],
     "drp_texture_pyramid_floats": [_I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_longlong)],
     "drp_texture_mip_build": [_P, _I, _I, _I, _I, _I, _P, _P],
-    "drp_texture_fwd": [_P, _P, _I, _I, _I, _I, _I, _P, _P, _I, _I, _I, _I, _I, _P, _P],
-    "drp_texture_bwd": [_P, _P, _I, _I, _I, _I, _I, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P],
+    "drp_texture_fwd": [_P, _P, _I, _I, _I, _I, _I, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P],
+    "drp_texture_bwd": [_P, _P, _I, _I, _I, _I, _I, _P, _P, _P, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P],
 }
 
 ABI_VERSION = 1

@@ -33,6 +33,7 @@ struct TexArgs {
     long long lofs[kTexMaxLevels];  // float offset of level k (k >= 1) in pyr; level k's texture n at + n H_k W_k C
     const float* uv;                // (N, h, w, 2)
     const float4* uv_da;            // (N, h, w) of (du/dX, du/dY, dv/dX, dv/dY), or null
+    const float* bias;              // (N, h, w) mip level bias added to the level of detail, or null
     long long npix, view_pix;       // N h w, h w
     int filter, boundary;
     float* out;
@@ -42,6 +43,7 @@ struct TexArgs {
     float* grad_pyr;
     float* grad_uv;
     float4* grad_uv_da;
+    float* grad_bias;  // (N, h, w), or null
     // C == 4 with every texel and pixel buffer of the call 16-byte aligned:
     // float4 loads, stores and atomics
     int vec4;
@@ -76,33 +78,42 @@ __device__ __forceinline__ float tex_log2(float x) {
 struct TexLod {
     int l0, l1;
     float f;
-    bool interior;
+    bool interior;   // lambda strictly inside (0, levels - 1): its gradient flows
+    bool da_active;  // lambda has the footprint term (uv_da given, footprint > 0)
     float r2;
     bool use_x;
     float ax, ay, bx, by;
 };
 
-// da: the pixel's (du/dX, du/dY, dv/dX, dv/dY) (zero without uv_da).
-__device__ __forceinline__ TexLod tex_lod(const TexArgs& a, float4 da) {
+// da: the pixel's (du/dX, du/dY, dv/dX, dv/dY) (zero without uv_da); b:
+// its mip level bias (zero without one).  lambda = 0.5 log2 of the larger
+// squared footprint (0 without uv_da or for a zero / non-finite footprint)
+// plus the bias, clamped to the pyramid.
+__device__ __forceinline__ TexLod tex_lod(const TexArgs& a, float4 da, float b) {
     TexLod L;
     L.l0 = L.l1 = 0;
     L.f = 0.f;
     L.interior = false;
+    L.da_active = false;
     L.r2 = 0.f;
     L.use_x = true;
     L.ax = L.ay = L.bx = L.by = 0.f;
-    if (!a.uv_da || a.levels <= 1 || a.filter < kTexMipNearest) return L;
-    L.ax = da.x * (float)a.W;
-    L.bx = da.y * (float)a.W;
-    L.ay = da.z * (float)a.H;
-    L.by = da.w * (float)a.H;
-    const float lx = L.ax * L.ax + L.ay * L.ay;
-    const float ly = L.bx * L.bx + L.by * L.by;
-    L.use_x = lx >= ly;
-    const float r2 = L.use_x ? lx : ly;
-    L.r2 = r2;
+    if ((!a.uv_da && !a.bias) || a.levels <= 1 || a.filter < kTexMipNearest) return L;
     float lam = 0.f;
-    if (r2 > 0.f && isfinite(r2)) lam = 0.5f * tex_log2(r2);
+    if (a.uv_da) {
+        L.ax = da.x * (float)a.W;
+        L.bx = da.y * (float)a.W;
+        L.ay = da.z * (float)a.H;
+        L.by = da.w * (float)a.H;
+        const float lx = L.ax * L.ax + L.ay * L.ay;
+        const float ly = L.bx * L.bx + L.by * L.by;
+        L.use_x = lx >= ly;
+        const float r2 = L.use_x ? lx : ly;
+        L.r2 = r2;
+        L.da_active = r2 > 0.f && isfinite(r2);
+        if (L.da_active) lam = 0.5f * tex_log2(r2);
+    }
+    if (a.bias) lam = lam + b;
     const float top = (float)(a.levels - 1);
     L.interior = lam > 0.f && lam < top;
     if (!(lam > 0.f)) lam = 0.f;
@@ -312,15 +323,24 @@ __global__ void __launch_bounds__(256) tex_mip_tile_kernel(TexArgs a, int base, 
 // loaded first, so that the later pixels' loads overlap the first's work.
 constexpr int kTexPix = 2;
 
-// The pixel's uv and uv_da (zero without uv_da).
-__device__ __forceinline__ void tex_inputs(const TexArgs& a, long long p, float& u, float& v, float4& da) {
+// The pixel's uv, uv_da and mip level bias (zero without them).
+struct TexIn {
+    float u, v, b;
+    float4 da;
+};
+
+__device__ __forceinline__ TexIn tex_inputs(const TexArgs& a, long long p) {
     const float2 uv = reinterpret_cast<const float2*>(a.uv)[p];
-    u = uv.x;
-    v = uv.y;
-    da = a.uv_da ? a.uv_da[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+    TexIn in;
+    in.u = uv.x;
+    in.v = uv.y;
+    in.da = a.uv_da ? a.uv_da[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+    in.b = a.bias ? a.bias[p] : 0.f;
+    return in;
 }
 
-__device__ __forceinline__ void tex_fwd_pixel(const TexArgs& a, long long p, float u, float v, float4 da) {
+__device__ __forceinline__ void tex_fwd_pixel(const TexArgs& a, long long p, const TexIn& in) {
+    const float u = in.u, v = in.v;
     const int n = (int)(p / a.view_pix), tn = a.Nt == 1 ? 0 : n;
     const int C = a.C;
     float* o = a.out + p * C;
@@ -330,7 +350,7 @@ __device__ __forceinline__ void tex_fwd_pixel(const TexArgs& a, long long p, flo
         for (int c = 0; c < C; ++c) o[c] = fetch(l0, i, C, c);
         return;
     }
-    const TexLod L = tex_lod(a, da);
+    const TexLod L = tex_lod(a, in.da, in.b);
     const Bilin B0 = bilin_setup(u, v, a.lw[L.l0], a.lh[L.l0], a.boundary);
     const float* v0 = tex_level(a, a.tex, a.pyr, L.l0, tn);
     if (a.vec4) {  // the same arithmetic per channel, one load per texel
@@ -359,14 +379,13 @@ __device__ __forceinline__ void tex_fwd_pixel(const TexArgs& a, long long p, flo
 // kTexPix pixels per thread, blockDim.x apart.
 __global__ void __launch_bounds__(256, 3) tex_fwd_kernel(TexArgs a) {
     const long long base = (long long)blockIdx.x * (kTexPix * blockDim.x) + threadIdx.x;
-    float u[kTexPix], v[kTexPix];
-    float4 da[kTexPix];
+    TexIn in[kTexPix];
 #pragma unroll
     for (int j = 0; j < kTexPix; ++j)
-        if (base + j * blockDim.x < a.npix) tex_inputs(a, base + j * blockDim.x, u[j], v[j], da[j]);
+        if (base + j * blockDim.x < a.npix) in[j] = tex_inputs(a, base + j * blockDim.x);
 #pragma unroll
     for (int j = 0; j < kTexPix; ++j)
-        if (base + j * blockDim.x < a.npix) tex_fwd_pixel(a, base + j * blockDim.x, u[j], v[j], da[j]);
+        if (base + j * blockDim.x < a.npix) tex_fwd_pixel(a, base + j * blockDim.x, in[j]);
 }
 
 // Sum of v over this lane's group (the lanes of `peers`, all of `active`
@@ -485,11 +504,12 @@ __device__ __forceinline__ void bilin_bwd4(const Quad& q, float* glvl, const Bil
 
 // One pixel's gradients: texel gradients added into the levels, the uv and
 // uv_da gradients written.
-__device__ __forceinline__ void tex_bwd_pixel(const TexArgs& a, long long p, float u, float v, float4 da) {
+__device__ __forceinline__ void tex_bwd_pixel(const TexArgs& a, long long p, const TexIn& in) {
+    const float u = in.u, v = in.v;
     const int n = (int)(p / a.view_pix), tn = a.Nt == 1 ? 0 : n;
     const int C = a.C;
     const float* g = a.grad_out + p * C;
-    float gu = 0.f, gv = 0.f;
+    float gu = 0.f, gv = 0.f, gb = 0.f;
     float4 gda = make_float4(0.f, 0.f, 0.f, 0.f);
     if (a.filter == kTexNearest) {
         float* G0 = grad_level(a, 0, tn);
@@ -500,10 +520,11 @@ __device__ __forceinline__ void tex_bwd_pixel(const TexArgs& a, long long p, flo
             warp_add<1>(i >= 0 ? G0 + (long long)i * C + c : nullptr, val, active);
         }
     } else {
-        const TexLod L = tex_lod(a, da);
+        const TexLod L = tex_lod(a, in.da, in.b);
         const Bilin B0 = bilin_setup(u, v, a.lw[L.l0], a.lh[L.l0], a.boundary);
         const float* P0 = tex_level(a, a.tex, a.pyr, L.l0, tn);
         const float f = L.f;
+        const bool want_dl = (a.grad_uv_da || a.grad_bias) && L.interior;
         float dl = 0.f;  // d out / d lambda . grad_out
         if (a.vec4) {
             const float4 g4 = reinterpret_cast<const float4*>(a.grad_out)[p];
@@ -515,7 +536,7 @@ __device__ __forceinline__ void tex_bwd_pixel(const TexArgs& a, long long p, flo
                 const Quad q1 = fetch_quad(tex_level(a, a.tex, a.pyr, L.l1, tn), B1);
                 bilin_bwd4(q1, grad_level(a, L.l1, tn), B1, L.l1, tn, a.Nt > 1, a.lw[L.l1], a.lh[L.l1], g4, f, gu,
                            gv);
-                if (a.grad_uv_da && L.interior) {
+                if (want_dl) {
                     const float4 s0 = bilerp4(B0, q0), s1 = bilerp4(B1, q1);
                     dl = fmaf(g4.x, s1.x - s0.x, dl);
                     dl = fmaf(g4.y, s1.y - s0.y, dl);
@@ -530,13 +551,14 @@ __device__ __forceinline__ void tex_bwd_pixel(const TexArgs& a, long long p, flo
                 const Bilin B1 = bilin_setup(u, v, a.lw[L.l1], a.lh[L.l1], a.boundary);
                 const float* P1 = tex_level(a, a.tex, a.pyr, L.l1, tn);
                 bilin_bwd(P1, grad_level(a, L.l1, tn), B1, a.lw[L.l1], a.lh[L.l1], C, g, f, gu, gv);
-                if (a.grad_uv_da && L.interior)
+                if (want_dl)
                     for (int c = 0; c < C; ++c)
                         dl = fmaf(g[c], bilin_value(P1, B1, C, c) - bilin_value(P0, B0, C, c), dl);
             }
         }
-        if (f > 0.f && a.grad_uv_da && L.interior) {
-            // lambda = 0.5 log2(r2): d lambda / d r2 = 0.5 / (r2 ln 2)
+        if (f > 0.f && want_dl) gb = dl;
+        if (f > 0.f && want_dl && a.grad_uv_da && L.da_active) {
+            // lambda = 0.5 log2(r2) + bias: d lambda / d r2 = 0.5 / (r2 ln 2)
             const float dr2 = dl * (0.72134752f / L.r2);
             if (L.use_x) {
                 gda.x = dr2 * 2.f * L.ax * (float)a.W;
@@ -549,20 +571,20 @@ __device__ __forceinline__ void tex_bwd_pixel(const TexArgs& a, long long p, flo
     }
     reinterpret_cast<float2*>(a.grad_uv)[p] = make_float2(gu, gv);
     if (a.grad_uv_da) a.grad_uv_da[p] = gda;
+    if (a.grad_bias) a.grad_bias[p] = gb;
 }
 
 // kTexPix pixels per thread, blockDim.x apart (the warp's lanes take each
 // pixel together: its atomics are aggregated over the warp).
 __global__ void __launch_bounds__(256, 3) tex_bwd_kernel(TexArgs a) {
     const long long base = (long long)blockIdx.x * (kTexPix * blockDim.x) + threadIdx.x;
-    float u[kTexPix], v[kTexPix];
-    float4 da[kTexPix];
+    TexIn in[kTexPix];
 #pragma unroll
     for (int j = 0; j < kTexPix; ++j)
-        if (base + j * blockDim.x < a.npix) tex_inputs(a, base + j * blockDim.x, u[j], v[j], da[j]);
+        if (base + j * blockDim.x < a.npix) in[j] = tex_inputs(a, base + j * blockDim.x);
 #pragma unroll
     for (int j = 0; j < kTexPix; ++j)
-        if (base + j * blockDim.x < a.npix) tex_bwd_pixel(a, base + j * blockDim.x, u[j], v[j], da[j]);
+        if (base + j * blockDim.x < a.npix) tex_bwd_pixel(a, base + j * blockDim.x, in[j]);
 }
 
 __device__ __forceinline__ float vadd(float a, float b) { return a + b; }
@@ -682,14 +704,14 @@ static int tex_levels_setup(TexArgs& a, const char* who, const float* tex, const
 }
 
 static int tex_setup(TexArgs& a, const char* who, const float* tex, const float* pyr, int num_tex, int height,
-                     int width, int channels, int levels, const float* uv, const float* uv_da, int num_views,
-                     int out_height, int out_width, int filter_mode, int boundary_mode) {
+                     int width, int channels, int levels, const float* uv, const float* uv_da, const float* bias,
+                     int num_views, int out_height, int out_width, int filter_mode, int boundary_mode) {
     const int st = tex_levels_setup(a, who, tex, pyr, num_tex, height, width, channels, levels);
     if (st) return st;
     if (!uv || num_views < 1 || (num_tex != 1 && num_tex != num_views) || out_height < 0 || out_width < 0 ||
         filter_mode < kTexNearest || filter_mode > kTexMipLinear || boundary_mode < kTexWrap ||
         boundary_mode > kTexMirror || (reinterpret_cast<uintptr_t>(uv) & 7) ||
-        (reinterpret_cast<uintptr_t>(uv_da) & 15)) {
+        (reinterpret_cast<uintptr_t>(uv_da) & 15) || (reinterpret_cast<uintptr_t>(bias) & 3)) {
         char msg[160];
         snprintf(msg, sizeof(msg), "%s: bad sampling arguments", who);
         drp_set_last_error(msg);
@@ -697,6 +719,7 @@ static int tex_setup(TexArgs& a, const char* who, const float* tex, const float*
     }
     a.uv = uv;
     a.uv_da = reinterpret_cast<const float4*>(uv_da);
+    a.bias = bias;
     a.view_pix = (long long)out_height * out_width;
     a.npix = a.view_pix * num_views;
     a.filter = filter_mode;
@@ -775,11 +798,12 @@ DRP_API int drp_texture_mip_build(const float* tex, int num_tex, int height, int
 }
 
 DRP_API int drp_texture_fwd(const float* tex, const float* pyr, int num_tex, int height, int width, int channels,
-                            int levels, const float* uv, const float* uv_da, int num_views, int out_height,
-                            int out_width, int filter_mode, int boundary_mode, float* out, void* stream) {
+                            int levels, const float* uv, const float* uv_da, const float* mip_level_bias,
+                            int num_views, int out_height, int out_width, int filter_mode, int boundary_mode,
+                            float* out, void* stream) {
     drp::TexArgs a;
     int st = drp::tex_setup(a, "drp_texture_fwd", tex, pyr, num_tex, height, width, channels, levels, uv, uv_da,
-                            num_views, out_height, out_width, filter_mode, boundary_mode);
+                            mip_level_bias, num_views, out_height, out_width, filter_mode, boundary_mode);
     if (st) return st;
     if (!out) {
         drp_set_last_error("drp_texture_fwd: null output");
@@ -796,15 +820,17 @@ DRP_API int drp_texture_fwd(const float* tex, const float* pyr, int num_tex, int
 }
 
 DRP_API int drp_texture_bwd(const float* tex, const float* pyr, int num_tex, int height, int width, int channels,
-                            int levels, const float* uv, const float* uv_da, int num_views, int out_height,
-                            int out_width, int filter_mode, int boundary_mode, const float* grad_out,
-                            float* grad_tex, float* grad_pyr, float* grad_uv, float* grad_uv_da, void* stream) {
+                            int levels, const float* uv, const float* uv_da, const float* mip_level_bias,
+                            int num_views, int out_height, int out_width, int filter_mode, int boundary_mode,
+                            const float* grad_out, float* grad_tex, float* grad_pyr, float* grad_uv,
+                            float* grad_uv_da, float* grad_mip_level_bias, void* stream) {
     drp::TexArgs a;
     int st = drp::tex_setup(a, "drp_texture_bwd", tex, pyr, num_tex, height, width, channels, levels, uv, uv_da,
-                            num_views, out_height, out_width, filter_mode, boundary_mode);
+                            mip_level_bias, num_views, out_height, out_width, filter_mode, boundary_mode);
     if (st) return st;
     if (!grad_out || !grad_tex || !grad_uv || (levels > 1 && !grad_pyr) || (grad_uv_da && !uv_da) ||
-        (reinterpret_cast<uintptr_t>(grad_uv) & 7) || (reinterpret_cast<uintptr_t>(grad_uv_da) & 15)) {
+        (grad_mip_level_bias && !mip_level_bias) || (reinterpret_cast<uintptr_t>(grad_uv) & 7) ||
+        (reinterpret_cast<uintptr_t>(grad_uv_da) & 15) || (reinterpret_cast<uintptr_t>(grad_mip_level_bias) & 3)) {
         drp_set_last_error("drp_texture_bwd: bad gradient buffers");
         return DRP_STATUS_INVALID_ARGUMENT;
     }
@@ -819,6 +845,7 @@ DRP_API int drp_texture_bwd(const float* tex, const float* pyr, int num_tex, int
              aligned16(grad_pyr);
     a.grad_uv = grad_uv;
     a.grad_uv_da = reinterpret_cast<float4*>(grad_uv_da);
+    a.grad_bias = grad_mip_level_bias;
     if (a.npix > 0) {
         const long long per_block = 256 * drp::kTexPix;
         drp::tex_bwd_kernel<<<(unsigned)((a.npix + per_block - 1) / per_block), 256, 0, s>>>(a);

@@ -635,25 +635,25 @@ def texture_construct_mip(tex, max_mip_level=None, cube_mode=False):
 
 class _TextureFn(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, tex, uv, uv_da, pyr, levels, filt, bnd):
+    def forward(ctx, tex, uv, uv_da, bias, pyr, levels, filt, bnd):
         Nt, H, W, C = tex.shape
         N, h, w = uv.shape[:3]
         if pyr is None:
             pyr = _tex_build(tex, levels)
         out = torch.empty((N, h, w, C), dtype=torch.float32, device=tex.device)
         _ffi.call("drp_texture_fwd", tex.data_ptr(), pyr.data_ptr(), Nt, H, W, C, levels, uv.data_ptr(),
-                  _ptr(uv_da), N, h, w, filt, bnd, out.data_ptr(), _stream(tex.device))
-        ctx.save_for_backward(tex, uv, uv_da, pyr)
+                  _ptr(uv_da), _ptr(bias), N, h, w, filt, bnd, out.data_ptr(), _stream(tex.device))
+        ctx.save_for_backward(tex, uv, uv_da, bias, pyr)
         ctx.meta = (levels, filt, bnd)
         ctx.set_materialize_grads(False)
         return out
 
     @staticmethod
     def backward(ctx, grad_out):
-        tex, uv, uv_da, pyr = ctx.saved_tensors
+        tex, uv, uv_da, bias, pyr = ctx.saved_tensors
         levels, filt, bnd = ctx.meta
         if grad_out is None:
-            return None, None, None, None, None, None, None
+            return None, None, None, None, None, None, None, None
         Nt, H, W, C = tex.shape
         N, h, w = uv.shape[:3]
         grad_out = grad_out.contiguous()
@@ -662,11 +662,13 @@ class _TextureFn(torch.autograd.Function):
         grad_uv = torch.empty_like(uv)
         want_da = uv_da is not None and ctx.needs_input_grad[2]
         grad_da = torch.empty_like(uv_da) if want_da else None
+        want_bias = bias is not None and ctx.needs_input_grad[3]
+        grad_bias = torch.empty_like(bias) if want_bias else None
         _ffi.call("drp_texture_bwd", tex.data_ptr(), pyr.data_ptr(), Nt, H, W, C, levels, uv.data_ptr(),
-                  _ptr(uv_da), N, h, w, filt, bnd, grad_out.data_ptr(), grad_tex.data_ptr(), grad_pyr.data_ptr(),
-                  grad_uv.data_ptr(), _ptr(grad_da), _stream(tex.device))
+                  _ptr(uv_da), _ptr(bias), N, h, w, filt, bnd, grad_out.data_ptr(), grad_tex.data_ptr(),
+                  grad_pyr.data_ptr(), grad_uv.data_ptr(), _ptr(grad_da), _ptr(grad_bias), _stream(tex.device))
         return (grad_tex if ctx.needs_input_grad[0] else None, grad_uv if ctx.needs_input_grad[1] else None,
-                grad_da, None, None, None, None)
+                grad_da, grad_bias, None, None, None, None)
 
 
 def texture(tex, uv, uv_da=None, mip_level_bias=None, mip=None, filter_mode="auto", boundary_mode="wrap",
@@ -675,27 +677,27 @@ def texture(tex, uv, uv_da=None, mip_level_bias=None, mip=None, filter_mode="aut
 
     Texel (x, y) is centred at ((x + 0.5) / W, (y + 0.5) / H).  filter_mode
     'nearest', 'linear', 'linear-mipmap-nearest', 'linear-mipmap-linear' or
-    'auto' (trilinear with ``uv_da``, else bilinear); the mip-mapped modes
-    choose the level from ``uv_da`` (N, h, w, 4) = (du/dX, du/dY, dv/dX,
-    dv/dY), e.g. interpolate(..., diff_attrs=...)'s derivatives of uv.
-    boundary_mode 'wrap', 'clamp', 'zero' or 'mirror' (mirrored repeat).  ``mip`` reuses a
-    texture_construct_mip pyramid of ``tex``.  Gradients reach ``tex``
-    (through the pyramid), ``uv`` and ``uv_da`` (trilinear, where the level of
-    detail is not clamped).  Not supported: mip_level_bias and cube maps.
+    'auto' (trilinear with ``uv_da`` or ``mip_level_bias``, else bilinear);
+    the mip-mapped modes choose the level from ``uv_da`` (N, h, w, 4) =
+    (du/dX, du/dY, dv/dX, dv/dY), e.g. interpolate(..., diff_attrs=...)'s
+    derivatives of uv, plus ``mip_level_bias`` (N, h, w) when given (alone,
+    it sets the level).  boundary_mode 'wrap', 'clamp', 'zero' or 'mirror'
+    (mirrored repeat).  ``mip`` reuses a texture_construct_mip pyramid of
+    ``tex``.  Gradients reach ``tex`` (through the pyramid), ``uv``, and
+    ``uv_da`` and ``mip_level_bias`` (trilinear, where the level of detail is
+    not clamped).  Not supported: cube maps.
     """
-    if mip_level_bias is not None:
-        raise NotImplementedError("mip_level_bias is not supported")
     if boundary_mode not in _TEX_BOUNDARIES:
         if boundary_mode == "cube":
             raise NotImplementedError("cube map textures are not supported")
         raise ValueError("boundary_mode must be one of %s" % sorted(_TEX_BOUNDARIES))
     if filter_mode == "auto":
-        filter_mode = "linear-mipmap-linear" if uv_da is not None else "linear"
+        filter_mode = "linear-mipmap-linear" if uv_da is not None or mip_level_bias is not None else "linear"
     if filter_mode not in _TEX_FILTERS:
         raise ValueError("filter_mode must be 'auto' or one of %s" % sorted(_TEX_FILTERS))
     mipmapped = filter_mode.startswith("linear-mipmap")
-    if mipmapped and uv_da is None:
-        raise ValueError("filter_mode %r needs uv_da" % filter_mode)
+    if mipmapped and uv_da is None and mip_level_bias is None:
+        raise ValueError("filter_mode %r needs uv_da or mip_level_bias" % filter_mode)
     _check_tensor("tex", tex, torch.float32, (4,))
     _check_tensor("uv", uv, torch.float32, (4,), device=tex.device, last=2)
     if tex.shape[0] not in (1, uv.shape[0]):
@@ -705,6 +707,11 @@ def texture(tex, uv, uv_da=None, mip_level_bias=None, mip=None, filter_mode="aut
         if tuple(uv_da.shape[:3]) != tuple(uv.shape[:3]):
             raise RuntimeError("uv_da must have the shape of uv with 4 channels")
         uv_da = uv_da.contiguous() if mipmapped else None
+    if mip_level_bias is not None:
+        _check_tensor("mip_level_bias", mip_level_bias, torch.float32, (3,), device=tex.device)
+        if tuple(mip_level_bias.shape) != tuple(uv.shape[:3]):
+            raise RuntimeError("mip_level_bias must have the shape of uv without its last dimension")
+        mip_level_bias = mip_level_bias.contiguous() if mipmapped else None
     tex = tex.contiguous()
     pyr = None
     if mipmapped:
@@ -715,5 +722,5 @@ def texture(tex, uv, uv_da=None, mip_level_bias=None, mip=None, filter_mode="aut
             pyr = mip.pyr
     else:
         levels = 1
-    return _TextureFn.apply(tex, uv.contiguous(), uv_da, pyr, levels, _TEX_FILTERS[filter_mode],
+    return _TextureFn.apply(tex, uv.contiguous(), uv_da, mip_level_bias, pyr, levels, _TEX_FILTERS[filter_mode],
                             _TEX_BOUNDARIES[boundary_mode])

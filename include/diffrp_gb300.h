@@ -301,10 +301,11 @@ int drp_transform_points_bwd(const float* grad_out, long long num_vertices, cons
  * Sampling: uv (num_views, out_height, out_width, 2), texel (x, y) centred
  * at ((x + 0.5) / W, (y + 0.5) / H); uv_da (num_views, out_height,
  * out_width, 4) = (du/dX, du/dY, dv/dX, dv/dY), 16-byte aligned, or NULL.
- * num_tex is 1 (shared) or num_views.  filter_mode: 0 nearest, 1 linear,
- * 2 linear-mipmap-nearest, 3 linear-mipmap-linear (level of detail 0.5
- * log2 of the larger squared footprint in level-0 texels, clamped to the
- * pyramid).  boundary_mode: 0 wrap, 1 clamp, 2 zero, 3 mirror (mirrored
+ * mip_level_bias (num_views, out_height, out_width), or NULL: added to
+ * the level of detail (alone, it sets it).  num_tex is 1 (shared) or
+ * num_views.  filter_mode: 0 nearest, 1 linear, 2 linear-mipmap-nearest,
+ * 3 linear-mipmap-linear (level of detail 0.5 log2 of the larger squared
+ * footprint in level-0 texels, plus the bias, clamped to the pyramid).  boundary_mode: 0 wrap, 1 clamp, 2 zero, 3 mirror (mirrored
  * repeat: period 2 x size, the second half reversed).  Textures of at most
  * 32768 x 32768.
  */
@@ -313,19 +314,21 @@ int drp_texture_pyramid_floats(int num_tex, int height, int width, int channels,
 int drp_texture_mip_build(const float* tex, int num_tex, int height, int width, int channels, int levels,
                           float* pyr, void* stream);
 int drp_texture_fwd(const float* tex, const float* pyr, int num_tex, int height, int width, int channels,
-                    int levels, const float* uv, const float* uv_da, int num_views, int out_height, int out_width,
-                    int filter_mode, int boundary_mode, float* out, void* stream);
+                    int levels, const float* uv, const float* uv_da, const float* mip_level_bias, int num_views,
+                    int out_height, int out_width, int filter_mode, int boundary_mode, float* out, void* stream);
 /*
  * Backward of drp_texture_fwd (and of the pyramid): grad_tex (tex layout) is
  * accumulated (caller zeroes); grad_pyr is scratch of the pyramid's size
  * (zeroed and consumed by the call); grad_uv (uv layout) is written;
- * grad_uv_da (uv_da layout, may be NULL) is written -- nonzero only for
+ * grad_uv_da (uv_da layout, may be NULL) and grad_mip_level_bias
+ * (mip_level_bias layout, may be NULL) are written -- nonzero only for
  * linear-mipmap-linear where the level of detail is not clamped.
  */
 int drp_texture_bwd(const float* tex, const float* pyr, int num_tex, int height, int width, int channels,
-                    int levels, const float* uv, const float* uv_da, int num_views, int out_height, int out_width,
-                    int filter_mode, int boundary_mode, const float* grad_out, float* grad_tex, float* grad_pyr,
-                    float* grad_uv, float* grad_uv_da, void* stream);
+                    int levels, const float* uv, const float* uv_da, const float* mip_level_bias, int num_views,
+                    int out_height, int out_width, int filter_mode, int boundary_mode, const float* grad_out,
+                    float* grad_tex, float* grad_pyr, float* grad_uv, float* grad_uv_da,
+                    float* grad_mip_level_bias, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Host transport (no counterpart in the reference, which leaves transfers  */

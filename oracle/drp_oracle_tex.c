@@ -28,8 +28,9 @@
  *    array (level k: (N, H_k, W_k, C)), the layout of texture.cu's pyramid.
  *  - Level of detail from uv_da = (du/dX, du/dY, dv/dX, dv/dY):
  *    lx = (du/dX W)^2 + (dv/dX H)^2, ly = (du/dY W)^2 + (dv/dY H)^2,
- *    lambda = 0.5 log2(max(lx, ly)), clamped to [0, levels - 1] (0 when the
- *    footprint is zero or not finite).  log2 is evaluated as e + 2 t p(t^2)
+ *    lambda = 0.5 log2(max(lx, ly)) (0 when the footprint is zero or not
+ *    finite, or without uv_da) plus the pixel's mip level bias when given,
+ *    clamped to [0, levels - 1].  log2 is evaluated as e + 2 t p(t^2)
  *    / ln 2 with x = m 2^e, m in [sqrt(1/2), sqrt(2)), t = (m - 1) / (m + 1)
  *    and the atanh series p = 1 + t^2/3 + t^4/5 + t^6/7 + t^8/9 (relative
  *    error below 2e-8), so that the CPU and the GPU round it identically.
@@ -189,26 +190,32 @@ static inline real tex_log2(real x) {
 typedef struct {
     int l0, l1;
     real f;           /* weight of l1 */
-    int interior;     /* lambda strictly inside (0, levels - 1): uv_da gradient flows */
+    int interior;     /* lambda strictly inside (0, levels - 1): lambda's gradient flows */
+    int da_active;    /* lambda has the footprint term (uv_da given, footprint > 0) */
     real r2;
     int use_x;        /* the X footprint is the larger */
     real ax, ay, bx, by;
 } lod_t;
 
-static void tex_lod(const real* da, int H, int W, int levels, int filter, lod_t* L) {
+/* bias: the pixel's mip level bias, added to lambda (NULL: none). */
+static void tex_lod(const real* da, const real* bias, int H, int W, int levels, int filter, lod_t* L) {
     memset(L, 0, sizeof(*L));
-    if (!da || levels <= 1 || filter < TEX_MIP_NEAREST) return;
-    L->ax = da[0] * (real)W;
-    L->bx = da[1] * (real)W;
-    L->ay = da[2] * (real)H;
-    L->by = da[3] * (real)H;
-    const real lx = L->ax * L->ax + L->ay * L->ay;
-    const real ly = L->bx * L->bx + L->by * L->by;
-    L->use_x = lx >= ly;
-    const real r2 = L->use_x ? lx : ly;
-    L->r2 = r2;
+    if ((!da && !bias) || levels <= 1 || filter < TEX_MIP_NEAREST) return;
     real lam = 0;
-    if (r2 > 0 && isfinite(r2)) lam = (real)0.5 * tex_log2(r2);
+    if (da) {
+        L->ax = da[0] * (real)W;
+        L->bx = da[1] * (real)W;
+        L->ay = da[2] * (real)H;
+        L->by = da[3] * (real)H;
+        const real lx = L->ax * L->ax + L->ay * L->ay;
+        const real ly = L->bx * L->bx + L->by * L->by;
+        L->use_x = lx >= ly;
+        const real r2 = L->use_x ? lx : ly;
+        L->r2 = r2;
+        L->da_active = r2 > 0 && isfinite(r2);
+        if (L->da_active) lam = (real)0.5 * tex_log2(r2);
+    }
+    if (bias) lam = lam + *bias;
     const real top = (real)(levels - 1);
     L->interior = lam > 0 && lam < top;
     if (!(lam > 0)) lam = 0;
@@ -305,8 +312,8 @@ static inline real bilin_value(const real* lvl, const bilin_t* B, int C, int c) 
 
 /* out (N, h, w, C).  tex pyramid per texture (Nt = 1 or N). */
 ORC_EXPORT void orc_tex_fwd(const real* tex, const real* pyr, int Nt, int H, int W, int C, int levels,
-                            const real* uv, const real* uv_da, int N, int h, int w, int filter, int boundary,
-                            real* out) {
+                            const real* uv, const real* uv_da, const real* bias, int N, int h, int w, int filter,
+                            int boundary, real* out) {
     const long npix = (long)h * w;
 #pragma omp parallel for schedule(static)
     for (long p = 0; p < (long)N * npix; ++p) {
@@ -325,7 +332,7 @@ ORC_EXPORT void orc_tex_fwd(const real* tex, const real* pyr, int Nt, int H, int
             continue;
         }
         lod_t L;
-        tex_lod(uv_da ? uv_da + 4 * p : NULL, H, W, levels, filter, &L);
+        tex_lod(uv_da ? uv_da + 4 * p : NULL, bias ? bias + p : NULL, H, W, levels, filter, &L);
         int h0, w0, h1, w1;
         level_dims(H, W, L.l0, &h0, &w0);
         level_dims(H, W, L.l1, &h1, &w1);
@@ -368,11 +375,12 @@ static void bilin_bwd(const real* lvl, real* glvl, const bilin_t* B, int w, int 
 }
 
 /* grad_tex (level 0) and grad_pyr (levels 1 .., zeroed by the caller)
- * accumulate; grad_uv (N, h, w, 2) and grad_uv_da (may be null) are
- * written.  Single-threaded (texel gradients are shared). */
+ * accumulate; grad_uv (N, h, w, 2), grad_uv_da and grad_bias (may be null)
+ * are written.  Single-threaded (texel gradients are shared). */
 ORC_EXPORT void orc_tex_bwd(const real* tex, const real* pyr, int Nt, int H, int W, int C, int levels,
-                            const real* uv, const real* uv_da, int N, int h, int w, int filter, int boundary,
-                            const real* grad_out, real* grad_tex, real* grad_pyr, real* grad_uv, real* grad_uv_da) {
+                            const real* uv, const real* uv_da, const real* bias, int N, int h, int w, int filter,
+                            int boundary, const real* grad_out, real* grad_tex, real* grad_pyr, real* grad_uv,
+                            real* grad_uv_da, real* grad_bias) {
     const long npix = (long)h * w;
     for (long p = 0; p < (long)N * npix; ++p) {
         const int n = (int)(p / npix), tn = Nt == 1 ? 0 : n;
@@ -382,6 +390,7 @@ ORC_EXPORT void orc_tex_bwd(const real* tex, const real* pyr, int Nt, int H, int
         const real* g = grad_out + p * C;
         real gu = 0, gv = 0;
         if (grad_uv_da) memset(grad_uv_da + 4 * p, 0, 4 * sizeof(real));
+        if (grad_bias) grad_bias[p] = 0;
         if (filter == TEX_NEAREST) {
 #ifdef REAL_IS_DOUBLE
             const int ix = (int)floor(tex_coord(u, W) + (real)0.5), iy = (int)floor(tex_coord(v, H) + (real)0.5);
@@ -397,7 +406,7 @@ ORC_EXPORT void orc_tex_bwd(const real* tex, const real* pyr, int Nt, int H, int
         }
         lod_t L;
         const real* da = uv_da ? uv_da + 4 * p : NULL;
-        tex_lod(da, H, W, levels, filter, &L);
+        tex_lod(da, bias ? bias + p : NULL, H, W, levels, filter, &L);
         int h0, w0, h1, w1;
         level_dims(H, W, L.l0, &h0, &w0);
         level_dims(H, W, L.l1, &h1, &w1);
@@ -412,18 +421,21 @@ ORC_EXPORT void orc_tex_bwd(const real* tex, const real* pyr, int Nt, int H, int
         bilin_bwd(P0, G0, &B0, w0, h0, C, g, f > 0 ? (real)1 - f : (real)1, &gu, &gv);
         if (f > 0) {
             bilin_bwd(P1, G1, &B1, w1, h1, C, g, f, &gu, &gv);
-            if (grad_uv_da && L.interior) {
-                real dl = 0;
+            if ((grad_uv_da || grad_bias) && L.interior) {
+                real dl = 0; /* d out / d lambda . grad_out */
                 for (int c = 0; c < C; ++c) dl += g[c] * (bilin_value(P1, &B1, C, c) - bilin_value(P0, &B0, C, c));
-                /* lambda = 0.5 log2(r2): d lambda / d r2 = 0.5 / (r2 ln 2) */
-                const real dr2 = dl * ((real)0.72134752f / L.r2);
-                real* gd = grad_uv_da + 4 * p;
-                if (L.use_x) {
-                    gd[0] = dr2 * (real)2 * L.ax * (real)W;
-                    gd[2] = dr2 * (real)2 * L.ay * (real)H;
-                } else {
-                    gd[1] = dr2 * (real)2 * L.bx * (real)W;
-                    gd[3] = dr2 * (real)2 * L.by * (real)H;
+                if (grad_bias) grad_bias[p] = dl;
+                if (grad_uv_da && L.da_active) {
+                    /* lambda = 0.5 log2(r2) + bias: d lambda / d r2 = 0.5 / (r2 ln 2) */
+                    const real dr2 = dl * ((real)0.72134752f / L.r2);
+                    real* gd = grad_uv_da + 4 * p;
+                    if (L.use_x) {
+                        gd[0] = dr2 * (real)2 * L.ax * (real)W;
+                        gd[2] = dr2 * (real)2 * L.ay * (real)H;
+                    } else {
+                        gd[1] = dr2 * (real)2 * L.bx * (real)W;
+                        gd[3] = dr2 * (real)2 * L.by * (real)H;
+                    }
                 }
             }
         }

@@ -78,11 +78,11 @@ def load(precision="f32"):
         lib.orc_tex_mip_build.restype = None
         lib.orc_tex_mip_bwd.argtypes = [_p, _c_int, _c_int, _c_int, _c_int, _c_int, _p]
         lib.orc_tex_mip_bwd.restype = None
-        lib.orc_tex_fwd.argtypes = [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _c_int, _c_int, _c_int,
-                                    _c_int, _c_int, _p]
+        lib.orc_tex_fwd.argtypes = [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _p, _c_int, _c_int,
+                                    _c_int, _c_int, _c_int, _p]
         lib.orc_tex_fwd.restype = None
-        lib.orc_tex_bwd.argtypes = [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _c_int, _c_int, _c_int,
-                                    _c_int, _c_int, _p, _p, _p, _p, _p]
+        lib.orc_tex_bwd.argtypes = [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _p, _c_int, _c_int,
+                                    _c_int, _c_int, _c_int, _p, _p, _p, _p, _p, _p]
         lib.orc_tex_bwd.restype = None
         for name in ["orc_raster_ids", "orc_shade", "orc_raster_bwd", "orc_interp_fwd", "orc_interp_bwd",
                      "orc_interp_sparse_fwd", "orc_topology", "orc_aa_fwd", "orc_aa_bwd"]:
@@ -399,7 +399,10 @@ def tex_mip_bwd(grad_tex, grad_pyr, levels, precision="f32"):
     return out
 
 
-def tex_fwd(tex, pyr, levels, uv, uv_da=None, filter_mode="linear", boundary_mode="wrap", precision="f32"):
+def tex_fwd(tex, pyr, levels, uv, uv_da=None, filter_mode="linear", boundary_mode="wrap", precision="f32",
+            bias=None):
+    """(N, h, w, C) samples; bias: the per-pixel mip level bias (N, h, w)
+    added to the level of detail, or None."""
     lib, dt = load(precision), _dt(precision)
     tex = np.ascontiguousarray(tex, dt)
     pyr = np.ascontiguousarray(pyr, dt)
@@ -407,15 +410,19 @@ def tex_fwd(tex, pyr, levels, uv, uv_da=None, filter_mode="linear", boundary_mod
     Nt, H, W, C = tex.shape
     N, h, w, _ = uv.shape
     da = None if uv_da is None else np.ascontiguousarray(uv_da, dt)
+    b = None if bias is None else np.ascontiguousarray(bias, dt)
     out = np.zeros((N, h, w, C), dt)
-    lib.orc_tex_fwd(_ptr(tex), _ptr(pyr), Nt, H, W, C, levels, _ptr(uv), None if da is None else _ptr(da), N, h, w,
-                    TEX_FILTERS[filter_mode], TEX_BOUNDARIES[boundary_mode], _ptr(out))
+    lib.orc_tex_fwd(_ptr(tex), _ptr(pyr), Nt, H, W, C, levels, _ptr(uv), None if da is None else _ptr(da),
+                    None if b is None else _ptr(b), N, h, w, TEX_FILTERS[filter_mode], TEX_BOUNDARIES[boundary_mode],
+                    _ptr(out))
     return out
 
 
-def tex_bwd(tex, pyr, levels, uv, uv_da, grad_out, filter_mode="linear", boundary_mode="wrap", precision="f32"):
-    """(grad_tex, grad_pyr, grad_uv, grad_uv_da or None); grad_tex holds the
-    level-0 share only (tex_mip_bwd adds the pyramid's)."""
+def tex_bwd(tex, pyr, levels, uv, uv_da, grad_out, filter_mode="linear", boundary_mode="wrap", precision="f32",
+            bias=None):
+    """(grad_tex, grad_pyr, grad_uv, grad_uv_da or None), plus grad_bias when
+    ``bias`` is given; grad_tex holds the level-0 share only (tex_mip_bwd
+    adds the pyramid's)."""
     lib, dt = load(precision), _dt(precision)
     tex = np.ascontiguousarray(tex, dt)
     pyr = np.ascontiguousarray(pyr, dt)
@@ -424,11 +431,16 @@ def tex_bwd(tex, pyr, levels, uv, uv_da, grad_out, filter_mode="linear", boundar
     Nt, H, W, C = tex.shape
     N, h, w, _ = uv.shape
     da = None if uv_da is None else np.ascontiguousarray(uv_da, dt)
+    b = None if bias is None else np.ascontiguousarray(bias, dt)
     gtex = np.zeros_like(tex)
     gpyr = np.zeros_like(pyr)
     guv = np.zeros_like(uv)
     gda = None if da is None else np.zeros_like(da)
-    lib.orc_tex_bwd(_ptr(tex), _ptr(pyr), Nt, H, W, C, levels, _ptr(uv), None if da is None else _ptr(da), N, h, w,
-                    TEX_FILTERS[filter_mode], TEX_BOUNDARIES[boundary_mode], _ptr(g), _ptr(gtex), _ptr(gpyr),
-                    _ptr(guv), None if gda is None else _ptr(gda))
+    gb = None if b is None else np.zeros_like(b)
+    lib.orc_tex_bwd(_ptr(tex), _ptr(pyr), Nt, H, W, C, levels, _ptr(uv), None if da is None else _ptr(da),
+                    None if b is None else _ptr(b), N, h, w, TEX_FILTERS[filter_mode], TEX_BOUNDARIES[boundary_mode],
+                    _ptr(g), _ptr(gtex), _ptr(gpyr), _ptr(guv), None if gda is None else _ptr(gda),
+                    None if gb is None else _ptr(gb))
+    if b is not None:
+        return gtex, gpyr, guv, gda, gb
     return gtex, gpyr, guv, gda

@@ -130,12 +130,16 @@ def test_texture_levels_and_validation(lib):
     # levels above the texture's pyramid
     assert lib.drp_texture_mip_build(p, 1, 8, 8, 4, 5, p, None) == 1
     # num_tex neither 1 nor num_views
-    assert lib.drp_texture_fwd(p, p, 3, 8, 8, 4, 1, p, None, 2, 4, 4, 1, 0, p, None) == 1
+    assert lib.drp_texture_fwd(p, p, 3, 8, 8, 4, 1, p, None, None, 2, 4, 4, 1, 0, p, None) == 1
     # filter and boundary codes out of range
-    assert lib.drp_texture_fwd(p, p, 1, 8, 8, 4, 1, p, None, 1, 4, 4, 4, 0, p, None) == 1
-    assert lib.drp_texture_fwd(p, p, 1, 8, 8, 4, 1, p, None, 1, 4, 4, 1, 4, p, None) == 1
+    assert lib.drp_texture_fwd(p, p, 1, 8, 8, 4, 1, p, None, None, 1, 4, 4, 4, 0, p, None) == 1
+    assert lib.drp_texture_fwd(p, p, 1, 8, 8, 4, 1, p, None, None, 1, 4, 4, 1, 4, p, None) == 1
     # uv not 8-byte aligned
-    assert lib.drp_texture_fwd(p, p, 1, 8, 8, 4, 1, ctypes.c_void_p(260), None, 1, 4, 4, 1, 0, p, None) == 1
+    assert lib.drp_texture_fwd(p, p, 1, 8, 8, 4, 1, ctypes.c_void_p(260), None, None, 1, 4, 4, 1, 0, p, None) == 1
+    # mip level bias not 4-byte aligned
+    assert lib.drp_texture_fwd(p, p, 1, 8, 8, 4, 1, p, None, ctypes.c_void_p(258), 1, 4, 4, 3, 0, p, None) == 1
     # uv_da gradient without uv_da
-    assert lib.drp_texture_bwd(p, p, 1, 8, 8, 4, 1, p, None, 1, 4, 4, 1, 0, p, p, p, p, p, None) == 1
+    assert lib.drp_texture_bwd(p, p, 1, 8, 8, 4, 1, p, None, None, 1, 4, 4, 1, 0, p, p, p, p, p, None, None) == 1
+    # mip level bias gradient without a bias
+    assert lib.drp_texture_bwd(p, p, 1, 8, 8, 4, 1, p, None, None, 1, 4, 4, 3, 0, p, p, p, p, None, p, None) == 1
     assert _ffi.kernel_launches() == before

@@ -134,3 +134,61 @@ def test_gradients_match_central_differences(filter_mode, boundary):
     for idx in [(0, 0, 1, 0), (1, 2, 2, 1), (0, 2, 3, 2), (1, 0, 0, 3)]:
         fd = _central(lambda d: loss(tex, uv, d), da, idx, 1e-8)
         assert abs(gda[idx] - fd) <= 1e-4 * max(1.0, abs(fd)), ("uv_da", idx, gda[idx], fd)
+
+
+def test_mip_level_bias_shifts_the_level():
+    """The per-pixel mip level bias adds to the level of detail (alone it
+    sets it), clamped to the pyramid: a level-index pyramid (level k holds
+    k) returns lambda itself under trilinear filtering."""
+    H = W = 64
+    L = O.tex_levels(H, W)
+    tex = np.zeros((1, H, W, 1), np.float32)
+    pyr = O.tex_mip_build(tex, L)
+    off = 0
+    for k in range(1, L):
+        n = max(H >> k, 1) * max(W >> k, 1)
+        pyr[off:off + n] = k
+        off += n
+    rng = np.random.default_rng(5)
+    n = 200
+    uv = np.full((1, 1, n, 2), 0.5, np.float32)
+    bias = rng.uniform(-2.0, L + 1.0, (1, 1, n)).astype(np.float32)
+    got = O.tex_fwd(tex, pyr, L, uv, None, "linear-mipmap-linear", "clamp", bias=bias)[0, 0, :, 0]
+    np.testing.assert_allclose(got, np.clip(bias[0, 0], 0, L - 1), rtol=0, atol=2e-6)
+    lam = rng.uniform(0.0, 3.0, n)
+    da = np.zeros((1, 1, n, 4), np.float32)
+    da[0, 0, :, 0] = 2.0 ** lam / W
+    bias = rng.uniform(-1.0, 2.0, (1, 1, n)).astype(np.float32)
+    got = O.tex_fwd(tex, pyr, L, uv, da, "linear-mipmap-linear", "clamp", bias=bias)[0, 0, :, 0]
+    ref = np.array([0.5 * math.log2(float(np.float32(s) * W) ** 2) for s in da[0, 0, :, 0]]) + bias[0, 0]
+    np.testing.assert_allclose(got, np.clip(ref, 0, L - 1), rtol=0, atol=3e-6)
+
+
+@pytest.mark.parametrize("with_da", [False, True])
+def test_mip_level_bias_gradient_matches_central_differences(with_da):
+    H, W, C = 12, 10, 3
+    L = O.tex_levels(H, W)
+    rng = np.random.default_rng(8)
+    tex = rng.uniform(-1, 1, (1, H, W, C))
+    uv = rng.uniform(-0.3, 1.3, (2, 3, 4, 2))
+    da = (rng.uniform(-0.3, 0.3, (2, 3, 4, 4)) / W * 2.0 ** rng.uniform(0.3, 1.5, (2, 3, 4, 1))) if with_da else None
+    bias = rng.uniform(0.2, 2.3, (2, 3, 4))
+    gout = rng.normal(size=(2, 3, 4, C))
+
+    def loss(b):
+        pyr = O.tex_mip_build(tex, L, "f64")
+        return float((O.tex_fwd(tex, pyr, L, uv, da, "linear-mipmap-linear", "wrap", "f64", bias=b) * gout).sum())
+
+    pyr = O.tex_mip_build(tex, L, "f64")
+    res = O.tex_bwd(tex, pyr, L, uv, da, gout, "linear-mipmap-linear", "wrap", "f64", bias=bias)
+    gb = res[4]
+    for idx in [(0, 0, 0), (1, 2, 3), (0, 1, 2), (1, 0, 1)]:
+        fd = _central(loss, bias, idx, 1e-7)
+        assert abs(gb[idx] - fd) <= 1e-5 * max(1.0, abs(fd)), (idx, gb[idx], fd)
+    if with_da:  # uv_da's gradient with the bias in lambda
+        def loss_da(d):
+            return float((O.tex_fwd(tex, pyr, L, uv, d, "linear-mipmap-linear", "wrap", "f64", bias=bias)
+                          * gout).sum())
+        for idx in [(0, 0, 1, 0), (1, 2, 2, 1)]:
+            fd = _central(loss_da, da, idx, 1e-8)
+            assert abs(res[3][idx] - fd) <= 1e-4 * max(1.0, abs(fd)), ("uv_da", idx, res[3][idx], fd)

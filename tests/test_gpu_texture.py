@@ -122,9 +122,9 @@ def test_interpolated_derivatives_drive_the_level(cuda_lib):
 def test_argument_errors(cuda_lib):
     from diffrp_gb300 import nvdr as dr
     tex, uv, da = _case(1, 1, 8, 8, 1, 4, 4)
-    with pytest.raises(NotImplementedError):
-        dr.texture(_t(tex), _t(uv), _t(da), mip_level_bias=_t(da[..., 0]))
-    with pytest.raises(ValueError):
+    with pytest.raises(RuntimeError):  # the bias takes uv's shape without its last dimension
+        dr.texture(_t(tex), _t(uv), _t(da), mip_level_bias=_t(da[..., :2]))
+    with pytest.raises(ValueError):  # mip-mapped without uv_da or a bias
         dr.texture(_t(tex), _t(uv), filter_mode="linear-mipmap-linear")
     with pytest.raises(NotImplementedError):
         dr.texture(_t(tex), _t(uv), boundary_mode="cube")
@@ -388,3 +388,37 @@ def test_session_gltf_material_with_derivatives(cuda_lib):
         images[deriv] = img.detach().cpu().numpy()[0]
     far_plain, far_mip = images[False][25:38, 30:98, 0], images[True][25:38, 30:98, 0]
     assert far_mip.std() < 0.5 * far_plain.std()
+
+
+@pytest.mark.parametrize("with_da", [False, True])
+@pytest.mark.parametrize("filter_mode", ["linear-mipmap-nearest", "linear-mipmap-linear"])
+def test_mip_level_bias(cuda_lib, with_da, filter_mode):
+    """nvdiffrast's mip_level_bias: added to the level of detail from uv_da
+    (alone, it sets it).  Forward bit-exact against the oracle; gradients to
+    the texture, uv, uv_da and the bias within 1e-5 of the largest."""
+    from diffrp_gb300 import nvdr as dr
+    H, W, C = 32, 24, 4
+    tex, uv, da = _case(1, 2, H, W, C, 17, 13, seed=6)
+    rng = np.random.default_rng(10)
+    bias = rng.uniform(-1.5, 5.5, (2, 17, 13)).astype(np.float32)
+    gout = rng.normal(size=(2, 17, 13, C)).astype(np.float32)
+    tex_t, uv_t, b_t = _t(tex).requires_grad_(True), _t(uv).requires_grad_(True), _t(bias).requires_grad_(True)
+    da_t = _t(da).requires_grad_(True) if with_da else None
+    out = dr.texture(tex_t, uv_t, da_t, mip_level_bias=b_t, filter_mode=filter_mode, boundary_mode="wrap")
+    L = O.tex_levels(H, W)
+    pyr = O.tex_mip_build(tex, L)
+    da_np = da if with_da else None
+    ref = O.tex_fwd(tex, pyr, L, uv, da_np, filter_mode, "wrap", bias=bias)
+    np.testing.assert_array_equal(out.detach().cpu().numpy(), ref)
+    out.backward(_t(gout))
+    g0, gpyr, guv, gda, gb = O.tex_bwd(tex, pyr, L, uv, da_np, gout, filter_mode, "wrap", bias=bias)
+    gtex = O.tex_mip_bwd(g0, gpyr, L)
+    pairs = [(tex_t.grad, gtex, "tex"), (uv_t.grad, guv, "uv"), (b_t.grad, gb, "bias")]
+    if with_da:
+        pairs.append((da_t.grad, gda, "uv_da"))
+    for got, want, what in pairs:
+        got = got.cpu().numpy()
+        scale = max(float(np.abs(want).max()), 1e-30)
+        assert float(np.abs(got - want).max()) <= 1e-5 * scale, what
+    if filter_mode == "linear-mipmap-linear":
+        assert np.abs(gb).max() > 0
