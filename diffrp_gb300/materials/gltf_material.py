@@ -16,10 +16,9 @@ from typing import Literal, Optional
 
 import torch
 
-from .. import nvdr as dr
 from ..utils.shader_ops import fsa, ones_like_vec
 from .base_material import SurfaceMaterial, SurfaceOutputStandard
-from .textured_material import sample_texture
+from .textured_material import PyramidCache, sample_texture
 
 __all__ = ["GLTFSampler", "GLTFMaterial"]
 
@@ -38,16 +37,7 @@ class GLTFSampler:
     image: torch.Tensor
     wrap_mode: Literal['repeat', 'clamp', 'mirror'] = 'repeat'
     interpolation: Literal['point', 'linear'] = 'linear'
-    _mip: Optional[object] = field(default=None, init=False, repr=False, compare=False)
-
-    def _pyramid(self):
-        # built once for a fixed image; a trained image (requires_grad) gets
-        # its pyramid rebuilt inside every sample so that gradients reach it
-        if self.image.requires_grad:
-            return None
-        if self._mip is None or self._mip.tex.data_ptr() != self.image.data_ptr():
-            self._mip = dr.texture_construct_mip(self.image[None].contiguous())
-        return self._mip
+    _pyramids: PyramidCache = field(default_factory=PyramidCache, init=False, repr=False, compare=False)
 
     def sample(self, uv: torch.Tensor, uv_da: Optional[torch.Tensor] = None) -> torch.Tensor:
         """(..., C) at uv (..., 2), (0, 0) at the image's bottom-left corner;
@@ -63,7 +53,7 @@ class GLTFSampler:
             return sample_texture(self.image, uv, None, wrap, filter_mode='nearest')
         if uv_da is None:
             return sample_texture(self.image, uv, None, wrap, filter_mode='linear')
-        return sample_texture(self.image, uv, uv_da, wrap, filter_mode='linear-mipmap-linear', mip=self._pyramid())
+        return sample_texture(self.image, uv, uv_da, wrap, filter_mode='linear-mipmap-linear', mip=self._pyramids.get(self.image))
 
 
 @dataclass

@@ -9,14 +9,35 @@ derivatives (``SurfaceInput.uv_da``, from a session with
 ``derivatives=True``), so that minified textures are filtered instead of
 aliased.  Without derivatives it samples bilinearly, as sample2d does.
 """
+import weakref
+
 import torch
 
 from .. import nvdr as dr
 from .base_material import SurfaceMaterial, SurfaceOutputStandard
 
-__all__ = ["sample_texture", "TexturedMaterial"]
+__all__ = ["sample_texture", "TexturedMaterial", "PyramidCache"]
 
 _WRAP = {"repeat": "wrap", "clamp": "clamp", "zero": "zero", "mirror": "mirror"}
+
+
+class PyramidCache:
+    """The mip pyramid of a material's fixed image, built on first use and
+    rebuilt when the image is another tensor or was modified in place (its
+    version counter moved).  A trained image (requires_grad) gets None:
+    texture() then builds the pyramid inside autograd, so that gradients
+    reach the image."""
+
+    def __init__(self):
+        self._ref, self._version, self._mip = None, None, None
+
+    def get(self, image):
+        if image.requires_grad:
+            return None
+        if self._ref is None or self._ref() is not image or self._version != image._version:
+            self._mip = dr.texture_construct_mip(image[None].contiguous())
+            self._ref, self._version = weakref.ref(image), image._version
+        return self._mip
 
 
 def sample_texture(image, uv, uv_da=None, wrap="repeat", filter_mode="auto", mip=None):
@@ -55,23 +76,14 @@ class TexturedMaterial(SurfaceMaterial):
         self.image = base_color_texture
         self.factor = base_color_factor
         self.wrap = wrap
-        self._mip = None
-
-    def _pyramid(self):
-        # the image's pyramid, built once; a trained image (requires_grad)
-        # rebuilds it in every texture() call so that gradients reach it
-        if self.image.requires_grad:
-            return None
-        if self._mip is None:
-            self._mip = dr.texture_construct_mip(self.image[None].contiguous())
-        return self._mip
+        self._pyramids = PyramidCache()
 
     def shade(self, su, si):
         try:
             uv_da = si.uv_da
         except RuntimeError:
             uv_da = None
-        rgba = sample_texture(self.image, si.uv, uv_da, self.wrap, mip=self._pyramid() if uv_da is not None else None)
+        rgba = sample_texture(self.image, si.uv, uv_da, self.wrap, mip=self._pyramids.get(self.image) if uv_da is not None else None)
         rgb = rgba[..., :3] * si.color[..., :3]
         if self.factor is not None:
             rgb = rgb * self.factor[..., :3]

@@ -422,3 +422,20 @@ def test_mip_level_bias(cuda_lib, with_da, filter_mode):
         assert float(np.abs(got - want).max()) <= 1e-5 * scale, what
     if filter_mode == "linear-mipmap-linear":
         assert np.abs(gb).max() > 0
+
+
+def test_material_pyramid_follows_the_image(cuda_lib):
+    """A sampler's cached pyramid is rebuilt when its image is modified in
+    place or replaced, so trilinear samples always see the current image."""
+    from diffrp_gb300.materials import GLTFSampler
+    rng = np.random.default_rng(12)
+    image = _t(rng.uniform(0, 1, (16, 16, 3)).astype(np.float32))
+    uv = _t(rng.uniform(0, 1, (64, 2)).astype(np.float32))
+    da = _t(np.full((64, 4), 0.2, np.float32))  # minified: coarse levels
+    s = GLTFSampler(image, "repeat")
+    first = s.sample(uv, da)
+    with torch.no_grad():
+        image.mul_(0.5)
+    torch.testing.assert_close(s.sample(uv, da), 0.5 * first, rtol=1e-6, atol=1e-6)
+    s.image = torch.zeros_like(image)
+    assert float(s.sample(uv, da).abs().max()) == 0.0
