@@ -9,7 +9,12 @@
  * diffrp's materials (diffrp/materials/gltf_material.py:47-48 through
  * diffrp/utils/shader_ops.py:224 sample2d, which samples without mipmaps).
  * nvdiffrast itself is not in the reference tree, so these rules are this
- * project's, stated once here and in the CUDA kernels (texture.cu):
+ * project's, stated once here and in the CUDA kernels (texture.cu).  The
+ * restatement is pinned by tests/test_cpu_texture.py against independent
+ * code -- torch's grid_sample for bilinear clamp / zero / mirror sampling, a
+ * numpy reshape-mean for the pyramid, math.log2 for the level of detail --
+ * and against float64 central differences for every gradient; parity with
+ * nvdiffrast's own outputs is unpinned (absent here).
  *
  *  - Texture (N, H, W, C), texel (x, y) centred at ((x + 0.5) / W,
  *    (y + 0.5) / H) in uv; row y = 0 at v = 0.
