@@ -598,19 +598,21 @@ constexpr int kTexMaxChain = 15;  // pyramid levels above level 0 of a texture o
 
 // The cascade of one channel group (V: float or float4) of level-1 texel
 // (x1, y1): every level's load issued first (levels above the top read the
-// top again; registers only), then the evaluation from the top.
-template <typename V>
+// top again; registers only), then the evaluation from the top.  MAXC: the
+// longest chain the launch holds (top <= MAXC), so that a pyramid of few
+// levels keeps few registers.
+template <typename V, int MAXC>
 __device__ __forceinline__ V mip_chain(const TexArgs& a, int n, int x1, int y1, int top, int c) {
-    V g[kTexMaxChain];
+    V g[MAXC];
 #pragma unroll
-    for (int k = 1; k <= kTexMaxChain; ++k) {  // level k holds (x1, y1)'s ancestor (x1 >> (k - 1), y1 >> (k - 1))
+    for (int k = 1; k <= MAXC; ++k) {  // level k holds (x1, y1)'s ancestor (x1 >> (k - 1), y1 >> (k - 1))
         const int j = k < top ? k : top;
         const float* G = a.grad_pyr + a.lofs[j] + (long long)n * a.lh[j] * a.lw[j] * a.C;
         g[k - 1] = *reinterpret_cast<const V*>(G + ((long long)(y1 >> (j - 1)) * a.lw[j] + (x1 >> (j - 1))) * a.C + c);
     }
     V t = g[0];
 #pragma unroll
-    for (int k = kTexMaxChain; k >= 1; --k) {
+    for (int k = MAXC; k >= 1; --k) {
         if (k > top) continue;
         if (k == top) {
             t = g[k - 1];
@@ -629,6 +631,7 @@ __device__ __forceinline__ V mip_chain(const TexArgs& a, int n, int x1, int y1, 
 // parents and evaluates that cascade from the top (t_{k-1} = G_{k-1} +
 // c_{k-1} t_k, the operations of one pass per level in the same order), then
 // adds c_0 t_1 into the gradients of its (up to) four level-0 texels.
+template <int MAXC>
 __global__ void __launch_bounds__(256) tex_mip_chain_kernel(TexArgs a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int w1 = a.lw[1], h1 = a.lh[1];
@@ -643,7 +646,7 @@ __global__ void __launch_bounds__(256) tex_mip_chain_kernel(TexArgs a) {
     const int C = a.C;
     float* g0 = a.grad_tex + (long long)n * a.H * a.W * C;
     if (a.vec4) {
-        const float4 t = vscale(m, mip_chain<float4>(a, n, x1, y1, top, 0));
+        const float4 t = vscale(m, mip_chain<float4, MAXC>(a, n, x1, y1, top, 0));
         for (int dy = 0; dy < 2; ++dy)
             for (int dx = 0; dx < 2; ++dx) {
                 const int x = 2 * x1 + dx, y = 2 * y1 + dy;
@@ -653,7 +656,7 @@ __global__ void __launch_bounds__(256) tex_mip_chain_kernel(TexArgs a) {
             }
     } else {
         for (int c = 0; c < C; ++c) {
-            const float t = m * mip_chain<float>(a, n, x1, y1, top, c);
+            const float t = m * mip_chain<float, MAXC>(a, n, x1, y1, top, c);
             for (int dy = 0; dy < 2; ++dy)
                 for (int dx = 0; dx < 2; ++dx) {
                     const int x = 2 * x1 + dx, y = 2 * y1 + dy;
@@ -853,7 +856,13 @@ DRP_API int drp_texture_bwd(const float* tex, const float* pyr, int num_tex, int
     }
     if (levels > 1 && a.filter >= drp::kTexMipNearest) {
         const long long n = (long long)num_tex * a.lh[1] * a.lw[1];
-        drp::tex_mip_chain_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+        const unsigned grid = (unsigned)((n + 255) / 256);
+        if (levels - 1 <= 7)
+            drp::tex_mip_chain_kernel<7><<<grid, 256, 0, s>>>(a);
+        else if (levels - 1 <= 11)
+            drp::tex_mip_chain_kernel<11><<<grid, 256, 0, s>>>(a);
+        else
+            drp::tex_mip_chain_kernel<drp::kTexMaxChain><<<grid, 256, 0, s>>>(a);
         drp_note_launch();
     }
     return drp_check_launch("drp_texture_bwd");

@@ -63,8 +63,9 @@ def test_forward_bit_exact(cuda_lib, filter_mode, boundary, Nt):
 
 
 # (textures, H, W, C): four channels take the float4 path; odd sizes, a
-# size-1 axis and per-view textures the per-channel one
-GRAD_SHAPES = [(1, 32, 24, 4), (2, 37, 53, 3), (1, 1, 9, 2), (2, 20, 44, 4)]
+# size-1 axis and per-view textures the per-channel one; 3 x 4099 has 13
+# levels (the pyramid gradient's longest chain variant)
+GRAD_SHAPES = [(1, 32, 24, 4), (2, 37, 53, 3), (1, 1, 9, 2), (2, 20, 44, 4), (1, 3, 4099, 2)]
 
 
 @pytest.mark.parametrize("shape", GRAD_SHAPES)
