@@ -638,9 +638,9 @@ def run_texture(dev, steps, warmup, cpu=True):
         el = time.perf_counter() - t0
         res["cpu_baseline"] = {"value": rows * n / el / 1e6, "unit": UNIT, "cores": O.default_threads(),
                                "kind": "port", "sample": "%d rows of the 1024x1024 output, fwd+bwd with the pyramid "
-                                                         "of the full texture, in %.2f s (forward and pyramid on "
-                                                         "the threads given, backward on one: its texel sums are "
-                                                         "shared)" % (rows, el)}
+                                                         "of the full texture, in %.2f s (the sampling forward on "
+                                                         "the threads given; the pyramid and the backward, whose "
+                                                         "texel sums are shared, on one)" % (rows, el)}
     return res
 
 
